@@ -1,0 +1,1244 @@
+/*
+ * GB300 (sm_103a) Crank-Nicolson step of GaDE: matrix-free operator,
+ * block-LU preconditioner, fused BiCGSTAB.  Exposes the C ABI of
+ * include/gade.h.
+ *
+ * Operator (replaces assembly + SpMV, tools/gpu_solver.cu:50-135 and
+ * tools/gpu_sparse.c:267-313).  Block (r,c) of S + H(t) is
+ *   delta_rc [S(k_r) + i h dt/2 h0(k_r)]
+ *   + sum_l H0l(r,c) (pg_l0 + k_r pg_l1 + k_c pg_l2 + k_r k_c pg_l3)
+ *          + H1l(r,c) (pgt_l0 + k_c pgt_l1 + k_r pgt_l2 + k_r k_c pgt_l3)
+ * (tools/solver.c:328-383).  Factoring the column kappa out,
+ *   y_r = D(k_r) x_r + sum_l [ M0_l(k_r) u_l + M1_l(k_r) w_l
+ *                            + M2_l(k_r) u'_l + M3_l(k_r) w'_l ]
+ * with u_l = sum_c H0l(r,c) x_c, w_l = sum_c H0l(r,c) k_c x_c (u', w' with
+ * H1l) and the per-step radial tables
+ *   M0 = pg0 + k pg1, M1 = pg2 + k pg3, M2 = pgt0 + k pgt2, M3 = pgt1 + k pgt3
+ * built once per step for every distinct kappa.  Nothing of size nnz(A) is
+ * ever stored.  When g is real and H0l/H1l imaginary (always true for the
+ * dumpCouplings physics) the coupling is real: tables and angular factors
+ * are stored as real numbers and each term costs 2 FMAs instead of 4.
+ *
+ * Preconditioner: exact LU of each distinct diagonal block of P^T,
+ * P = S + i h dt/2 h0, in a banded ordering; one warp per block row solves
+ * 32 rows at a time with the pre-inverted 32x32 diagonal blocks.
+ *
+ * BiCGSTAB (tools/bicgstab.c:125-295): 5 kernels per iteration; the update
+ * of p and s is fused into the preconditioner, dots into the operator and
+ * the x/r update; every scalar lives on the device and reductions are
+ * deterministic (per-CTA partials summed in a fixed order by the last CTA).
+ */
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "gade_internal.h"
+#include "../../include/gade.h"
+
+#define SOL 137.035999084
+
+/* ------------------------------------------------------------------ */
+/* errors                                                              */
+/* ------------------------------------------------------------------ */
+static thread_local char g_err[1024];
+
+static int fail(int code, const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+extern "C" const char *gade_last_error(void) { return g_err; }
+
+#define CK(call)                                                                     \
+    do {                                                                             \
+        cudaError_t e_ = (call);                                                     \
+        if (e_ != cudaSuccess)                                                       \
+            return fail(GADE_ERR_CUDA, "%s:%d %s: %s", __FILE__, __LINE__, #call,    \
+                        cudaGetErrorString(e_));                                     \
+    } while (0)
+
+#define CKL()                                                                        \
+    do {                                                                             \
+        cudaError_t e_ = cudaGetLastError();                                         \
+        if (e_ != cudaSuccess)                                                       \
+            return fail(GADE_ERR_CUDA, "%s:%d launch: %s", __FILE__, __LINE__,       \
+                        cudaGetErrorString(e_));                                     \
+        s->launches++;                                                               \
+    } while (0)
+
+/* ------------------------------------------------------------------ */
+/* complex helpers                                                     */
+/* ------------------------------------------------------------------ */
+template <typename R> struct Cx;
+template <> struct Cx<double> { typedef double2 T; };
+template <> struct Cx<float> { typedef float2 T; };
+
+template <typename C> __device__ __forceinline__ C mk(double re, double im) { C c; c.x = re; c.y = im; return c; }
+template <typename C> __device__ __forceinline__ C cadd(C a, C b) { C c; c.x = a.x + b.x; c.y = a.y + b.y; return c; }
+template <typename C> __device__ __forceinline__ C csub(C a, C b) { C c; c.x = a.x - b.x; c.y = a.y - b.y; return c; }
+template <typename C> __device__ __forceinline__ C cmul(C a, C b)
+{
+    C c; c.x = a.x * b.x - a.y * b.y; c.y = a.x * b.y + a.y * b.x; return c;
+}
+/* acc += a*b */
+template <typename C> __device__ __forceinline__ void cfma(C &acc, C a, C b)
+{
+    acc.x = fma(a.x, b.x, acc.x); acc.x = fma(-a.y, b.y, acc.x);
+    acc.y = fma(a.x, b.y, acc.y); acc.y = fma(a.y, b.x, acc.y);
+}
+/* acc += a*b, a real */
+template <typename C, typename R> __device__ __forceinline__ void rfma(C &acc, R a, C b)
+{
+    acc.x = fma(a, b.x, acc.x); acc.y = fma(a, b.y, acc.y);
+}
+__device__ __forceinline__ double2 cdiv(double2 a, double2 b)
+{
+    /* Smith's algorithm (robust complex division) */
+    double2 q;
+    if (fabs(b.x) >= fabs(b.y)) {
+        double r = b.y / b.x, d = b.x + b.y * r;
+        q.x = (a.x + a.y * r) / d; q.y = (a.y - a.x * r) / d;
+    } else {
+        double r = b.x / b.y, d = b.x * r + b.y;
+        q.x = (a.x * r + a.y) / d; q.y = (a.y * r - a.x) / d;
+    }
+    return q;
+}
+struct alignas(32) R4d { double a, b, c, d; };
+struct alignas(16) R4f { float a, b, c, d; };
+template <typename R> struct R4;
+template <> struct R4<double> { typedef R4d T; };
+template <> struct R4<float> { typedef R4f T; };
+template <typename C> struct alignas(16) C4 { C a, b, c, d; };
+
+/* ------------------------------------------------------------------ */
+/* device scalars of one BiCGSTAB solve                                */
+/* ------------------------------------------------------------------ */
+struct DevScal {
+    double2 rho_prev, rho, alpha, w;
+    double r0_sqnorm, rhs_sqnorm, rr;
+    double2 r0v, ts;
+    double tt;
+    double pad[4];
+};
+
+enum { RED_RHS = 0, RED_RESTART, RED_R0V, RED_TS, RED_UPDATE, RED_NONE };
+enum { AX_PLAIN = 0, AX_PARTS, AX_R0V, AX_TS, AX_RHS, AX_RESTART };
+enum { PC_PLAIN = 0, PC_P, PC_S };
+
+#define NRED 4   /* values per partial: up to 4 doubles */
+
+/* ------------------------------------------------------------------ */
+/* operator parameters                                                 */
+/* ------------------------------------------------------------------ */
+struct OpP {
+    int nblk, B, lmax, W, nk, RM, CM;
+    const int *row_kidx, *act_ptr, *act_l, *ang_ptr, *ang_c;
+    const void *ang_a0, *ang_a0k, *ang_a1, *ang_a1k;
+    const int *chunk_nrows, *chunk_ncols, *chunk_rows, *chunk_cols, *chunk_lcol;
+    const void *M;             /* [lmax][nk][W][B] */
+    const void *S_ell, *Hst_ell;
+};
+
+struct VecP {
+    void *out0, *out1, *out2;      /* outputs by mode */
+    const void *in0, *in1;         /* r0 / s / rhs by mode */
+};
+
+struct RedP {
+    double *part;                  /* [nCTA][NRED] */
+    unsigned int *ticket;
+    DevScal *sc;
+    int kind;
+};
+
+/* Block-wide deterministic sum of NV doubles; result valid in thread 0. */
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double *sh)
+{
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int k = 0; k < NV; k++) sh[k * nt + tid] = v[k];
+    __syncthreads();
+    for (int s = 1; s < nt; s <<= 1) {
+        /* pairwise in fixed order: thread tid (multiple of 2s) adds tid+s */
+        if ((tid % (2 * s)) == 0 && tid + s < nt)
+            for (int k = 0; k < NV; k++) sh[k * nt + tid] += sh[k * nt + tid + s];
+        __syncthreads();
+    }
+    for (int k = 0; k < NV; k++) v[k] = sh[k * nt];
+    __syncthreads();
+}
+
+/* Per-CTA partials + last-CTA finalisation (fixed summation order). */
+__device__ void reduce_finish(RedP red, double (&v)[NRED], double *sh)
+{
+    __shared__ bool am_last;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const unsigned ncta = gridDim.x * gridDim.y;
+    const unsigned cta = blockIdx.y * gridDim.x + blockIdx.x;
+    block_sum<NRED>(v, sh);
+    if (tid == 0) {
+        for (int k = 0; k < NRED; k++) red.part[(size_t)cta * NRED + k] = v[k];
+        __threadfence();
+        unsigned t = atomicAdd(red.ticket, 1u);
+        am_last = (t == ncta - 1);
+    }
+    __syncthreads();
+    if (!am_last) return;
+    __threadfence();
+    double acc[NRED] = {0, 0, 0, 0};
+    for (unsigned j = tid; j < ncta; j += nt)
+        for (int k = 0; k < NRED; k++) acc[k] += __ldcg(&red.part[(size_t)j * NRED + k]);
+    block_sum<NRED>(acc, sh);
+    if (tid == 0) {
+        DevScal *sc = red.sc;
+        switch (red.kind) {
+        case RED_RHS:
+            sc->r0_sqnorm = acc[0];
+            sc->rr = acc[0];
+            sc->rhs_sqnorm = acc[1];
+            sc->rho = make_double2(acc[0], 0.0);
+            sc->rho_prev = make_double2(1.0, 0.0);
+            sc->alpha = make_double2(1.0, 0.0);
+            sc->w = make_double2(1.0, 0.0);
+            break;
+        case RED_RESTART:
+            sc->r0_sqnorm = acc[0];
+            sc->rr = acc[0];
+            sc->rho = make_double2(acc[0], 0.0);
+            break;
+        case RED_R0V:
+            sc->r0v = make_double2(acc[0], acc[1]);
+            sc->alpha = cdiv(sc->rho, sc->r0v);
+            break;
+        case RED_TS:
+            sc->tt = acc[0];
+            sc->ts = make_double2(acc[1], acc[2]);
+            sc->w = acc[0] > 0 ? make_double2(acc[1] / acc[0], acc[2] / acc[0]) : make_double2(0.0, 0.0);
+            break;
+        case RED_UPDATE:
+            sc->rr = acc[0];
+            sc->rho_prev = sc->rho;
+            sc->rho = make_double2(acc[1], acc[2]);
+            break;
+        }
+        *red.ticket = 0u;
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* per-step radial tables                                              */
+/* ------------------------------------------------------------------ */
+struct TabP {
+    int lmax, nk, W, B, blk_nnz;
+    const int *kvals, *ell_pos;
+    const void *g, *gt;           /* [lmax][3][4][blk_nnz] (a in the l-parity set) */
+    void *M;                      /* [lmax][nk][W][B] */
+};
+
+/* coef[l*3 + ia]: SoL * i h dt/2 * f_a for a = (l%2+1)%2 + 2 ia.
+ * RC: imaginary parts only (pg is imaginary, the stored table is -Im M). */
+template <typename R, bool RC>
+__global__ void k_tables(TabP T, const double2 *__restrict__ coef)
+{
+    typedef typename Cx<R>::T C;
+    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long long per_l = (long long)T.W * T.B;
+    if (tid >= per_l * T.lmax) return;
+    const int l = (int)(tid / per_l);
+    const int slot = (int)(tid % per_l);      /* j*B + i */
+    const int k = T.ell_pos[slot];
+    if (RC) {
+        typedef typename R4<R>::T Q4;
+        double pg[4] = {0, 0, 0, 0}, pgt[4] = {0, 0, 0, 0};
+        if (k >= 0) {
+            const double *g = (const double *)T.g, *gt = (const double *)T.gt;
+            for (int ia = 0; ia < 3; ia++) {
+                const double c = coef[l * 3 + ia].y;
+                for (int q = 0; q < 4; q++) {
+                    size_t off = (((size_t)l * 3 + ia) * 4 + q) * T.blk_nnz + k;
+                    pg[q] = fma(c, g[off], pg[q]);
+                    pgt[q] = fma(c, gt[off], pgt[q]);
+                }
+            }
+        }
+        Q4 *M = (Q4 *)T.M;
+        for (int kk = 0; kk < T.nk; kk++) {
+            const double kap = (double)T.kvals[kk];
+            Q4 m;
+            m.a = (R)(-fma(kap, pg[1], pg[0]));
+            m.b = (R)(-fma(kap, pg[3], pg[2]));
+            m.c = (R)(-fma(kap, pgt[2], pgt[0]));
+            m.d = (R)(-fma(kap, pgt[3], pgt[1]));
+            M[((size_t)l * T.nk + kk) * per_l + slot] = m;
+        }
+    } else {
+        double2 pg[4], pgt[4];
+        for (int q = 0; q < 4; q++) { pg[q] = make_double2(0, 0); pgt[q] = make_double2(0, 0); }
+        if (k >= 0) {
+            const double2 *g = (const double2 *)T.g, *gt = (const double2 *)T.gt;
+            for (int ia = 0; ia < 3; ia++) {
+                const double2 c = coef[l * 3 + ia];
+                for (int q = 0; q < 4; q++) {
+                    size_t off = (((size_t)l * 3 + ia) * 4 + q) * T.blk_nnz + k;
+                    cfma(pg[q], c, g[off]);
+                    cfma(pgt[q], c, gt[off]);
+                }
+            }
+        }
+        C4<C> *M = (C4<C> *)T.M;
+        for (int kk = 0; kk < T.nk; kk++) {
+            const double kap = (double)T.kvals[kk];
+            C4<C> m;
+            m.a = mk<C>(fma(kap, pg[1].x, pg[0].x), fma(kap, pg[1].y, pg[0].y));
+            m.b = mk<C>(fma(kap, pg[3].x, pg[2].x), fma(kap, pg[3].y, pg[2].y));
+            m.c = mk<C>(fma(kap, pgt[2].x, pgt[0].x), fma(kap, pgt[2].y, pgt[0].y));
+            m.d = mk<C>(fma(kap, pgt[3].x, pgt[1].x), fma(kap, pgt[3].y, pgt[1].y));
+            M[((size_t)l * T.nk + kk) * per_l + slot] = m;
+        }
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* matrix-free operator                                                */
+/* ------------------------------------------------------------------ */
+/* grid (nchunk, nblk); blockDim = RM (one thread per row of the chunk) */
+template <typename R, bool RC>
+__global__ void __launch_bounds__(128) k_apply(OpP P, const typename Cx<R>::T *__restrict__ x, int mode,
+                                               VecP V, RedP red)
+{
+    typedef typename Cx<R>::T C;
+    extern __shared__ unsigned char smem_raw[];
+    C *xr = (C *)smem_raw;                    /* [CM] */
+    C *u0 = xr + P.CM, *u1 = u0 + P.CM, *u2 = u1 + P.CM, *u3 = u2 + P.CM;
+    double *shred = (double *)(u3 + P.CM);    /* [NRED * blockDim] */
+
+    const int q = blockIdx.x, r = blockIdx.y, tid = threadIdx.x, nt = blockDim.x;
+    const int B = P.B, W = P.W;
+    const int kk = P.row_kidx[r];
+    const int nrows = P.chunk_nrows[q], ncols = P.chunk_ncols[q];
+    const int i = (tid < nrows) ? P.chunk_rows[q * P.RM + tid] : -1;
+    const int *cols = P.chunk_cols + (size_t)q * P.CM;
+    const int *lcol = P.chunk_lcol + (size_t)q * W * P.RM;
+    const C *xb = x + (size_t)r * B;
+
+    for (int c = tid; c < ncols; c += nt) xr[c] = xb[cols[c]];
+    __syncthreads();
+
+    C accS = mk<C>(0, 0), accH = mk<C>(0, 0);
+    if (i >= 0) {
+        const C *Se = (const C *)P.S_ell + (size_t)kk * W * B;
+        const C *He = (const C *)P.Hst_ell + (size_t)kk * W * B;
+        for (int j = 0; j < W; j++) {
+            const int lc = lcol[j * P.RM + tid];
+            if (lc >= 0) {
+                const C xv = xr[lc];
+                cfma(accS, Se[(size_t)j * B + i], xv);
+                cfma(accH, He[(size_t)j * B + i], xv);
+            }
+        }
+    }
+
+    for (int a = P.act_ptr[r]; a < P.act_ptr[r + 1]; a++) {
+        const int l = P.act_l[a];
+        const int e0 = P.ang_ptr[r * P.lmax + l], e1 = P.ang_ptr[r * P.lmax + l + 1];
+        __syncthreads();
+        for (int c = tid; c < ncols; c += nt) {
+            const int gc = cols[c];
+            C U = mk<C>(0, 0), Wv = mk<C>(0, 0), U1 = mk<C>(0, 0), W1 = mk<C>(0, 0);
+            for (int e = e0; e < e1; e++) {
+                const C xv = x[(size_t)P.ang_c[e] * B + gc];
+                if (RC) {
+                    rfma(U, ((const R *)P.ang_a0)[e], xv);
+                    rfma(Wv, ((const R *)P.ang_a0k)[e], xv);
+                    rfma(U1, ((const R *)P.ang_a1)[e], xv);
+                    rfma(W1, ((const R *)P.ang_a1k)[e], xv);
+                } else {
+                    cfma(U, ((const C *)P.ang_a0)[e], xv);
+                    cfma(Wv, ((const C *)P.ang_a0k)[e], xv);
+                    cfma(U1, ((const C *)P.ang_a1)[e], xv);
+                    cfma(W1, ((const C *)P.ang_a1k)[e], xv);
+                }
+            }
+            u0[c] = U; u1[c] = Wv; u2[c] = U1; u3[c] = W1;
+        }
+        __syncthreads();
+        if (i >= 0) {
+            const size_t base = ((size_t)l * P.nk + kk) * W * B;
+            for (int j = 0; j < W; j++) {
+                const int lc = lcol[j * P.RM + tid];
+                if (lc < 0) continue;
+                if (RC) {
+                    typedef typename R4<R>::T Q4;
+                    const Q4 m = ((const Q4 *)P.M)[base + (size_t)j * B + i];
+                    rfma(accH, m.a, u0[lc]);
+                    rfma(accH, m.b, u1[lc]);
+                    rfma(accH, m.c, u2[lc]);
+                    rfma(accH, m.d, u3[lc]);
+                } else {
+                    const C4<C> m = ((const C4<C> *)P.M)[base + (size_t)j * B + i];
+                    cfma(accH, m.a, u0[lc]);
+                    cfma(accH, m.b, u1[lc]);
+                    cfma(accH, m.c, u2[lc]);
+                    cfma(accH, m.d, u3[lc]);
+                }
+            }
+        }
+    }
+
+    /* epilogue */
+    double v[NRED] = {0, 0, 0, 0};
+    if (i >= 0) {
+        const size_t gi = (size_t)r * B + i;
+        const C ax = cadd(accH, accS);
+        switch (mode) {
+        case AX_PLAIN:
+            ((C *)V.out0)[gi] = ax;
+            break;
+        case AX_PARTS:
+            ((C *)V.out0)[gi] = accS;
+            ((C *)V.out1)[gi] = accH;
+            break;
+        case AX_R0V: {          /* v = A y ; <r0, v> */
+            ((C *)V.out0)[gi] = ax;
+            const C r0 = ((const C *)V.in0)[gi];
+            v[0] = (double)r0.x * ax.x + (double)r0.y * ax.y;
+            v[1] = (double)r0.x * ax.y - (double)r0.y * ax.x;
+            break;
+        }
+        case AX_TS: {           /* t = A z ; <t,t>, <t,s> */
+            ((C *)V.out0)[gi] = ax;
+            const C sv = ((const C *)V.in0)[gi];
+            v[0] = (double)ax.x * ax.x + (double)ax.y * ax.y;
+            v[1] = (double)ax.x * sv.x + (double)ax.y * sv.y;
+            v[2] = (double)ax.x * sv.y - (double)ax.y * sv.x;
+            break;
+        }
+        case AX_RHS: {          /* rhs = -Hx + Sx ; r = rhs - (Hx + Sx) ; r0 = r */
+            const C rhs = csub(accS, accH);
+            const C rv = csub(rhs, ax);
+            ((C *)V.out0)[gi] = rhs;
+            ((C *)V.out1)[gi] = rv;
+            ((C *)V.out2)[gi] = rv;
+            v[0] = (double)rv.x * rv.x + (double)rv.y * rv.y;
+            v[1] = (double)rhs.x * rhs.x + (double)rhs.y * rhs.y;
+            break;
+        }
+        case AX_RESTART: {      /* r = rhs - A x ; r0 = r */
+            const C rhs = ((const C *)V.in0)[gi];
+            const C rv = csub(rhs, ax);
+            ((C *)V.out1)[gi] = rv;
+            ((C *)V.out2)[gi] = rv;
+            v[0] = (double)rv.x * rv.x + (double)rv.y * rv.y;
+            break;
+        }
+        }
+    }
+    if (red.kind != RED_NONE) reduce_finish(red, v, shred);
+}
+
+/* ------------------------------------------------------------------ */
+/* block-LU preconditioner                                             */
+/* ------------------------------------------------------------------ */
+struct PcP {
+    int nblk, B, bw, Bp, nch, wpc;
+    const int *row_kidx, *ord;
+    const void *Lb, *Ub, *Linv, *Uinv;
+};
+
+/* one warp per block row; wpc warps per CTA.
+ * mode PC_PLAIN: b = in0
+ * mode PC_P    : p = r + beta (p - w v)  (in0 = r, io = p, in1 = v); b = p
+ * mode PC_S    : s = r - alpha v         (in0 = r, in1 = v, out s);   b = s  */
+template <typename R>
+__global__ void k_precond(PcP Q, int mode, const typename Cx<R>::T *__restrict__ in0,
+                          const typename Cx<R>::T *__restrict__ in1, typename Cx<R>::T *io,
+                          typename Cx<R>::T *__restrict__ out, const DevScal *__restrict__ sc)
+{
+    typedef typename Cx<R>::T C;
+    extern __shared__ unsigned char smem_raw[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int r = blockIdx.x * Q.wpc + warp;
+    C *buf = (C *)smem_raw + (size_t)warp * (Q.Bp + 32);
+    C *tb = buf + Q.Bp;
+    if (r >= Q.nblk) return;
+    const int B = Q.B, Bp = Q.Bp, bw = Q.bw;
+    const int kk = Q.row_kidx[r];
+    const size_t off = (size_t)r * B;
+
+    C beta = mk<C>(0, 0), negw = mk<C>(0, 0), nega = mk<C>(0, 0);
+    if (mode == PC_P) {
+        const double2 a = cdiv(sc->rho, sc->rho_prev);
+        const double2 b = cdiv(sc->alpha, sc->w);
+        beta = mk<C>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+        negw = mk<C>(-sc->w.x, -sc->w.y);
+    } else if (mode == PC_S) {
+        nega = mk<C>(-sc->alpha.x, -sc->alpha.y);
+    }
+    /* load (and update) the right-hand side in the banded ordering */
+    for (int o = lane; o < Bp; o += 32) {
+        C val = mk<C>(0, 0);
+        if (o < B) {
+            const int n = Q.ord[o];
+            const size_t gi = off + n;
+            if (mode == PC_PLAIN) {
+                val = in0[gi];
+            } else if (mode == PC_P) {
+                C t = io[gi];
+                cfma(t, negw, in1[gi]);            /* p - w v */
+                C pv = in0[gi];
+                cfma(pv, beta, t);                 /* r + beta (p - w v) */
+                io[gi] = pv;
+                val = pv;
+            } else {
+                C sv = in0[gi];
+                cfma(sv, nega, in1[gi]);           /* r - alpha v */
+                io[gi] = sv;
+                val = sv;
+            }
+        }
+        buf[o] = val;
+    }
+    __syncwarp();
+    const C *Lb = (const C *)Q.Lb + (size_t)kk * bw * Bp;
+    const C *Ub = (const C *)Q.Ub + (size_t)kk * bw * Bp;
+    const C *Li = (const C *)Q.Linv + (size_t)kk * Q.nch * 1024;
+    const C *Ui = (const C *)Q.Uinv + (size_t)kk * Q.nch * 1024;
+    /* forward: L y = b */
+    for (int c = 0; c < Q.nch; c++) {
+        const int o = 32 * c + lane;
+        C t = buf[o];
+        for (int d = 1; d <= bw; d++) {
+            const int src = o - d;
+            if (src >= 32 * c) continue;            /* inside this chunk: via Linv */
+            if (src < 0) break;
+            C lv = Lb[(size_t)(d - 1) * Bp + o];
+            lv.x = -lv.x; lv.y = -lv.y;
+            cfma(t, lv, buf[src]);
+        }
+        tb[lane] = t;
+        __syncwarp();
+        C y = mk<C>(0, 0);
+        const C *Lc = Li + (size_t)c * 1024;
+        for (int j = 0; j <= lane; j++) cfma(y, Lc[j * 32 + lane], tb[j]);
+        __syncwarp();
+        buf[o] = y;
+        __syncwarp();
+    }
+    /* backward: U x = y */
+    for (int c = Q.nch - 1; c >= 0; c--) {
+        const int o = 32 * c + lane;
+        C t = buf[o];
+        for (int d = 1; d <= bw; d++) {
+            const int src = o + d;
+            if (src < 32 * (c + 1)) continue;
+            if (src >= B) break;
+            C uv = Ub[(size_t)(d - 1) * Bp + o];
+            uv.x = -uv.x; uv.y = -uv.y;
+            cfma(t, uv, buf[src]);
+        }
+        tb[lane] = t;
+        __syncwarp();
+        C xv = mk<C>(0, 0);
+        const C *Uc = Ui + (size_t)c * 1024;
+        for (int j = lane; j < 32; j++) cfma(xv, Uc[j * 32 + lane], tb[j]);
+        __syncwarp();
+        buf[o] = xv;
+        __syncwarp();
+    }
+    for (int o = lane; o < B; o += 32) out[off + Q.ord[o]] = buf[o];
+}
+
+/* ------------------------------------------------------------------ */
+/* x += alpha y + w z ; r = s - w t ; |r|^2, <r0, r>                    */
+/* ------------------------------------------------------------------ */
+template <typename R>
+__global__ void k_update(long long n, typename Cx<R>::T *x, const typename Cx<R>::T *__restrict__ y,
+                         const typename Cx<R>::T *__restrict__ z, typename Cx<R>::T *r,
+                         const typename Cx<R>::T *__restrict__ s, const typename Cx<R>::T *__restrict__ t,
+                         const typename Cx<R>::T *__restrict__ r0, RedP red)
+{
+    typedef typename Cx<R>::T C;
+    extern __shared__ unsigned char smem_raw[];
+    double *shred = (double *)smem_raw;
+    const double2 al = red.sc->alpha, w = red.sc->w;
+    const C a = mk<C>(al.x, al.y), wc = mk<C>(w.x, w.y), nw = mk<C>(-w.x, -w.y);
+    double v[NRED] = {0, 0, 0, 0};
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        C zz = cmul(a, y[i]);
+        cfma(zz, wc, z[i]);
+        x[i] = cadd(x[i], zz);
+        C rv = s[i];
+        cfma(rv, nw, t[i]);
+        r[i] = rv;
+        const C q = r0[i];
+        v[0] += (double)rv.x * rv.x + (double)rv.y * rv.y;
+        v[1] += (double)q.x * rv.x + (double)q.y * rv.y;
+        v[2] += (double)q.x * rv.y - (double)q.y * rv.x;
+    }
+    reduce_finish(red, v, shred);
+}
+
+/* ------------------------------------------------------------------ */
+/* solver object                                                       */
+/* ------------------------------------------------------------------ */
+struct gade_solver {
+    int device;
+    cudaStream_t stream;
+    int prec, rc;
+    long long n;
+    int nblk, B, lmax, W, nk, RM, CM, nchunk;
+    int bw, Bp, nch, wpc;
+    double dt, h;
+    /* operator tables */
+    int *d_row_kidx, *d_act_ptr, *d_act_l, *d_ang_ptr, *d_ang_c;
+    void *d_ang_a0, *d_ang_a0k, *d_ang_a1, *d_ang_a1k;
+    int *d_chunk_nrows, *d_chunk_ncols, *d_chunk_rows, *d_chunk_cols, *d_chunk_lcol;
+    void *d_M, *d_S_ell, *d_Hst_ell;
+    int *d_kvals, *d_ell_pos;
+    void *d_g, *d_gt;
+    int blk_nnz;
+    /* preconditioner */
+    int *d_ord;
+    void *d_Lb, *d_Ub, *d_Linv, *d_Uinv;
+    /* vectors */
+    double2 *x, *rhs, *r, *r0, *p, *v, *y, *z, *s, *t, *tmp0, *tmp1;
+    /* reductions */
+    double *d_part;
+    unsigned int *d_ticket;
+    DevScal *d_sc, *h_sc;
+    double2 *d_coef, *h_coef;
+    int upd_grid, upd_block;
+    long long launches;
+    int has_time;
+    std::vector<void *> allocs;
+    /* event-pair profiling: kind 0 apply, 1 precond, 2 other */
+    int profile;
+    std::vector<cudaEvent_t> ev_pool;
+    std::vector<int> ev_kind;
+    size_t ev_used;
+    long long prof_n[3];
+    double prof_ms[3];
+};
+
+static void prof_begin(gade_solver *s, cudaStream_t st)
+{
+    if (!s->profile) return;
+    if (s->ev_used + 2 > s->ev_pool.size()) {
+        for (int k = 0; k < 64; k++) {
+            cudaEvent_t e;
+            if (cudaEventCreate(&e) != cudaSuccess) { s->profile = 0; return; }
+            s->ev_pool.push_back(e);
+        }
+        s->ev_kind.resize(s->ev_pool.size() / 2 + 1);
+    }
+    cudaEventRecord(s->ev_pool[s->ev_used], st);
+}
+
+static void prof_end(gade_solver *s, cudaStream_t st, int kind)
+{
+    if (!s->profile) return;
+    cudaEventRecord(s->ev_pool[s->ev_used + 1], st);
+    s->ev_kind[s->ev_used / 2] = kind;
+    s->ev_used += 2;
+}
+
+static void prof_collect(gade_solver *s)
+{
+    if (s->ev_used == 0) return;
+    cudaEventSynchronize(s->ev_pool[s->ev_used - 1]);
+    for (size_t k = 0; k < s->ev_used; k += 2) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, s->ev_pool[k], s->ev_pool[k + 1]);
+        int kind = s->ev_kind[k / 2];
+        s->prof_n[kind]++;
+        s->prof_ms[kind] += ms;
+    }
+    s->ev_used = 0;
+}
+
+template <typename T>
+static int dev_upload(gade_solver *s, T **d, const T *h, size_t count)
+{
+    size_t bytes = sizeof(T) * (count ? count : 1);
+    void *p = nullptr;
+    CK(cudaMalloc(&p, bytes));
+    s->allocs.push_back(p);
+    if (h && count) CK(cudaMemcpy(p, h, sizeof(T) * count, cudaMemcpyHostToDevice));
+    else CK(cudaMemset(p, 0, bytes));
+    *d = (T *)p;
+    return GADE_OK;
+}
+
+#define UP(dst, src, cnt) do { int rc_ = dev_upload(s, &(dst), (src), (size_t)(cnt)); if (rc_) { gade_solver_free(s); return rc_; } } while (0)
+
+struct gade_problem_handle;   /* gade_problem is the host struct */
+
+extern "C" int gade_problem_load(const char *dir, int32_t lmax, gade_problem **out)
+{
+    char err[1024] = {0};
+    if (!dir || !out) return fail(GADE_ERR_ARG, "gade_problem_load: NULL argument");
+    int rc = gade_problem_read(dir, lmax, out, err, sizeof(err));
+    if (rc) return fail(rc, "%s", err);
+    return GADE_OK;
+}
+
+extern "C" int gade_problem_get_info(const gade_problem *p, gade_problem_info *info)
+{
+    if (!p || !info) return fail(GADE_ERR_ARG, "gade_problem_get_info: NULL argument");
+    info->lmax = p->lmax; info->nblk = p->nblk; info->blkdim = p->blkdim; info->blk_nnz = p->blk_nnz;
+    info->n = p->n;
+    info->hall_nnz = p->hall_Ap[p->nblk];
+    info->nnz_full = (int64_t)info->hall_nnz * p->blk_nnz;
+    info->real_coupling = p->real_coupling;
+    return GADE_OK;
+}
+
+extern "C" int gade_problem_get_psi0(const gade_problem *p, double *psi, int32_t *perm)
+{
+    if (!p) return fail(GADE_ERR_ARG, "gade_problem_get_psi0: NULL problem");
+    if (psi) memcpy(psi, p->psi0, sizeof(gc64) * (size_t)p->n);
+    if (perm) memcpy(perm, p->xperm, sizeof(int32_t) * (size_t)p->n);
+    return GADE_OK;
+}
+
+extern "C" void gade_problem_free(gade_problem *p) { gade_problem_release(p); }
+
+extern "C" void gade_solver_free(gade_solver *s)
+{
+    if (!s) return;
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(s->device);
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    for (void *p : s->allocs) cudaFree(p);
+    for (cudaEvent_t e : s->ev_pool) cudaEventDestroy(e);
+    if (s->h_sc) cudaFreeHost(s->h_sc);
+    if (s->h_coef) cudaFreeHost(s->h_coef);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    cudaSetDevice(cur);
+    delete s;
+}
+
+static int choose_chunk_splines(int nblk, int B, int nsm)
+{
+    int half = (B % 2 == 0) ? B / 2 : B;
+    int target = 2 * nsm;
+    int nch = (target + nblk - 1) / nblk;
+    if (nch < 1) nch = 1;
+    int cs = (half + nch - 1) / nch;
+    cs = ((cs + 15) / 16) * 16;
+    if (cs < 16) cs = 16;
+    if (cs > 64) cs = 64;
+    return cs;
+}
+
+extern "C" int gade_solver_create(const gade_problem *p, double dt, double h, int32_t precision,
+                                  int32_t device, gade_solver **out)
+{
+    if (!p || !out) return fail(GADE_ERR_ARG, "gade_solver_create: NULL argument");
+    *out = nullptr;
+    if (precision != GADE_PREC_FP64 && precision != GADE_PREC_MIXED)
+        return fail(GADE_ERR_ARG, "gade_solver_create: unknown precision %d", precision);
+    if (!(dt > 0) || !std::isfinite(dt)) return fail(GADE_ERR_ARG, "gade_solver_create: dt must be finite and > 0");
+    int ndev = 0;
+    CK(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) return fail(GADE_ERR_ARG, "gade_solver_create: no CUDA device %d", device);
+    CK(cudaSetDevice(device));
+    cudaDeviceProp prop;
+    CK(cudaGetDeviceProperties(&prop, device));
+
+    char err[1024] = {0};
+    gade_setup *su = nullptr;
+    int cs = choose_chunk_splines(p->nblk, p->blkdim, prop.multiProcessorCount);
+    int rcode = gade_setup_build(p, dt, h, cs, &su, err, sizeof(err));
+    if (rcode) return fail(rcode, "%s", err);
+    if (su->chunk_rows_max > 128) { gade_setup_release(su); return fail(GADE_ERR_ARG, "chunk too large"); }
+
+    gade_solver *s = new gade_solver();
+    s->device = device;
+    s->prec = precision;
+    s->rc = p->real_coupling;
+    s->n = p->n; s->nblk = p->nblk; s->B = p->blkdim; s->lmax = p->lmax;
+    s->W = su->W; s->nk = su->nk; s->RM = su->chunk_rows_max; s->CM = su->chunk_cols_max;
+    s->nchunk = su->nchunk; s->bw = su->bw; s->Bp = su->Bp; s->nch = su->nch;
+    s->dt = dt; s->h = h; s->blk_nnz = p->blk_nnz;
+    if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        gade_setup_release(su); delete s; return fail(GADE_ERR_CUDA, "stream creation failed");
+    }
+    const size_t WB = (size_t)s->W * s->B;
+
+    UP(s->d_row_kidx, su->row_kidx, s->nblk);
+    UP(s->d_act_ptr, su->act_ptr, s->nblk + 1);
+    UP(s->d_act_l, su->act_l, su->n_act);
+    UP(s->d_ang_ptr, su->ang_ptr, (size_t)s->nblk * s->lmax + 1);
+    UP(s->d_ang_c, su->ang_c, su->n_ang);
+    {
+        const gc64 *src[4] = {su->ang_a0, su->ang_a0k, su->ang_a1, su->ang_a1k};
+        void **dst[4] = {&s->d_ang_a0, &s->d_ang_a0k, &s->d_ang_a1, &s->d_ang_a1k};
+        for (int k = 0; k < 4; k++) {
+            if (s->rc) {
+                std::vector<double> im((size_t)su->n_ang + 1);
+                for (int64_t e = 0; e < su->n_ang; e++) im[e] = src[k][e].im;
+                double *d; UP(d, im.data(), su->n_ang); *dst[k] = d;
+            } else {
+                double2 *d; UP(d, (const double2 *)src[k], su->n_ang); *dst[k] = d;
+            }
+        }
+    }
+    UP(s->d_chunk_nrows, su->chunk_nrows, s->nchunk);
+    UP(s->d_chunk_ncols, su->chunk_ncols, s->nchunk);
+    UP(s->d_chunk_rows, su->chunk_rows, (size_t)s->nchunk * s->RM);
+    UP(s->d_chunk_cols, su->chunk_cols, (size_t)s->nchunk * s->CM);
+    UP(s->d_chunk_lcol, su->chunk_lcol, (size_t)s->nchunk * s->W * s->RM);
+    {
+        double2 *d;
+        UP(d, (const double2 *)su->S_ell, (size_t)s->nk * WB); s->d_S_ell = d;
+        UP(d, (const double2 *)su->Hst_ell, (size_t)s->nk * WB); s->d_Hst_ell = d;
+    }
+    UP(s->d_kvals, su->kvals, s->nk);
+    UP(s->d_ell_pos, su->ell_pos, WB);
+    {
+        /* radial tables of the three pulse components used by each l */
+        const size_t bn = (size_t)p->blk_nnz;
+        const size_t cnt = (size_t)s->lmax * 3 * 4 * bn;
+        if (s->rc) {
+            std::vector<double> g(cnt), gt(cnt);
+            for (int l = 0; l < s->lmax; l++)
+                for (int ia = 0; ia < 3; ia++) {
+                    int a = (l % 2 + 1) % 2 + 2 * ia;
+                    for (int q = 0; q < 4; q++)
+                        for (size_t k = 0; k < bn; k++) {
+                            size_t src = (((size_t)a * s->lmax + l) * 4 + q) * bn + k;
+                            size_t dst = (((size_t)l * 3 + ia) * 4 + q) * bn + k;
+                            g[dst] = p->g[src].re; gt[dst] = p->gt[src].re;
+                        }
+                }
+            double *d; UP(d, g.data(), cnt); s->d_g = d; UP(d, gt.data(), cnt); s->d_gt = d;
+        } else {
+            std::vector<double2> g(cnt), gt(cnt);
+            for (int l = 0; l < s->lmax; l++)
+                for (int ia = 0; ia < 3; ia++) {
+                    int a = (l % 2 + 1) % 2 + 2 * ia;
+                    for (int q = 0; q < 4; q++)
+                        for (size_t k = 0; k < bn; k++) {
+                            size_t src = (((size_t)a * s->lmax + l) * 4 + q) * bn + k;
+                            size_t dst = (((size_t)l * 3 + ia) * 4 + q) * bn + k;
+                            g[dst] = make_double2(p->g[src].re, p->g[src].im);
+                            gt[dst] = make_double2(p->gt[src].re, p->gt[src].im);
+                        }
+                }
+            double2 *d; UP(d, g.data(), cnt); s->d_g = d; UP(d, gt.data(), cnt); s->d_gt = d;
+        }
+        size_t mcount = (size_t)s->lmax * s->nk * WB;
+        if (s->rc) { R4d *d; UP(d, (const R4d *)nullptr, mcount); s->d_M = d; }
+        else { C4<double2> *d; UP(d, (const C4<double2> *)nullptr, mcount); s->d_M = d; }
+    }
+    /* preconditioner */
+    UP(s->d_ord, su->ord, s->B);
+    {
+        double2 *d;
+        UP(d, (const double2 *)su->Lb, (size_t)s->nk * s->bw * s->Bp); s->d_Lb = d;
+        UP(d, (const double2 *)su->Ub, (size_t)s->nk * s->bw * s->Bp); s->d_Ub = d;
+        UP(d, (const double2 *)su->Linv, (size_t)s->nk * s->nch * 1024); s->d_Linv = d;
+        UP(d, (const double2 *)su->Uinv, (size_t)s->nk * s->nch * 1024); s->d_Uinv = d;
+    }
+    {
+        size_t per_warp = sizeof(double2) * (size_t)(s->Bp + 32);
+        int wpc = (int)((48 * 1024) / per_warp);
+        if (wpc > 4) wpc = 4;
+        if (wpc < 1) wpc = 1;
+        s->wpc = wpc;
+        if (per_warp * wpc > 200 * 1024) { gade_setup_release(su); gade_solver_free(s); return fail(GADE_ERR_ARG, "block dimension too large"); }
+    }
+    /* vectors */
+    double2 **vecs[] = {&s->x, &s->rhs, &s->r, &s->r0, &s->p, &s->v, &s->y, &s->z, &s->s, &s->t, &s->tmp0, &s->tmp1};
+    for (double2 **vp : vecs) UP(*vp, (const double2 *)nullptr, (size_t)s->n);
+    CK(cudaMemcpy(s->x, p->psi0, sizeof(double2) * (size_t)s->n, cudaMemcpyHostToDevice));
+    /* reductions */
+    s->upd_block = 256;
+    s->upd_grid = 2 * prop.multiProcessorCount;
+    size_t max_cta = (size_t)s->nchunk * s->nblk;
+    if ((size_t)s->upd_grid > max_cta) max_cta = s->upd_grid;
+    UP(s->d_part, (const double *)nullptr, max_cta * NRED);
+    UP(s->d_ticket, (const unsigned *)nullptr, 1);
+    UP(s->d_sc, (const DevScal *)nullptr, 1);
+    UP(s->d_coef, (const double2 *)nullptr, (size_t)s->lmax * 3);
+    if (cudaMallocHost((void **)&s->h_sc, sizeof(DevScal)) != cudaSuccess ||
+        cudaMallocHost((void **)&s->h_coef, sizeof(double2) * (size_t)s->lmax * 3) != cudaSuccess) {
+        gade_setup_release(su); gade_solver_free(s); return fail(GADE_ERR_CUDA, "pinned allocation failed");
+    }
+    {
+        size_t smem = sizeof(double2) * (size_t)(s->Bp + 32) * s->wpc;
+        if (smem > 48 * 1024)
+            cudaFuncSetAttribute(k_precond<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    }
+    gade_setup_release(su);
+    *out = s;
+    return GADE_OK;
+}
+
+static OpP op_params(const gade_solver *s)
+{
+    OpP P;
+    P.nblk = s->nblk; P.B = s->B; P.lmax = s->lmax; P.W = s->W; P.nk = s->nk; P.RM = s->RM; P.CM = s->CM;
+    P.row_kidx = s->d_row_kidx; P.act_ptr = s->d_act_ptr; P.act_l = s->d_act_l;
+    P.ang_ptr = s->d_ang_ptr; P.ang_c = s->d_ang_c;
+    P.ang_a0 = s->d_ang_a0; P.ang_a0k = s->d_ang_a0k; P.ang_a1 = s->d_ang_a1; P.ang_a1k = s->d_ang_a1k;
+    P.chunk_nrows = s->d_chunk_nrows; P.chunk_ncols = s->d_chunk_ncols; P.chunk_rows = s->d_chunk_rows;
+    P.chunk_cols = s->d_chunk_cols; P.chunk_lcol = s->d_chunk_lcol;
+    P.M = s->d_M; P.S_ell = s->d_S_ell; P.Hst_ell = s->d_Hst_ell;
+    return P;
+}
+
+static PcP pc_params(const gade_solver *s)
+{
+    PcP Q;
+    Q.nblk = s->nblk; Q.B = s->B; Q.bw = s->bw; Q.Bp = s->Bp; Q.nch = s->nch; Q.wpc = s->wpc;
+    Q.row_kidx = s->d_row_kidx; Q.ord = s->d_ord;
+    Q.Lb = s->d_Lb; Q.Ub = s->d_Ub; Q.Linv = s->d_Linv; Q.Uinv = s->d_Uinv;
+    return Q;
+}
+
+static int launch_apply(gade_solver *s, const double2 *x, int mode, VecP V, int redkind, cudaStream_t st)
+{
+    OpP P = op_params(s);
+    RedP red = {s->d_part, s->d_ticket, s->d_sc, redkind};
+    dim3 grid(s->nchunk, s->nblk);
+    int nt = s->RM;
+    size_t smem = sizeof(double2) * 5 * (size_t)s->CM + sizeof(double) * NRED * nt;
+    prof_begin(s, st);
+    if (s->rc) k_apply<double, true><<<grid, nt, smem, st>>>(P, x, mode, V, red);
+    else k_apply<double, false><<<grid, nt, smem, st>>>(P, x, mode, V, red);
+    prof_end(s, st, 0);
+    CKL();
+    return GADE_OK;
+}
+
+static int launch_precond(gade_solver *s, int mode, const double2 *in0, const double2 *in1, double2 *io,
+                          double2 *out, cudaStream_t st)
+{
+    PcP Q = pc_params(s);
+    int grid = (s->nblk + s->wpc - 1) / s->wpc;
+    size_t smem = sizeof(double2) * (size_t)(s->Bp + 32) * s->wpc;
+    prof_begin(s, st);
+    k_precond<double><<<grid, 32 * s->wpc, smem, st>>>(Q, mode, in0, in1, io, out, s->d_sc);
+    prof_end(s, st, 1);
+    CKL();
+    return GADE_OK;
+}
+
+static int launch_tables(gade_solver *s, const double *ft)
+{
+    /* c_a = SoL * (i h dt/2) * f_a, as in tools/solver.c:274 */
+    const double hdt2 = s->h * s->dt / 2;
+    for (int l = 0; l < s->lmax; l++)
+        for (int ia = 0; ia < 3; ia++) {
+            int a = (l % 2 + 1) % 2 + 2 * ia;
+            double fr = ft[2 * a], fi = ft[2 * a + 1];
+            /* (SoL * (0 + i hdt2)) * (fr + i fi) */
+            double cr = 0.0 * SOL, ci = SOL * hdt2;
+            s->h_coef[l * 3 + ia] = make_double2(cr * fr - ci * fi, cr * fi + ci * fr);
+        }
+    if (s->rc)
+        for (int a = 0; a < 6; a++)
+            if (ft[2 * a + 1] != 0.0)
+                return fail(GADE_ERR_ARG, "pulse factor f_%d has an imaginary part; the real-coupling tables need real f(t)", a);
+    CK(cudaMemcpyAsync(s->d_coef, s->h_coef, sizeof(double2) * (size_t)s->lmax * 3, cudaMemcpyHostToDevice, s->stream));
+    TabP T;
+    T.lmax = s->lmax; T.nk = s->nk; T.W = s->W; T.B = s->B; T.blk_nnz = s->blk_nnz;
+    T.kvals = s->d_kvals; T.ell_pos = s->d_ell_pos; T.g = s->d_g; T.gt = s->d_gt; T.M = s->d_M;
+    long long total = (long long)s->lmax * s->W * s->B;
+    int nt = 256;
+    long long grid = (total + nt - 1) / nt;
+    prof_begin(s, s->stream);
+    if (s->rc) k_tables<double, true><<<(unsigned)grid, nt, 0, s->stream>>>(T, s->d_coef);
+    else k_tables<double, false><<<(unsigned)grid, nt, 0, s->stream>>>(T, s->d_coef);
+    prof_end(s, s->stream, 2);
+    CKL();
+    s->has_time = 1;
+    return GADE_OK;
+}
+
+static int sync_scal(gade_solver *s)
+{
+    CK(cudaMemcpyAsync(s->h_sc, s->d_sc, sizeof(DevScal), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return GADE_OK;
+}
+
+extern "C" int gade_solver_set_time(gade_solver *s, const double *ft)
+{
+    if (!s || !ft) return fail(GADE_ERR_ARG, "gade_solver_set_time: NULL argument");
+    CK(cudaSetDevice(s->device));
+    int rc = launch_tables(s, ft);
+    if (rc) return rc;
+    CK(cudaStreamSynchronize(s->stream));
+    return GADE_OK;
+}
+
+extern "C" int gade_solver_set_x(gade_solver *s, const double *x, int64_t n)
+{
+    if (!s || !x) return fail(GADE_ERR_ARG, "gade_solver_set_x: NULL argument");
+    if (n != s->n) return fail(GADE_ERR_ARG, "gade_solver_set_x: size %lld != %lld", (long long)n, s->n);
+    CK(cudaSetDevice(s->device));
+    CK(cudaMemcpyAsync(s->x, x, sizeof(double2) * (size_t)n, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return GADE_OK;
+}
+
+extern "C" int gade_solver_get_x(gade_solver *s, double *x, int64_t n)
+{
+    if (!s || !x) return fail(GADE_ERR_ARG, "gade_solver_get_x: NULL argument");
+    if (n != s->n) return fail(GADE_ERR_ARG, "gade_solver_get_x: size %lld != %lld", (long long)n, s->n);
+    CK(cudaSetDevice(s->device));
+    CK(cudaMemcpyAsync(x, s->x, sizeof(double2) * (size_t)n, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return GADE_OK;
+}
+
+extern "C" int gade_solver_apply(gade_solver *s, const double *x, double *y, double *Sx, double *Hx)
+{
+    if (!s || !x) return fail(GADE_ERR_ARG, "gade_solver_apply: NULL argument");
+    if (!s->has_time) return fail(GADE_ERR_STATE, "gade_solver_apply: call gade_solver_set_time first");
+    CK(cudaSetDevice(s->device));
+    const size_t bytes = sizeof(double2) * (size_t)s->n;
+    CK(cudaMemcpyAsync(s->tmp0, x, bytes, cudaMemcpyHostToDevice, s->stream));
+    VecP V = {};
+    int rc;
+    if (y) {
+        V.out0 = s->tmp1;
+        if ((rc = launch_apply(s, s->tmp0, AX_PLAIN, V, RED_NONE, s->stream))) return rc;
+        CK(cudaMemcpyAsync(y, s->tmp1, bytes, cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+    }
+    if (Sx || Hx) {
+        V.out0 = s->tmp1; V.out1 = s->s;   /* s is scratch here */
+        if ((rc = launch_apply(s, s->tmp0, AX_PARTS, V, RED_NONE, s->stream))) return rc;
+        if (Sx) CK(cudaMemcpyAsync(Sx, s->tmp1, bytes, cudaMemcpyDeviceToHost, s->stream));
+        if (Hx) CK(cudaMemcpyAsync(Hx, s->s, bytes, cudaMemcpyDeviceToHost, s->stream));
+    }
+    CK(cudaStreamSynchronize(s->stream));
+    return GADE_OK;
+}
+
+extern "C" int gade_solver_apply_device(gade_solver *s, const void *x_dev, void *y_dev, void *stream)
+{
+    if (!s || !x_dev || !y_dev) return fail(GADE_ERR_ARG, "gade_solver_apply_device: NULL argument");
+    if (!s->has_time) return fail(GADE_ERR_STATE, "gade_solver_apply_device: call gade_solver_set_time first");
+    VecP V = {};
+    V.out0 = y_dev;
+    return launch_apply(s, (const double2 *)x_dev, AX_PLAIN, V, RED_NONE,
+                        stream ? (cudaStream_t)stream : s->stream);
+}
+
+extern "C" int gade_solver_precond(gade_solver *s, const double *b, double *z)
+{
+    if (!s || !b || !z) return fail(GADE_ERR_ARG, "gade_solver_precond: NULL argument");
+    CK(cudaSetDevice(s->device));
+    const size_t bytes = sizeof(double2) * (size_t)s->n;
+    CK(cudaMemcpyAsync(s->tmp0, b, bytes, cudaMemcpyHostToDevice, s->stream));
+    int rc = launch_precond(s, PC_PLAIN, s->tmp0, nullptr, nullptr, s->tmp1, s->stream);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(z, s->tmp1, bytes, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return GADE_OK;
+}
+
+extern "C" int64_t gade_solver_launch_count(const gade_solver *s) { return s ? s->launches : -1; }
+
+extern "C" int gade_solver_step(gade_solver *s, const double *ft, int32_t maxit, double tol,
+                                gade_step_stats *stats)
+{
+    if (!s || !ft) return fail(GADE_ERR_ARG, "gade_solver_step: NULL argument");
+    if (maxit < 0) return fail(GADE_ERR_ARG, "gade_solver_step: maxit < 0");
+    CK(cudaSetDevice(s->device));
+    int rc;
+    gade_step_stats st = {};
+    if ((rc = launch_tables(s, ft))) return rc;
+    /* rhs = S x - H x, r = rhs - A x, r0 = r (tools/dirac_solver.c:533-536,
+       tools/gpu_bicgstab.c:169-181) */
+    VecP V = {};
+    V.out0 = s->rhs; V.out1 = s->r; V.out2 = s->r0;
+    if ((rc = launch_apply(s, s->x, AX_RHS, V, RED_RHS, s->stream))) return rc;
+    if ((rc = sync_scal(s))) return rc;
+    const double rhs_sqnorm = s->h_sc->rhs_sqnorm;
+    double r0_sqnorm = s->h_sc->r0_sqnorm;
+    if (!std::isfinite(rhs_sqnorm) || !std::isfinite(r0_sqnorm))
+        return fail(GADE_ERR_NUMERIC, "non-finite right-hand side or residual");
+    if (rhs_sqnorm == 0) {
+        CK(cudaMemsetAsync(s->x, 0, sizeof(double2) * (size_t)s->n, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        st.iters = 0; st.tol_error = 0;
+        if (stats) *stats = st;
+        return GADE_OK;
+    }
+    const double tol2 = tol * tol * rhs_sqnorm;
+    const double eps2 = 1e-12 * 1e-12;
+    if (r0_sqnorm < tol2) {
+        st.iters = 0; st.tol_error = sqrt(r0_sqnorm / rhs_sqnorm);
+        if (stats) *stats = st;
+        return GADE_OK;
+    }
+    int i = 0;
+    double rr = r0_sqnorm;
+    while (i < maxit) {
+        /* restart when r has become orthogonal to r0; the CPU build tests
+           the real part of rho (fabs of a C complex), tools/bicgstab.c:208 */
+        if (fabs(s->h_sc->rho.x) < eps2 * r0_sqnorm) {
+            VecP R = {};
+            R.in0 = s->rhs; R.out1 = s->r; R.out2 = s->r0;
+            if ((rc = launch_apply(s, s->x, AX_RESTART, R, RED_RESTART, s->stream))) return rc;
+            if ((rc = sync_scal(s))) return rc;
+            r0_sqnorm = s->h_sc->r0_sqnorm;
+            st.restarts++;
+        }
+        /* p = r + beta (p - w v); y = M^-1 p */
+        if ((rc = launch_precond(s, PC_P, s->r, s->v, s->p, s->y, s->stream))) return rc;
+        /* v = A y; alpha = rho / <r0, v> */
+        VecP A1 = {}; A1.out0 = s->v; A1.in0 = s->r0;
+        if ((rc = launch_apply(s, s->y, AX_R0V, A1, RED_R0V, s->stream))) return rc;
+        /* s = r - alpha v; z = M^-1 s */
+        if ((rc = launch_precond(s, PC_S, s->r, s->v, s->s, s->z, s->stream))) return rc;
+        /* t = A z; w = <t,s>/<t,t> */
+        VecP A2 = {}; A2.out0 = s->t; A2.in0 = s->s;
+        if ((rc = launch_apply(s, s->z, AX_TS, A2, RED_TS, s->stream))) return rc;
+        /* x += alpha y + w z; r = s - w t; |r|^2; rho = <r0, r> */
+        {
+            RedP red = {s->d_part, s->d_ticket, s->d_sc, RED_UPDATE};
+            prof_begin(s, s->stream);
+            k_update<double><<<s->upd_grid, s->upd_block, sizeof(double) * NRED * s->upd_block, s->stream>>>(
+                s->n, s->x, s->y, s->z, s->r, s->s, s->t, s->r0, red);
+            prof_end(s, s->stream, 2);
+            CKL();
+        }
+        if ((rc = sync_scal(s))) return rc;
+        rr = s->h_sc->rr;
+        if (!std::isfinite(rr)) return fail(GADE_ERR_NUMERIC, "BiCGSTAB residual became non-finite at iteration %d", i);
+        if (rr < tol2) break;
+        ++i;
+    }
+    st.iters = i;
+    st.tol_error = sqrt(rr / rhs_sqnorm);
+    if (stats) *stats = st;
+    return GADE_OK;
+}
+
+extern "C" int gade_solver_time_apply(gade_solver *s, int32_t reps, double *ms)
+{
+    if (!s || !ms || reps < 1) return fail(GADE_ERR_ARG, "gade_solver_time_apply: bad argument");
+    if (!s->has_time) return fail(GADE_ERR_STATE, "gade_solver_time_apply: call gade_solver_set_time first");
+    CK(cudaSetDevice(s->device));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1));
+    VecP V = {}; V.out0 = s->tmp1;
+    int rc;
+    if ((rc = launch_apply(s, s->x, AX_PLAIN, V, RED_NONE, s->stream))) return rc;
+    CK(cudaEventRecord(e0, s->stream));
+    for (int k = 0; k < reps; k++)
+        if ((rc = launch_apply(s, s->x, AX_PLAIN, V, RED_NONE, s->stream))) return rc;
+    CK(cudaEventRecord(e1, s->stream));
+    CK(cudaEventSynchronize(e1));
+    float t = 0;
+    CK(cudaEventElapsedTime(&t, e0, e1));
+    *ms = t / reps;
+    cudaEventDestroy(e0); cudaEventDestroy(e1);
+    return GADE_OK;
+}
+
+extern "C" int gade_solver_time_precond(gade_solver *s, int32_t reps, double *ms)
+{
+    if (!s || !ms || reps < 1) return fail(GADE_ERR_ARG, "gade_solver_time_precond: bad argument");
+    CK(cudaSetDevice(s->device));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1));
+    int rc;
+    if ((rc = launch_precond(s, PC_PLAIN, s->x, nullptr, nullptr, s->tmp1, s->stream))) return rc;
+    CK(cudaEventRecord(e0, s->stream));
+    for (int k = 0; k < reps; k++)
+        if ((rc = launch_precond(s, PC_PLAIN, s->x, nullptr, nullptr, s->tmp1, s->stream))) return rc;
+    CK(cudaEventRecord(e1, s->stream));
+    CK(cudaEventSynchronize(e1));
+    float t = 0;
+    CK(cudaEventElapsedTime(&t, e0, e1));
+    *ms = t / reps;
+    cudaEventDestroy(e0); cudaEventDestroy(e1);
+    return GADE_OK;
+}
+
+extern "C" void *gade_solver_stream(const gade_solver *s) { return s ? (void *)s->stream : nullptr; }
+
+extern "C" int gade_solver_profile(gade_solver *s, int32_t enable)
+{
+    if (!s) return fail(GADE_ERR_ARG, "gade_solver_profile: NULL solver");
+    CK(cudaSetDevice(s->device));
+    prof_collect(s);
+    s->profile = enable ? 1 : 0;
+    return GADE_OK;
+}
+
+extern "C" int gade_solver_kernel_times(gade_solver *s, gade_kernel_times *out)
+{
+    if (!s || !out) return fail(GADE_ERR_ARG, "gade_solver_kernel_times: NULL argument");
+    CK(cudaSetDevice(s->device));
+    CK(cudaStreamSynchronize(s->stream));
+    prof_collect(s);
+    out->apply_launches = s->prof_n[0]; out->apply_ms = s->prof_ms[0];
+    out->precond_launches = s->prof_n[1]; out->precond_ms = s->prof_ms[1];
+    out->other_launches = s->prof_n[2]; out->other_ms = s->prof_ms[2];
+    for (int k = 0; k < 3; k++) { s->prof_n[k] = 0; s->prof_ms[k] = 0; }
+    return GADE_OK;
+}
+
+/* 8 independent FMA chains per thread; 2 flops per FMA */
+__global__ void k_fp64_peak(double *out, int iters, double m, double c)
+{
+    double a0 = threadIdx.x * 1e-9, a1 = a0 + 1e-9, a2 = a0 + 2e-9, a3 = a0 + 3e-9;
+    double a4 = a0 + 4e-9, a5 = a0 + 5e-9, a6 = a0 + 6e-9, a7 = a0 + 7e-9;
+    for (int i = 0; i < iters; i++) {
+        a0 = fma(a0, m, c); a1 = fma(a1, m, c); a2 = fma(a2, m, c); a3 = fma(a3, m, c);
+        a4 = fma(a4, m, c); a5 = fma(a5, m, c); a6 = fma(a6, m, c); a7 = fma(a7, m, c);
+    }
+    double s = ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
+    if (s == 1234.5) out[blockIdx.x * blockDim.x + threadIdx.x] = s;   /* keep the chains live */
+}
+
+extern "C" int gade_probe_fp64_peak(int32_t device, double *tflops)
+{
+    if (!tflops) return fail(GADE_ERR_ARG, "gade_probe_fp64_peak: NULL argument");
+    CK(cudaSetDevice(device));
+    cudaDeviceProp prop;
+    CK(cudaGetDeviceProperties(&prop, device));
+    const int blocks = prop.multiProcessorCount * 8, threads = 256, iters = 4096;
+    double *out = nullptr;
+    CK(cudaMalloc(&out, sizeof(double) * blocks * threads));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1));
+    k_fp64_peak<<<blocks, threads>>>(out, iters, 0.9999999, 1e-12);   /* warm-up */
+    CK(cudaGetLastError());
+    float best = 1e30f;
+    for (int rep = 0; rep < 5; rep++) {
+        CK(cudaEventRecord(e0));
+        k_fp64_peak<<<blocks, threads>>>(out, iters, 0.9999999, 1e-12);
+        CK(cudaEventRecord(e1));
+        CK(cudaEventSynchronize(e1));
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best) best = ms;
+    }
+    cudaEventDestroy(e0); cudaEventDestroy(e1);
+    cudaFree(out);
+    const double flops = 2.0 * 8.0 * iters * (double)blocks * threads;
+    *tflops = flops / (best * 1e-3) / 1e12;
+    return GADE_OK;
+}

@@ -1,0 +1,240 @@
+"""ctypes binding of ``libgade_gb300.so`` (include/gade.h).
+
+The library is the product: there is no Python or CPU fallback.  Loading
+fails loudly when the shared library is missing or does not export the ABI.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+import os
+
+import numpy as np
+
+from . import build as _build
+
+GADE_PREC_FP64 = 0
+GADE_PREC_MIXED = 1
+
+
+class GadeError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"gade error {code}: {msg}")
+        self.code = code
+
+
+class ProblemInfo(C.Structure):
+    _fields_ = [("lmax", C.c_int32), ("nblk", C.c_int32), ("blkdim", C.c_int32), ("blk_nnz", C.c_int32),
+                ("n", C.c_int64), ("hall_nnz", C.c_int64), ("nnz_full", C.c_int64),
+                ("real_coupling", C.c_int32)]
+
+
+class StepStats(C.Structure):
+    _fields_ = [("iters", C.c_int32), ("tol_error", C.c_double), ("restarts", C.c_int32),
+                ("refinements", C.c_int32), ("inner_iters", C.c_int32), ("true_residual", C.c_double)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class KernelTimes(C.Structure):
+    _fields_ = [("apply_launches", C.c_int64), ("apply_ms", C.c_double),
+                ("precond_launches", C.c_int64), ("precond_ms", C.c_double),
+                ("other_launches", C.c_int64), ("other_ms", C.c_double)]
+
+
+_LIB = None
+
+# every entry point of include/gade.h with its ctypes signature
+_SIGS = {
+    "gade_last_error": (C.c_char_p, []),
+    "gade_problem_load": (C.c_int, [C.c_char_p, C.c_int32, C.POINTER(C.c_void_p)]),
+    "gade_problem_get_info": (C.c_int, [C.c_void_p, C.POINTER(ProblemInfo)]),
+    "gade_problem_get_psi0": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "gade_problem_free": (None, [C.c_void_p]),
+    "gade_solver_create": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int32, C.c_int32,
+                                     C.POINTER(C.c_void_p)]),
+    "gade_solver_free": (None, [C.c_void_p]),
+    "gade_solver_set_x": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),
+    "gade_solver_get_x": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),
+    "gade_solver_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_double, C.POINTER(StepStats)]),
+    "gade_solver_set_time": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "gade_solver_apply": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "gade_solver_precond": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "gade_solver_apply_device": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "gade_solver_launch_count": (C.c_int64, [C.c_void_p]),
+    "gade_solver_time_apply": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_double)]),
+    "gade_solver_time_precond": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_double)]),
+    "gade_solver_stream": (C.c_void_p, [C.c_void_p]),
+    "gade_solver_profile": (C.c_int, [C.c_void_p, C.c_int32]),
+    "gade_solver_kernel_times": (C.c_int, [C.c_void_p, C.POINTER(KernelTimes)]),
+    "gade_probe_fp64_peak": (C.c_int, [C.c_int32, C.POINTER(C.c_double)]),
+}
+
+
+def library_path() -> str:
+    return _build.library_path()
+
+
+def load_library() -> C.CDLL:
+    """Load libgade_gb300.so; raise if it has not been built."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = library_path()
+    if not os.path.exists(path):
+        raise GadeError(-1, f"{path} is missing: run dirac_hydrogen_code_gb300.build.build() "
+                            "(or __graft_entry__.build()) first; there is no fallback path")
+    lib = C.CDLL(path)
+    for name, (res, args) in _SIGS.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def _check(rc: int):
+    if rc != 0:
+        msg = load_library().gade_last_error().decode(errors="replace")
+        raise GadeError(rc, msg)
+
+
+def _cbuf(a: np.ndarray) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.complex128)
+
+
+class Problem:
+    """Host copy of the solver inputs (tools/dirac_solver.c:223-388)."""
+
+    def __init__(self, workdir: str, lmax: int):
+        lib = load_library()
+        h = C.c_void_p()
+        _check(lib.gade_problem_load(os.fsencode(workdir), int(lmax), C.byref(h)))
+        self._h = h
+        info = ProblemInfo()
+        _check(lib.gade_problem_get_info(h, C.byref(info)))
+        self.info = {k: getattr(info, k) for k, _ in ProblemInfo._fields_}
+        self.n = int(info.n)
+
+    def psi0(self) -> tuple[np.ndarray, np.ndarray]:
+        psi = np.empty(self.n, np.complex128)
+        perm = np.empty(self.n, np.int32)
+        _check(load_library().gade_problem_get_psi0(self._h, psi.ctypes.data, perm.ctypes.data))
+        return psi, perm
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load_library().gade_problem_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Solver:
+    """Device solver of one pulse; mirrors the reference GPU interface
+    (gpu_solver.h, gpu_sparse.h, gpu_bicgstab.h) through include/gade.h."""
+
+    def __init__(self, problem: Problem, dt: float, h: float = 1.0, precision: str = "fp64",
+                 device: int = 0):
+        lib = load_library()
+        prec = {"fp64": GADE_PREC_FP64, "mixed": GADE_PREC_MIXED}[precision]
+        hs = C.c_void_p()
+        _check(lib.gade_solver_create(problem._h, float(dt), float(h), prec, int(device), C.byref(hs)))
+        self._h = hs
+        self.n = problem.n
+        self.problem = problem
+
+    # gpu_put_vec / gpu_get_vec
+    def set_x(self, x: np.ndarray):
+        x = _cbuf(x)
+        if x.shape != (self.n,):
+            raise ValueError(f"state must have {self.n} entries")
+        _check(load_library().gade_solver_set_x(self._h, x.ctypes.data, self.n))
+
+    def get_x(self) -> np.ndarray:
+        x = np.empty(self.n, np.complex128)
+        _check(load_library().gade_solver_get_x(self._h, x.ctypes.data, self.n))
+        return x
+
+    # pgsum part of gpu_compute_timedep_matrices
+    def set_time(self, ft: np.ndarray):
+        ft = _cbuf(ft)
+        _check(load_library().gade_solver_set_time(self._h, ft.ctypes.data))
+
+    # gpu_HS_spmv_fun
+    def apply(self, x: np.ndarray, parts: bool = False):
+        x = _cbuf(x)
+        y = np.empty(self.n, np.complex128)
+        if parts:
+            sx = np.empty(self.n, np.complex128)
+            hx = np.empty(self.n, np.complex128)
+            _check(load_library().gade_solver_apply(self._h, x.ctypes.data, y.ctypes.data,
+                                                    sx.ctypes.data, hx.ctypes.data))
+            return y, sx, hx
+        _check(load_library().gade_solver_apply(self._h, x.ctypes.data, y.ctypes.data, None, None))
+        return y
+
+    # gpu_LU_precond_fun
+    def precond(self, b: np.ndarray) -> np.ndarray:
+        b = _cbuf(b)
+        z = np.empty(self.n, np.complex128)
+        _check(load_library().gade_solver_precond(self._h, b.ctypes.data, z.ctypes.data))
+        return z
+
+    # loop body of tools/dirac_solver.c:503-551
+    def step(self, ft: np.ndarray, maxit: int = 500, tol: float = 1e-16) -> dict:
+        ft = _cbuf(ft)
+        st = StepStats()
+        _check(load_library().gade_solver_step(self._h, ft.ctypes.data, int(maxit), float(tol), C.byref(st)))
+        return st.as_dict()
+
+    def apply_device(self, x_ptr: int, y_ptr: int, stream: int = 0):
+        _check(load_library().gade_solver_apply_device(self._h, C.c_void_p(x_ptr), C.c_void_p(y_ptr),
+                                                       C.c_void_p(stream) if stream else None))
+
+    def launch_count(self) -> int:
+        return int(load_library().gade_solver_launch_count(self._h))
+
+    def time_apply(self, reps: int = 20) -> float:
+        ms = C.c_double()
+        _check(load_library().gade_solver_time_apply(self._h, int(reps), C.byref(ms)))
+        return ms.value
+
+    def time_precond(self, reps: int = 20) -> float:
+        ms = C.c_double()
+        _check(load_library().gade_solver_time_precond(self._h, int(reps), C.byref(ms)))
+        return ms.value
+
+    def stream(self) -> int:
+        return int(load_library().gade_solver_stream(self._h) or 0)
+
+    def profile(self, enable: bool = True):
+        _check(load_library().gade_solver_profile(self._h, 1 if enable else 0))
+
+    def kernel_times(self) -> dict:
+        kt = KernelTimes()
+        _check(load_library().gade_solver_kernel_times(self._h, C.byref(kt)))
+        return {k: getattr(kt, k) for k, _ in KernelTimes._fields_}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load_library().gade_solver_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def fp64_peak_tflops(device: int = 0) -> float:
+    """Measured FP64 FMA throughput (TFLOP/s) of the device."""
+    v = C.c_double()
+    _check(load_library().gade_probe_fp64_peak(int(device), C.byref(v)))
+    return v.value

@@ -1,0 +1,151 @@
+/*
+ * gade.h — C ABI of the GB300-native Crank-Nicolson step of GaDE
+ * (JVembe/dirac_hydrogen_code, tools/ solver).
+ *
+ * One process, one GPU (sm_103a).  Plain C types only: complex numbers are
+ * interleaved (re, im) doubles, indices are int32/int64, streams are passed
+ * as void*.  Every entry point returns GADE_OK (0) or an error code; the
+ * message of the last error on the calling thread is gade_last_error().
+ * Nothing here calls exit(): the reference's ERROR()/CHECK_GPU() exits
+ * (tools/utils.h:42-46, tools/cuda_translate.h:100-125) become status codes.
+ *
+ * Each function cites the reference interface it replaces.
+ */
+#ifndef GADE_H
+#define GADE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GADE_OK            0
+#define GADE_ERR_IO        1   /* file cannot be opened                        */
+#define GADE_ERR_FORMAT    2   /* malformed input file                         */
+#define GADE_ERR_CUDA      3   /* CUDA runtime / launch failure                */
+#define GADE_ERR_ARG       4   /* invalid argument or size                     */
+#define GADE_ERR_NUMERIC   5   /* zero pivot, non-finite residual              */
+#define GADE_ERR_STATE     6   /* call order violated                          */
+
+/* precision of the time step */
+#define GADE_PREC_FP64     0   /* complex128 everywhere (reference parity)     */
+#define GADE_PREC_MIXED    1   /* complex64 inner BiCGSTAB in FP64 refinement  */
+
+typedef struct gade_problem gade_problem;   /* host copy of the input files  */
+typedef struct gade_solver  gade_solver;    /* device state of one pulse     */
+
+typedef struct {
+    int32_t lmax, nblk, blkdim, blk_nnz;
+    int64_t n;            /* state dimension nblk*blkdim                       */
+    int64_t hall_nnz;     /* non-zero blocks of H.csr                          */
+    int64_t nnz_full;     /* non-zeros of the assembled operator (reference)   */
+    int32_t real_coupling;/* 1: g real, H0l/H1l imaginary (fast path)          */
+} gade_problem_info;
+
+typedef struct {
+    int32_t iters;        /* reference semantics: index of breaking iteration  */
+    double  tol_error;    /* sqrt(|r|^2/|b|^2) of the recursive residual       */
+    int32_t restarts;     /* BiCGSTAB restarts (|rho| tiny)                     */
+    int32_t refinements;  /* outer FP64 refinement sweeps (mixed precision)    */
+    int32_t inner_iters;  /* total inner complex64 iterations (mixed)          */
+    double  true_residual;/* FP64 |b - A x|/|b| at exit (mixed precision only) */
+} gade_step_stats;
+
+/* Message of the last failing call on this thread ("" if none). */
+const char *gade_last_error(void);
+
+/* Reads H.csr, H0l<l>/H1l<l>.csr, g<q>a<a>l<l>.csr, h0<n>.csr, s<n>.csr and
+ * psi0.vec from dir, like tools/dirac_solver.c:223-388 (csr_read,
+ * csr_conj_transpose, vec_read, vec_read_perm). */
+int gade_problem_load(const char *dir, int32_t lmax, gade_problem **out);
+int gade_problem_get_info(const gade_problem *p, gade_problem_info *info);
+/* psi0.vec contents: psi (2n doubles) and perm (n int32), either may be NULL.
+ * Replaces vec_read/vec_read_perm (tools/dirac_solver.c:68-108). */
+int gade_problem_get_psi0(const gade_problem *p, double *psi, int32_t *perm);
+void gade_problem_free(gade_problem *p);
+
+/* Builds the device solver for a fixed time step dt (and h, always 1 in the
+ * reference): uploads the radial and angular tables, the stationary blocks
+ * and the block-LU preconditioner.  Replaces gpu_init_model_matrices +
+ * gpu_compute_row_col (tools/gpu_solver.cu:137-236, 288-327),
+ * compute_stationary_matrices + compute_preconditioner
+ * (tools/solver.c:409-485), slu_compute_ilu (tools/superlu.c:154-266),
+ * gpu_put_csr(L,U,S) + gpu_lu_analyze (tools/gpu_sparse.c:60-109,162-233)
+ * and gpu_sparse_init/gpu_blas_init.  x is set to psi0.
+ * precision: GADE_PREC_FP64 or GADE_PREC_MIXED. device: CUDA ordinal. */
+int gade_solver_create(const gade_problem *p, double dt, double h, int32_t precision,
+                       int32_t device, gade_solver **out);
+void gade_solver_free(gade_solver *s);
+
+/* State vector in the solver's (permuted) order; 2n doubles.
+ * Replaces gpu_put_vec / gpu_get_vec (tools/gpu_sparse.c:120-152). */
+int gade_solver_set_x(gade_solver *s, const double *x, int64_t n);
+int gade_solver_get_x(gade_solver *s, double *x, int64_t n);
+
+/* One Crank-Nicolson step at time t with pulse factors ft (6 complex, i.e.
+ * 12 doubles, beoyndDipolePulse_axialPart at t): assembles nothing — the
+ * operator S + H(t) is applied matrix-free — then forms
+ * rhs = S x - H(t) x and solves (S + H(t)) x' = rhs with right-block-LU-
+ * preconditioned BiCGSTAB warm-started at x.  Replaces the loop body
+ * tools/dirac_solver.c:503-551 (gpu_compute_timedep_matrices, gpu_spmv,
+ * gpu_spmv_local, gpu_bicgstab of tools/gpu_bicgstab.c:133-307).
+ * maxit/tol: the reference hard-codes 500 and 1e-16 (dirac_solver.c:506-507).
+ * stats may be NULL. */
+int gade_solver_step(gade_solver *s, const double *ft, int32_t maxit, double tol,
+                     gade_step_stats *stats);
+
+/* Sets the time-dependent radial tables for pulse factors ft without solving
+ * (the pgsum part of gpu_compute_timedep_matrices, tools/gpu_solver.cu:50-82). */
+int gade_solver_set_time(gade_solver *s, const double *ft);
+
+/* y = S x + H(t) x for host vectors (2n doubles each), with the tables of
+ * the last set_time/step.  Replaces gpu_HS_spmv_fun
+ * (tools/dirac_solver.c:141-156) with alpha=1, beta=0.  Sx and Hx may be
+ * NULL; when given they receive the two parts separately
+ * (gpu_spmv_local(S) and gpu_spmv(Hfull), tools/gpu_sparse.c:267-313). */
+int gade_solver_apply(gade_solver *s, const double *x, double *y, double *Sx, double *Hx);
+
+/* z = (P^T)^{-1} b with P = S + i h dt/2 h0 block diagonal.  Replaces
+ * gpu_LU_precond_fun / gpu_lu_solve (tools/dirac_solver.c:158-165,
+ * tools/gpu_sparse.c:235-263) and slu_lu_solve (tools/superlu.c:268-290). */
+int gade_solver_precond(gade_solver *s, const double *b, double *z);
+
+/* Device-resident variants: x, y are device pointers to n complex128 values
+ * in HBM, stream is a cudaStream_t passed as void* (NULL: the solver's
+ * stream).  No host synchronisation. */
+int gade_solver_apply_device(gade_solver *s, const void *x_dev, void *y_dev, void *stream);
+
+/* Number of this library's kernel launches since creation (instrumentation). */
+int64_t gade_solver_launch_count(const gade_solver *s);
+
+/* Device time of the last apply issued by gade_solver_time_apply, and a
+ * helper that times `reps` back-to-back operator applies with CUDA events on
+ * the solver's stream; ms receives the average. */
+int gade_solver_time_apply(gade_solver *s, int32_t reps, double *ms);
+int gade_solver_time_precond(gade_solver *s, int32_t reps, double *ms);
+
+/* The cudaStream_t (as void*) on which every call of this solver is ordered;
+ * callers record their own CUDA events on it. */
+void *gade_solver_stream(const gade_solver *s);
+
+/* Device time of this solver's kernels, measured with CUDA events around each
+ * launch while enabled (off by default; no reference counterpart — the
+ * reference times whole BiCGSTAB calls with gettimeofday, tools/dirac_solver.c:547-551). */
+typedef struct {
+    int64_t apply_launches;   double apply_ms;     /* matrix-free operator      */
+    int64_t precond_launches; double precond_ms;   /* block-LU solves           */
+    int64_t other_launches;   double other_ms;     /* tables, vector updates    */
+} gade_kernel_times;
+int gade_solver_profile(gade_solver *s, int32_t enable);
+/* Synchronises, returns the accumulated times and resets them. */
+int gade_solver_kernel_times(gade_solver *s, gade_kernel_times *out);
+
+/* Measured FP64 FMA throughput of a device in TFLOP/s (2 flops per DFMA),
+ * from a dependent-chain-free FMA kernel timed with CUDA events. */
+int gade_probe_fp64_peak(int32_t device, double *tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GADE_H */
