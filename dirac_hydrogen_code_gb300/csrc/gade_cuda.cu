@@ -629,6 +629,7 @@ struct gade_solver {
     size_t ev_used;
     long long prof_n[3];
     double prof_ms[3];
+    double apply_flops, precond_flops;   /* FP64 flops of one launch */
 };
 
 static void prof_begin(gade_solver *s, cudaStream_t st)
@@ -882,6 +883,23 @@ extern "C" int gade_solver_create(const gade_problem *p, double dt, double h, in
         size_t smem = sizeof(double2) * (size_t)(s->Bp + 32) * s->wpc;
         if (smem > 48 * 1024)
             cudaFuncSetAttribute(k_precond<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    }
+    {
+        /* exact FP64 flop count of one operator apply (2 per FMA) */
+        const double fma_c = s->rc ? 2.0 : 4.0;     /* FMAs of one coupling term */
+        double fmas = 8.0 * (double)p->blk_nnz * s->nblk;             /* diagonal blocks */
+        for (int r = 0; r < s->nblk; r++)
+            for (int a = su->act_ptr[r]; a < su->act_ptr[r + 1]; a++) {
+                int l = su->act_l[a];
+                double ne = su->ang_ptr[r * s->lmax + l + 1] - su->ang_ptr[r * s->lmax + l];
+                double cols = 0;
+                for (int q = 0; q < s->nchunk; q++) cols += su->chunk_ncols[q];
+                fmas += 4.0 * fma_c * ne * cols;                       /* gather u, w, u', w' */
+                fmas += 4.0 * fma_c * (double)p->blk_nnz;              /* radial tables */
+            }
+        s->apply_flops = 2.0 * fmas;
+        /* block solves: per lane and chunk, bw band terms + 32 inverse terms, 2 sweeps */
+        s->precond_flops = 2.0 * 4.0 * (double)s->nblk * 32.0 * s->nch * 2.0 * (s->bw + 32);
     }
     gade_setup_release(su);
     *out = s;
@@ -1240,5 +1258,13 @@ extern "C" int gade_probe_fp64_peak(int32_t device, double *tflops)
     cudaFree(out);
     const double flops = 2.0 * 8.0 * iters * (double)blocks * threads;
     *tflops = flops / (best * 1e-3) / 1e12;
+    return GADE_OK;
+}
+
+extern "C" int gade_solver_flops(const gade_solver *s, double *apply_flops, double *precond_flops)
+{
+    if (!s) return fail(GADE_ERR_ARG, "gade_solver_flops: NULL solver");
+    if (apply_flops) *apply_flops = s->apply_flops;
+    if (precond_flops) *precond_flops = s->precond_flops;
     return GADE_OK;
 }

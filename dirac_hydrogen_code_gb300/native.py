@@ -69,6 +69,7 @@ _SIGS = {
     "gade_solver_profile": (C.c_int, [C.c_void_p, C.c_int32]),
     "gade_solver_kernel_times": (C.c_int, [C.c_void_p, C.POINTER(KernelTimes)]),
     "gade_probe_fp64_peak": (C.c_int, [C.c_int32, C.POINTER(C.c_double)]),
+    "gade_solver_flops": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
 }
 
 
@@ -220,6 +221,12 @@ class Solver:
         kt = KernelTimes()
         _check(load_library().gade_solver_kernel_times(self._h, C.byref(kt)))
         return {k: getattr(kt, k) for k, _ in KernelTimes._fields_}
+
+    def flops(self) -> tuple[float, float]:
+        """(FP64 flops of one operator apply, of one preconditioner solve)."""
+        a, b = C.c_double(), C.c_double()
+        _check(load_library().gade_solver_flops(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def close(self):
         if getattr(self, "_h", None):

@@ -141,6 +141,10 @@ int gade_solver_profile(gade_solver *s, int32_t enable);
 /* Synchronises, returns the accumulated times and resets them. */
 int gade_solver_kernel_times(gade_solver *s, gade_kernel_times *out);
 
+/* FP64 flops (2 per FMA) executed by one operator apply and one
+ * preconditioner solve, counted exactly from the set-up structure. */
+int gade_solver_flops(const gade_solver *s, double *apply_flops, double *precond_flops);
+
 /* Measured FP64 FMA throughput of a device in TFLOP/s (2 flops per DFMA),
  * from a dependent-chain-free FMA kernel timed with CUDA events. */
 int gade_probe_fp64_peak(int32_t device, double *tflops);

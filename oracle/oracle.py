@@ -361,6 +361,7 @@ class StepRecord:
     time: float
     iters: int
     tol_error: float
+    elapsed: float = 0.0          # wall seconds of the step (assembly + rhs + solve)
 
 
 def run(workdir: str, maxtime: float, lmax: int, E0: float, omega: float, cycles: float,
@@ -383,12 +384,13 @@ def run(workdir: str, maxtime: float, lmax: int, E0: float, omega: float, cycles
         if max_steps is not None and len(recs) >= max_steps:
             break
         t = t + dt
+        t0 = _time.perf_counter()
         ft = pulse(E0, omega, cycles, t)
         H = timedep(p, dt, ft, h)
         rhs = -(H @ x) + S @ x
         mv = lambda y: H @ y + S @ y
         iters, tol_err = bicgstab(mv, rhs, x, M.solve, wsp, maxit, tol)
-        recs.append(StepRecord(it, t, iters, tol_err))
+        recs.append(StepRecord(it, t, iters, tol_err, _time.perf_counter() - t0))
         if callback is not None:
             callback(it, t, x)
         it += 1
