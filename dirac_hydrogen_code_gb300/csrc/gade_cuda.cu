@@ -128,7 +128,9 @@ struct DevScal {
     double r0_sqnorm, rhs_sqnorm, rr;
     double2 r0v, ts;
     double tt;
-    double pad[4];
+    unsigned int err;      /* bit 0: a bounded mbarrier wait timed out */
+    unsigned int pad0;
+    double pad[3];
 };
 
 enum { RED_RHS = 0, RED_RESTART, RED_R0V, RED_TS, RED_UPDATE, RED_NONE };
@@ -447,61 +449,108 @@ __global__ void __launch_bounds__(128) k_apply(OpP P, const typename Cx<R>::T *_
 }
 
 /* ------------------------------------------------------------------ */
-/* block-LU preconditioner                                             */
+/* block-LU preconditioner, TMA-staged factors                          */
 /* ------------------------------------------------------------------ */
-struct PcP {
-    int nblk, B, bw, Bp, nch, wpc;
+/* Factor data of one 32-row chunk is contiguous in HBM:
+ *   [Linv (32x32, column-major [j][lane])][band: BWP rows [d][lane] holding
+ *   L(o, o-d-1) only where that source row lies before the chunk, else 0]
+ * (and the same for U with the sources after the chunk).  One elected lane
+ * streams chunk k+1 into shared memory with cp.async.bulk on an mbarrier
+ * while the warp computes chunk k.  Every wait is bounded: on timeout the
+ * kernel sets sc->err, drains its copies (bounded) and returns. */
+struct PcT {
+    int nblk, B, Bp, nch;
     const int *row_kidx, *ord;
-    const void *Lb, *Ub, *Linv, *Uinv;
+    const double2 *FL, *FU;        /* [nk][nch][CH] */
 };
 
-/* one warp per block row; wpc warps per CTA.
- * mode PC_PLAIN: b = in0
- * mode PC_P    : p = r + beta (p - w v)  (in0 = r, io = p, in1 = v); b = p
- * mode PC_S    : s = r - alpha v         (in0 = r, in1 = v, out s);   b = s  */
-template <typename R>
-__global__ void k_precond(PcP Q, int mode, const typename Cx<R>::T *__restrict__ in0,
-                          const typename Cx<R>::T *__restrict__ in1, typename Cx<R>::T *io,
-                          typename Cx<R>::T *__restrict__ out, const DevScal *__restrict__ sc)
+__device__ __forceinline__ unsigned smem_u32(const void *p)
 {
-    typedef typename Cx<R>::T C;
-    extern __shared__ unsigned char smem_raw[];
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int r = blockIdx.x * Q.wpc + warp;
-    C *buf = (C *)smem_raw + (size_t)warp * (Q.Bp + 32);
-    C *tb = buf + Q.Bp;
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity)
+{
+    unsigned ok;
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(smem_u32(bar)), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ void tma_bulk_load(void *dst, const void *src, unsigned bytes, uint64_t *bar)
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+#define MBAR_SPIN_LIMIT (1u << 22)
+
+template <int BWP>
+__global__ void __launch_bounds__(32) k_precond_tma(PcT Q, int mode, const double2 *__restrict__ in0,
+                                                    const double2 *__restrict__ in1, double2 *io,
+                                                    double2 *__restrict__ out, DevScal *sc)
+{
+    constexpr int CH = 1024 + 32 * BWP;
+    extern __shared__ __align__(128) unsigned char smem_tma[];
+    double2 *fac = (double2 *)smem_tma;          /* [2][CH] */
+    double2 *buf = fac + 2 * CH;                 /* [Bp]    */
+    double2 *tb = buf + Q.Bp;                    /* [32]    */
+    __shared__ __align__(8) uint64_t bar[2];
+    const int lane = threadIdx.x, r = blockIdx.x;
     if (r >= Q.nblk) return;
-    const int B = Q.B, Bp = Q.Bp, bw = Q.bw;
+    const int B = Q.B, Bp = Q.Bp, nch = Q.nch;
     const int kk = Q.row_kidx[r];
     const size_t off = (size_t)r * B;
+    const double2 *FL = Q.FL + (size_t)kk * nch * CH;
+    const double2 *FU = Q.FU + (size_t)kk * nch * CH;
+    const unsigned bytes = CH * sizeof(double2);
 
-    C beta = mk<C>(0, 0), negw = mk<C>(0, 0), nega = mk<C>(0, 0);
+    if (lane == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        tma_bulk_load(fac, FL, bytes, &bar[0]);          /* first forward chunk */
+    }
+
+    double2 beta = make_double2(0, 0), negw = make_double2(0, 0), nega = make_double2(0, 0);
     if (mode == PC_P) {
         const double2 a = cdiv(sc->rho, sc->rho_prev);
         const double2 b = cdiv(sc->alpha, sc->w);
-        beta = mk<C>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-        negw = mk<C>(-sc->w.x, -sc->w.y);
+        beta = make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+        negw = make_double2(-sc->w.x, -sc->w.y);
     } else if (mode == PC_S) {
-        nega = mk<C>(-sc->alpha.x, -sc->alpha.y);
+        nega = make_double2(-sc->alpha.x, -sc->alpha.y);
     }
-    /* load (and update) the right-hand side in the banded ordering */
     for (int o = lane; o < Bp; o += 32) {
-        C val = mk<C>(0, 0);
+        double2 val = make_double2(0, 0);
         if (o < B) {
-            const int n = Q.ord[o];
-            const size_t gi = off + n;
+            const size_t gi = off + Q.ord[o];
             if (mode == PC_PLAIN) {
                 val = in0[gi];
             } else if (mode == PC_P) {
-                C t = io[gi];
-                cfma(t, negw, in1[gi]);            /* p - w v */
-                C pv = in0[gi];
-                cfma(pv, beta, t);                 /* r + beta (p - w v) */
+                double2 t = io[gi];
+                cfma(t, negw, in1[gi]);
+                double2 pv = in0[gi];
+                cfma(pv, beta, t);
                 io[gi] = pv;
                 val = pv;
             } else {
-                C sv = in0[gi];
-                cfma(sv, nega, in1[gi]);           /* r - alpha v */
+                double2 sv = in0[gi];
+                cfma(sv, nega, in1[gi]);
                 io[gi] = sv;
                 val = sv;
             }
@@ -509,51 +558,68 @@ __global__ void k_precond(PcP Q, int mode, const typename Cx<R>::T *__restrict__
         buf[o] = val;
     }
     __syncwarp();
-    const C *Lb = (const C *)Q.Lb + (size_t)kk * bw * Bp;
-    const C *Ub = (const C *)Q.Ub + (size_t)kk * bw * Bp;
-    const C *Li = (const C *)Q.Linv + (size_t)kk * Q.nch * 1024;
-    const C *Ui = (const C *)Q.Uinv + (size_t)kk * Q.nch * 1024;
-    /* forward: L y = b */
-    for (int c = 0; c < Q.nch; c++) {
+
+    const int nk = 2 * nch;           /* chunk steps: forward then backward */
+    bool ok = true;
+    int k = 0;
+    for (; k < nk; k++) {
+        const int fwd = k < nch;
+        const int c = fwd ? k : nch - 1 - (k - nch);
+        if (lane == 0 && k + 1 < nk) {
+            const int k1 = k + 1;
+            const int c1 = k1 < nch ? k1 : nch - 1 - (k1 - nch);
+            const double2 *src = (k1 < nch ? FL : FU) + (size_t)c1 * CH;
+            tma_bulk_load(fac + (k1 & 1) * CH, src, bytes, &bar[k1 & 1]);
+        }
+        unsigned spins = 0;
+        while (!mbar_try_wait(&bar[k & 1], (k >> 1) & 1)) {
+            if (++spins > MBAR_SPIN_LIMIT) { ok = false; break; }
+        }
+        if (!__all_sync(0xffffffffu, ok)) { ok = false; break; }
+        const double2 *F = fac + (k & 1) * CH;
         const int o = 32 * c + lane;
-        C t = buf[o];
-        for (int d = 1; d <= bw; d++) {
-            const int src = o - d;
-            if (src >= 32 * c) continue;            /* inside this chunk: via Linv */
-            if (src < 0) break;
-            C lv = Lb[(size_t)(d - 1) * Bp + o];
-            lv.x = -lv.x; lv.y = -lv.y;
-            cfma(t, lv, buf[src]);
+        double2 t = buf[o];
+        if (fwd) {
+#pragma unroll
+            for (int d = 1; d <= BWP; d++) {
+                double2 lv = F[1024 + (d - 1) * 32 + lane];
+                lv.x = -lv.x; lv.y = -lv.y;
+                cfma(t, lv, buf[o - d >= 0 ? o - d : 0]);
+            }
+        } else {
+#pragma unroll
+            for (int d = 1; d <= BWP; d++) {
+                double2 uv = F[1024 + (d - 1) * 32 + lane];
+                uv.x = -uv.x; uv.y = -uv.y;
+                cfma(t, uv, buf[o + d < Bp ? o + d : Bp - 1]);
+            }
         }
         tb[lane] = t;
         __syncwarp();
-        C y = mk<C>(0, 0);
-        const C *Lc = Li + (size_t)c * 1024;
-        for (int j = 0; j <= lane; j++) cfma(y, Lc[j * 32 + lane], tb[j]);
+        double2 a0 = make_double2(0, 0), a1 = a0, a2 = a0, a3 = a0;
+#pragma unroll
+        for (int j = 0; j < 32; j += 4) {
+            cfma(a0, F[(j + 0) * 32 + lane], tb[j + 0]);
+            cfma(a1, F[(j + 1) * 32 + lane], tb[j + 1]);
+            cfma(a2, F[(j + 2) * 32 + lane], tb[j + 2]);
+            cfma(a3, F[(j + 3) * 32 + lane], tb[j + 3]);
+        }
         __syncwarp();
-        buf[o] = y;
+        buf[o] = make_double2((a0.x + a1.x) + (a2.x + a3.x), (a0.y + a1.y) + (a2.y + a3.y));
         __syncwarp();
     }
-    /* backward: U x = y */
-    for (int c = Q.nch - 1; c >= 0; c--) {
-        const int o = 32 * c + lane;
-        C t = buf[o];
-        for (int d = 1; d <= bw; d++) {
-            const int src = o + d;
-            if (src < 32 * (c + 1)) continue;
-            if (src >= B) break;
-            C uv = Ub[(size_t)(d - 1) * Bp + o];
-            uv.x = -uv.x; uv.y = -uv.y;
-            cfma(t, uv, buf[src]);
+    if (!ok) {
+        if (lane == 0) {
+            atomicOr(&sc->err, 1u);
+            /* drain the copies still in flight (bounded) before exiting */
+            for (int kk2 = k; kk2 < k + 2 && kk2 < nk; kk2++) {
+                unsigned spins = 0;
+                while (!mbar_try_wait(&bar[kk2 & 1], (kk2 >> 1) & 1) && ++spins < MBAR_SPIN_LIMIT) {
+                }
+            }
         }
-        tb[lane] = t;
         __syncwarp();
-        C xv = mk<C>(0, 0);
-        const C *Uc = Ui + (size_t)c * 1024;
-        for (int j = lane; j < 32; j++) cfma(xv, Uc[j * 32 + lane], tb[j]);
-        __syncwarp();
-        buf[o] = xv;
-        __syncwarp();
+        return;
     }
     for (int o = lane; o < B; o += 32) out[off + Q.ord[o]] = buf[o];
 }
@@ -598,7 +664,7 @@ struct gade_solver {
     int prec, rc;
     long long n;
     int nblk, B, lmax, W, nk, RM, CM, nchunk;
-    int bw, Bp, nch, wpc;
+    int bw, Bp, nch;
     double dt, h;
     /* operator tables */
     int *d_row_kidx, *d_act_ptr, *d_act_l, *d_ang_ptr, *d_ang_c;
@@ -611,6 +677,8 @@ struct gade_solver {
     /* preconditioner */
     int *d_ord;
     void *d_Lb, *d_Ub, *d_Linv, *d_Uinv;
+    double2 *d_FL, *d_FU;       /* chunk-packed factors for the TMA kernel */
+    int bwp;
     /* vectors */
     double2 *x, *rhs, *r, *r0, *p, *v, *y, *z, *s, *t, *tmp0, *tmp1;
     /* reductions */
@@ -855,12 +923,39 @@ extern "C" int gade_solver_create(const gade_problem *p, double dt, double h, in
         UP(d, (const double2 *)su->Uinv, (size_t)s->nk * s->nch * 1024); s->d_Uinv = d;
     }
     {
-        size_t per_warp = sizeof(double2) * (size_t)(s->Bp + 32);
-        int wpc = (int)((48 * 1024) / per_warp);
-        if (wpc > 4) wpc = 4;
-        if (wpc < 1) wpc = 1;
-        s->wpc = wpc;
-        if (per_warp * wpc > 200 * 1024) { gade_setup_release(su); gade_solver_free(s); return fail(GADE_ERR_ARG, "block dimension too large"); }
+        /* chunk-packed factors: [nk][nch][Linv | masked band] */
+        s->bwp = s->bw <= 16 ? 16 : 32;
+        if (s->bw > 32) { gade_setup_release(su); gade_solver_free(s); return fail(GADE_ERR_ARG, "preconditioner band %d wider than 32 is not supported", s->bw); }
+        const int CH = 1024 + 32 * s->bwp;
+        std::vector<double2> FL((size_t)s->nk * s->nch * CH), FU((size_t)s->nk * s->nch * CH);
+        for (int kk = 0; kk < s->nk; kk++)
+            for (int c = 0; c < s->nch; c++) {
+                double2 *fl = &FL[((size_t)kk * s->nch + c) * CH];
+                double2 *fu = &FU[((size_t)kk * s->nch + c) * CH];
+                memcpy(fl, su->Linv + ((size_t)kk * s->nch + c) * 1024, 1024 * sizeof(double2));
+                memcpy(fu, su->Uinv + ((size_t)kk * s->nch + c) * 1024, 1024 * sizeof(double2));
+                for (int d = 1; d <= s->bwp; d++)
+                    for (int lane = 0; lane < 32; lane++) {
+                        int o = 32 * c + lane;
+                        double2 lv = make_double2(0, 0), uv = make_double2(0, 0);
+                        if (d <= s->bw && o - d >= 0 && o - d < 32 * c) {
+                            gc64 v = su->Lb[((size_t)kk * s->bw + d - 1) * s->Bp + o];
+                            lv = make_double2(v.re, v.im);
+                        }
+                        if (d <= s->bw && o + d < s->B && o + d >= 32 * (c + 1)) {
+                            gc64 v = su->Ub[((size_t)kk * s->bw + d - 1) * s->Bp + o];
+                            uv = make_double2(v.re, v.im);
+                        }
+                        fl[1024 + (d - 1) * 32 + lane] = lv;
+                        fu[1024 + (d - 1) * 32 + lane] = uv;
+                    }
+            }
+        UP(s->d_FL, FL.data(), FL.size());
+        UP(s->d_FU, FU.data(), FU.size());
+        size_t smem = sizeof(double2) * ((size_t)2 * CH + s->Bp + 32);
+        if (smem > 220 * 1024) { gade_setup_release(su); gade_solver_free(s); return fail(GADE_ERR_ARG, "block dimension too large for the preconditioner"); }
+        cudaFuncSetAttribute(k_precond_tma<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_precond_tma<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     }
     /* vectors */
     double2 **vecs[] = {&s->x, &s->rhs, &s->r, &s->r0, &s->p, &s->v, &s->y, &s->z, &s->s, &s->t, &s->tmp0, &s->tmp1};
@@ -880,11 +975,6 @@ extern "C" int gade_solver_create(const gade_problem *p, double dt, double h, in
         gade_setup_release(su); gade_solver_free(s); return fail(GADE_ERR_CUDA, "pinned allocation failed");
     }
     {
-        size_t smem = sizeof(double2) * (size_t)(s->Bp + 32) * s->wpc;
-        if (smem > 48 * 1024)
-            cudaFuncSetAttribute(k_precond<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    }
-    {
         /* exact FP64 flop count of one operator apply (2 per FMA) */
         const double fma_c = s->rc ? 2.0 : 4.0;     /* FMAs of one coupling term */
         double fmas = 8.0 * (double)p->blk_nnz * s->nblk;             /* diagonal blocks */
@@ -899,7 +989,7 @@ extern "C" int gade_solver_create(const gade_problem *p, double dt, double h, in
             }
         s->apply_flops = 2.0 * fmas;
         /* block solves: per lane and chunk, bw band terms + 32 inverse terms, 2 sweeps */
-        s->precond_flops = 2.0 * 4.0 * (double)s->nblk * 32.0 * s->nch * 2.0 * (s->bw + 32);
+        s->precond_flops = 2.0 * 4.0 * (double)s->nblk * 32.0 * s->nch * 2.0 * (s->bwp + 32);
     }
     gade_setup_release(su);
     *out = s;
@@ -917,15 +1007,6 @@ static OpP op_params(const gade_solver *s)
     P.chunk_cols = s->d_chunk_cols; P.chunk_lcol = s->d_chunk_lcol;
     P.M = s->d_M; P.S_ell = s->d_S_ell; P.Hst_ell = s->d_Hst_ell;
     return P;
-}
-
-static PcP pc_params(const gade_solver *s)
-{
-    PcP Q;
-    Q.nblk = s->nblk; Q.B = s->B; Q.bw = s->bw; Q.Bp = s->Bp; Q.nch = s->nch; Q.wpc = s->wpc;
-    Q.row_kidx = s->d_row_kidx; Q.ord = s->d_ord;
-    Q.Lb = s->d_Lb; Q.Ub = s->d_Ub; Q.Linv = s->d_Linv; Q.Uinv = s->d_Uinv;
-    return Q;
 }
 
 static int launch_apply(gade_solver *s, const double2 *x, int mode, VecP V, int redkind, cudaStream_t st)
@@ -946,11 +1027,14 @@ static int launch_apply(gade_solver *s, const double2 *x, int mode, VecP V, int 
 static int launch_precond(gade_solver *s, int mode, const double2 *in0, const double2 *in1, double2 *io,
                           double2 *out, cudaStream_t st)
 {
-    PcP Q = pc_params(s);
-    int grid = (s->nblk + s->wpc - 1) / s->wpc;
-    size_t smem = sizeof(double2) * (size_t)(s->Bp + 32) * s->wpc;
+    PcT Q;
+    Q.nblk = s->nblk; Q.B = s->B; Q.Bp = s->Bp; Q.nch = s->nch;
+    Q.row_kidx = s->d_row_kidx; Q.ord = s->d_ord; Q.FL = s->d_FL; Q.FU = s->d_FU;
+    const int CH = 1024 + 32 * s->bwp;
+    size_t smem = sizeof(double2) * ((size_t)2 * CH + s->Bp + 32);
     prof_begin(s, st);
-    k_precond<double><<<grid, 32 * s->wpc, smem, st>>>(Q, mode, in0, in1, io, out, s->d_sc);
+    if (s->bwp == 16) k_precond_tma<16><<<s->nblk, 32, smem, st>>>(Q, mode, in0, in1, io, out, s->d_sc);
+    else k_precond_tma<32><<<s->nblk, 32, smem, st>>>(Q, mode, in0, in1, io, out, s->d_sc);
     prof_end(s, st, 1);
     CKL();
     return GADE_OK;
@@ -992,6 +1076,11 @@ static int sync_scal(gade_solver *s)
 {
     CK(cudaMemcpyAsync(s->h_sc, s->d_sc, sizeof(DevScal), cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
+    if (s->h_sc->err) {
+        unsigned e = s->h_sc->err;
+        CK(cudaMemsetAsync(&s->d_sc->err, 0, sizeof(unsigned), s->stream));
+        return fail(GADE_ERR_CUDA, "device wait timed out (flags %u): TMA copy did not complete", e);
+    }
     return GADE_OK;
 }
 
@@ -1069,8 +1158,7 @@ extern "C" int gade_solver_precond(gade_solver *s, const double *b, double *z)
     int rc = launch_precond(s, PC_PLAIN, s->tmp0, nullptr, nullptr, s->tmp1, s->stream);
     if (rc) return rc;
     CK(cudaMemcpyAsync(z, s->tmp1, bytes, cudaMemcpyDeviceToHost, s->stream));
-    CK(cudaStreamSynchronize(s->stream));
-    return GADE_OK;
+    return sync_scal(s);
 }
 
 extern "C" int64_t gade_solver_launch_count(const gade_solver *s) { return s ? s->launches : -1; }
