@@ -148,7 +148,7 @@ struct OpP {
     const void *ang_a0, *ang_a0k, *ang_a1, *ang_a1k;
     const int *chunk_nrows, *chunk_ncols, *chunk_rows, *chunk_cols, *chunk_lcol;
     const void *M;             /* [lmax][nk][W][B] */
-    const void *S_ell, *Hst_ell;
+    const void *S_ell, *Hst_ell, *D_ell;
 };
 
 struct VecP {
@@ -321,39 +321,53 @@ __global__ void __launch_bounds__(128) k_apply(OpP P, const typename Cx<R>::T *_
     typedef typename Cx<R>::T C;
     extern __shared__ unsigned char smem_raw[];
     C *xr = (C *)smem_raw;                    /* [CM] */
-    C *u0 = xr + P.CM, *u1 = u0 + P.CM, *u2 = u1 + P.CM, *u3 = u2 + P.CM;
-    double *shred = (double *)(u3 + P.CM);    /* [NRED * blockDim] */
+    C *ub = xr + P.CM;                        /* [2][4][CM] double-buffered u, w, u', w' */
+    double *shred = (double *)(ub + 8 * P.CM); /* [NRED * blockDim] */
 
     const int q = blockIdx.x, r = blockIdx.y, tid = threadIdx.x, nt = blockDim.x;
-    const int B = P.B, W = P.W;
+    const int B = P.B, W = P.W, CM = P.CM;
     const int kk = P.row_kidx[r];
     const int nrows = P.chunk_nrows[q], ncols = P.chunk_ncols[q];
     const int i = (tid < nrows) ? P.chunk_rows[q * P.RM + tid] : -1;
-    const int *cols = P.chunk_cols + (size_t)q * P.CM;
+    const int *cols = P.chunk_cols + (size_t)q * CM;
     const int *lcol = P.chunk_lcol + (size_t)q * W * P.RM;
     const C *xb = x + (size_t)r * B;
+    /* rhs/parts modes need S x and H x apart; A x modes use D = S + i h dt/2 h0 */
+    const bool separate = (mode == AX_RHS || mode == AX_PARTS);
 
     for (int c = tid; c < ncols; c += nt) xr[c] = xb[cols[c]];
     __syncthreads();
 
     C accS = mk<C>(0, 0), accH = mk<C>(0, 0);
     if (i >= 0) {
-        const C *Se = (const C *)P.S_ell + (size_t)kk * W * B;
-        const C *He = (const C *)P.Hst_ell + (size_t)kk * W * B;
-        for (int j = 0; j < W; j++) {
-            const int lc = lcol[j * P.RM + tid];
-            if (lc >= 0) {
-                const C xv = xr[lc];
-                cfma(accS, Se[(size_t)j * B + i], xv);
-                cfma(accH, He[(size_t)j * B + i], xv);
+        if (separate) {
+            const C *Se = (const C *)P.S_ell + (size_t)kk * W * B;
+            const C *He = (const C *)P.Hst_ell + (size_t)kk * W * B;
+            for (int j = 0; j < W; j++) {
+                const int lc = lcol[j * P.RM + tid];
+                if (lc >= 0) {
+                    const C xv = xr[lc];
+                    cfma(accS, Se[(size_t)j * B + i], xv);
+                    cfma(accH, He[(size_t)j * B + i], xv);
+                }
+            }
+        } else {
+            const C *De = (const C *)P.D_ell + (size_t)kk * W * B;
+            for (int j = 0; j < W; j++) {
+                const int lc = lcol[j * P.RM + tid];
+                if (lc >= 0) cfma(accS, De[(size_t)j * B + i], xr[lc]);
             }
         }
     }
 
-    for (int a = P.act_ptr[r]; a < P.act_ptr[r + 1]; a++) {
+    int buf = 0;
+    for (int a = P.act_ptr[r]; a < P.act_ptr[r + 1]; a++, buf ^= 1) {
         const int l = P.act_l[a];
         const int e0 = P.ang_ptr[r * P.lmax + l], e1 = P.ang_ptr[r * P.lmax + l + 1];
-        __syncthreads();
+        C *u0 = ub + buf * 4 * CM, *u1 = u0 + CM, *u2 = u1 + CM, *u3 = u2 + CM;
+        /* gather into the buffer not read by the previous order's apply; one
+           barrier per order suffices (every thread finished apply(a-1) before
+           it gathered for a) */
         for (int c = tid; c < ncols; c += nt) {
             const int gc = cols[c];
             C U = mk<C>(0, 0), Wv = mk<C>(0, 0), U1 = mk<C>(0, 0), W1 = mk<C>(0, 0);
@@ -499,18 +513,25 @@ __device__ __forceinline__ void tma_bulk_load(void *dst, const void *src, unsign
 
 #define MBAR_SPIN_LIMIT (1u << 22)
 
+/* 4 warps per block row, one per SM sub-partition (each has its own FP64
+ * unit): in every 32-row step warp w applies band terms d = 4w+1..4w+4 and
+ * the inverse-block columns j = 8w..8w+7; partial sums meet in shared memory. */
 template <int BWP>
-__global__ void __launch_bounds__(32) k_precond_tma(PcT Q, int mode, const double2 *__restrict__ in0,
-                                                    const double2 *__restrict__ in1, double2 *io,
-                                                    double2 *__restrict__ out, DevScal *sc)
+__global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const double2 *__restrict__ in0,
+                                                     const double2 *__restrict__ in1, double2 *io,
+                                                     double2 *__restrict__ out, DevScal *sc)
 {
     constexpr int CH = 1024 + 32 * BWP;
+    constexpr int DPW = BWP / 4;                 /* band terms per warp */
     extern __shared__ __align__(128) unsigned char smem_tma[];
-    double2 *fac = (double2 *)smem_tma;          /* [2][CH] */
-    double2 *buf = fac + 2 * CH;                 /* [Bp]    */
-    double2 *tb = buf + Q.Bp;                    /* [32]    */
+    double2 *fac = (double2 *)smem_tma;          /* [2][CH]  */
+    double2 *buf = fac + 2 * CH;                 /* [Bp]     */
+    double2 *pt = buf + Q.Bp;                    /* [4][32] partial t */
+    double2 *py = pt + 128;                      /* [4][32] partial y */
     __shared__ __align__(8) uint64_t bar[2];
-    const int lane = threadIdx.x, r = blockIdx.x;
+    __shared__ int all_ok;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int r = blockIdx.x;
     if (r >= Q.nblk) return;
     const int B = Q.B, Bp = Q.Bp, nch = Q.nch;
     const int kk = Q.row_kidx[r];
@@ -519,11 +540,12 @@ __global__ void __launch_bounds__(32) k_precond_tma(PcT Q, int mode, const doubl
     const double2 *FU = Q.FU + (size_t)kk * nch * CH;
     const unsigned bytes = CH * sizeof(double2);
 
-    if (lane == 0) {
+    if (tid == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         tma_bulk_load(fac, FL, bytes, &bar[0]);          /* first forward chunk */
+        all_ok = 1;
     }
 
     double2 beta = make_double2(0, 0), negw = make_double2(0, 0), nega = make_double2(0, 0);
@@ -535,7 +557,7 @@ __global__ void __launch_bounds__(32) k_precond_tma(PcT Q, int mode, const doubl
     } else if (mode == PC_S) {
         nega = make_double2(-sc->alpha.x, -sc->alpha.y);
     }
-    for (int o = lane; o < Bp; o += 32) {
+    for (int o = tid; o < Bp; o += 128) {
         double2 val = make_double2(0, 0);
         if (o < B) {
             const size_t gi = off + Q.ord[o];
@@ -557,71 +579,74 @@ __global__ void __launch_bounds__(32) k_precond_tma(PcT Q, int mode, const doubl
         }
         buf[o] = val;
     }
-    __syncwarp();
+    __syncthreads();
 
     const int nk = 2 * nch;           /* chunk steps: forward then backward */
-    bool ok = true;
     int k = 0;
     for (; k < nk; k++) {
         const int fwd = k < nch;
         const int c = fwd ? k : nch - 1 - (k - nch);
-        if (lane == 0 && k + 1 < nk) {
+        if (tid == 0 && k + 1 < nk) {
             const int k1 = k + 1;
             const int c1 = k1 < nch ? k1 : nch - 1 - (k1 - nch);
             const double2 *src = (k1 < nch ? FL : FU) + (size_t)c1 * CH;
             tma_bulk_load(fac + (k1 & 1) * CH, src, bytes, &bar[k1 & 1]);
         }
         unsigned spins = 0;
+        bool ok = true;
         while (!mbar_try_wait(&bar[k & 1], (k >> 1) & 1)) {
             if (++spins > MBAR_SPIN_LIMIT) { ok = false; break; }
         }
-        if (!__all_sync(0xffffffffu, ok)) { ok = false; break; }
+        if (!ok) all_ok = 0;
+        __syncthreads();
+        if (!all_ok) break;
         const double2 *F = fac + (k & 1) * CH;
         const int o = 32 * c + lane;
-        double2 t = buf[o];
-        if (fwd) {
+        /* band terms of this warp */
+        double2 t = (wid == 0) ? buf[o] : make_double2(0, 0);
 #pragma unroll
-            for (int d = 1; d <= BWP; d++) {
-                double2 lv = F[1024 + (d - 1) * 32 + lane];
-                lv.x = -lv.x; lv.y = -lv.y;
-                cfma(t, lv, buf[o - d >= 0 ? o - d : 0]);
-            }
-        } else {
-#pragma unroll
-            for (int d = 1; d <= BWP; d++) {
-                double2 uv = F[1024 + (d - 1) * 32 + lane];
-                uv.x = -uv.x; uv.y = -uv.y;
-                cfma(t, uv, buf[o + d < Bp ? o + d : Bp - 1]);
-            }
+        for (int q = 0; q < DPW; q++) {
+            const int d = wid * DPW + q + 1;
+            double2 bv = F[1024 + (d - 1) * 32 + lane];
+            bv.x = -bv.x; bv.y = -bv.y;
+            const int src = fwd ? (o - d >= 0 ? o - d : 0) : (o + d < Bp ? o + d : Bp - 1);
+            cfma(t, bv, buf[src]);
         }
-        tb[lane] = t;
-        __syncwarp();
-        double2 a0 = make_double2(0, 0), a1 = a0, a2 = a0, a3 = a0;
+        pt[wid * 32 + lane] = t;
+        __syncthreads();
+        /* this warp's 8 columns of the inverse block */
+        double2 a0 = make_double2(0, 0), a1 = a0;
 #pragma unroll
-        for (int j = 0; j < 32; j += 4) {
-            cfma(a0, F[(j + 0) * 32 + lane], tb[j + 0]);
-            cfma(a1, F[(j + 1) * 32 + lane], tb[j + 1]);
-            cfma(a2, F[(j + 2) * 32 + lane], tb[j + 2]);
-            cfma(a3, F[(j + 3) * 32 + lane], tb[j + 3]);
+        for (int q = 0; q < 8; q += 2) {
+            const int j0 = wid * 8 + q, j1 = j0 + 1;
+            const double2 t0 = make_double2((pt[j0].x + pt[32 + j0].x) + (pt[64 + j0].x + pt[96 + j0].x),
+                                            (pt[j0].y + pt[32 + j0].y) + (pt[64 + j0].y + pt[96 + j0].y));
+            const double2 t1 = make_double2((pt[j1].x + pt[32 + j1].x) + (pt[64 + j1].x + pt[96 + j1].x),
+                                            (pt[j1].y + pt[32 + j1].y) + (pt[64 + j1].y + pt[96 + j1].y));
+            cfma(a0, F[j0 * 32 + lane], t0);
+            cfma(a1, F[j1 * 32 + lane], t1);
         }
-        __syncwarp();
-        buf[o] = make_double2((a0.x + a1.x) + (a2.x + a3.x), (a0.y + a1.y) + (a2.y + a3.y));
-        __syncwarp();
+        py[wid * 32 + lane] = make_double2(a0.x + a1.x, a0.y + a1.y);
+        __syncthreads();
+        if (wid == 0)
+            buf[o] = make_double2((py[lane].x + py[32 + lane].x) + (py[64 + lane].x + py[96 + lane].x),
+                                  (py[lane].y + py[32 + lane].y) + (py[64 + lane].y + py[96 + lane].y));
+        __syncthreads();
     }
-    if (!ok) {
-        if (lane == 0) {
+    if (!all_ok) {
+        if (tid == 0) {
             atomicOr(&sc->err, 1u);
             /* drain the copies still in flight (bounded) before exiting */
-            for (int kk2 = k; kk2 < k + 2 && kk2 < nk; kk2++) {
+            for (int k2 = k; k2 < k + 2 && k2 < nk; k2++) {
                 unsigned spins = 0;
-                while (!mbar_try_wait(&bar[kk2 & 1], (kk2 >> 1) & 1) && ++spins < MBAR_SPIN_LIMIT) {
+                while (!mbar_try_wait(&bar[k2 & 1], (k2 >> 1) & 1) && ++spins < MBAR_SPIN_LIMIT) {
                 }
             }
         }
-        __syncwarp();
+        __syncthreads();
         return;
     }
-    for (int o = lane; o < B; o += 32) out[off + Q.ord[o]] = buf[o];
+    for (int o = tid; o < B; o += 128) out[off + Q.ord[o]] = buf[o];
 }
 
 /* ------------------------------------------------------------------ */
@@ -670,7 +695,7 @@ struct gade_solver {
     int *d_row_kidx, *d_act_ptr, *d_act_l, *d_ang_ptr, *d_ang_c;
     void *d_ang_a0, *d_ang_a0k, *d_ang_a1, *d_ang_a1k;
     int *d_chunk_nrows, *d_chunk_ncols, *d_chunk_rows, *d_chunk_cols, *d_chunk_lcol;
-    void *d_M, *d_S_ell, *d_Hst_ell;
+    void *d_M, *d_S_ell, *d_Hst_ell, *d_D_ell;
     int *d_kvals, *d_ell_pos;
     void *d_g, *d_gt;
     int blk_nnz;
@@ -874,6 +899,10 @@ extern "C" int gade_solver_create(const gade_problem *p, double dt, double h, in
         double2 *d;
         UP(d, (const double2 *)su->S_ell, (size_t)s->nk * WB); s->d_S_ell = d;
         UP(d, (const double2 *)su->Hst_ell, (size_t)s->nk * WB); s->d_Hst_ell = d;
+        std::vector<double2> D((size_t)s->nk * WB);
+        for (size_t e = 0; e < D.size(); e++)
+            D[e] = make_double2(su->S_ell[e].re + su->Hst_ell[e].re, su->S_ell[e].im + su->Hst_ell[e].im);
+        UP(d, D.data(), D.size()); s->d_D_ell = d;
     }
     UP(s->d_kvals, su->kvals, s->nk);
     UP(s->d_ell_pos, su->ell_pos, WB);
@@ -952,7 +981,7 @@ extern "C" int gade_solver_create(const gade_problem *p, double dt, double h, in
             }
         UP(s->d_FL, FL.data(), FL.size());
         UP(s->d_FU, FU.data(), FU.size());
-        size_t smem = sizeof(double2) * ((size_t)2 * CH + s->Bp + 32);
+        size_t smem = sizeof(double2) * ((size_t)2 * CH + s->Bp + 256);
         if (smem > 220 * 1024) { gade_setup_release(su); gade_solver_free(s); return fail(GADE_ERR_ARG, "block dimension too large for the preconditioner"); }
         cudaFuncSetAttribute(k_precond_tma<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         cudaFuncSetAttribute(k_precond_tma<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -977,7 +1006,7 @@ extern "C" int gade_solver_create(const gade_problem *p, double dt, double h, in
     {
         /* exact FP64 flop count of one operator apply (2 per FMA) */
         const double fma_c = s->rc ? 2.0 : 4.0;     /* FMAs of one coupling term */
-        double fmas = 8.0 * (double)p->blk_nnz * s->nblk;             /* diagonal blocks */
+        double fmas = 4.0 * (double)p->blk_nnz * s->nblk;             /* diagonal blocks (A x modes) */
         for (int r = 0; r < s->nblk; r++)
             for (int a = su->act_ptr[r]; a < su->act_ptr[r + 1]; a++) {
                 int l = su->act_l[a];
@@ -1005,7 +1034,7 @@ static OpP op_params(const gade_solver *s)
     P.ang_a0 = s->d_ang_a0; P.ang_a0k = s->d_ang_a0k; P.ang_a1 = s->d_ang_a1; P.ang_a1k = s->d_ang_a1k;
     P.chunk_nrows = s->d_chunk_nrows; P.chunk_ncols = s->d_chunk_ncols; P.chunk_rows = s->d_chunk_rows;
     P.chunk_cols = s->d_chunk_cols; P.chunk_lcol = s->d_chunk_lcol;
-    P.M = s->d_M; P.S_ell = s->d_S_ell; P.Hst_ell = s->d_Hst_ell;
+    P.M = s->d_M; P.S_ell = s->d_S_ell; P.Hst_ell = s->d_Hst_ell; P.D_ell = s->d_D_ell;
     return P;
 }
 
@@ -1015,7 +1044,7 @@ static int launch_apply(gade_solver *s, const double2 *x, int mode, VecP V, int 
     RedP red = {s->d_part, s->d_ticket, s->d_sc, redkind};
     dim3 grid(s->nchunk, s->nblk);
     int nt = s->RM;
-    size_t smem = sizeof(double2) * 5 * (size_t)s->CM + sizeof(double) * NRED * nt;
+    size_t smem = sizeof(double2) * 9 * (size_t)s->CM + sizeof(double) * NRED * nt;
     prof_begin(s, st);
     if (s->rc) k_apply<double, true><<<grid, nt, smem, st>>>(P, x, mode, V, red);
     else k_apply<double, false><<<grid, nt, smem, st>>>(P, x, mode, V, red);
@@ -1031,10 +1060,10 @@ static int launch_precond(gade_solver *s, int mode, const double2 *in0, const do
     Q.nblk = s->nblk; Q.B = s->B; Q.Bp = s->Bp; Q.nch = s->nch;
     Q.row_kidx = s->d_row_kidx; Q.ord = s->d_ord; Q.FL = s->d_FL; Q.FU = s->d_FU;
     const int CH = 1024 + 32 * s->bwp;
-    size_t smem = sizeof(double2) * ((size_t)2 * CH + s->Bp + 32);
+    size_t smem = sizeof(double2) * ((size_t)2 * CH + s->Bp + 256);
     prof_begin(s, st);
-    if (s->bwp == 16) k_precond_tma<16><<<s->nblk, 32, smem, st>>>(Q, mode, in0, in1, io, out, s->d_sc);
-    else k_precond_tma<32><<<s->nblk, 32, smem, st>>>(Q, mode, in0, in1, io, out, s->d_sc);
+    if (s->bwp == 16) k_precond_tma<16><<<s->nblk, 128, smem, st>>>(Q, mode, in0, in1, io, out, s->d_sc);
+    else k_precond_tma<32><<<s->nblk, 128, smem, st>>>(Q, mode, in0, in1, io, out, s->d_sc);
     prof_end(s, st, 1);
     CKL();
     return GADE_OK;
