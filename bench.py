@@ -294,13 +294,16 @@ def run_ours(args):
 
 
 def _ncu_traffic():
-    """DRAM bytes per k_apply launch from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", "k_apply_traffic.json")
+    """DRAM bytes per k_apply launch (dram__bytes_read.sum + dram__bytes_write.sum)
+    from the committed ncu summary of this workload."""
+    path = os.path.join(ROOT, "profiles", f"k_apply_{WORKLOAD}.md")
     try:
-        with open(path) as f:
-            return json.load(f).get("dram_bytes_per_launch")
-    except Exception:
-        return None
+        for line in open(path):
+            if line.startswith("dram_bytes_per_launch:"):
+                return int(line.split(":")[1])
+    except OSError:
+        pass
+    return None
 
 
 def main():
