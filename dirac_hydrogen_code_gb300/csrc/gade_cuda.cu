@@ -133,7 +133,7 @@ struct DevScal {
     double pad[3];
 };
 
-enum { RED_RHS = 0, RED_RESTART, RED_R0V, RED_TS, RED_UPDATE, RED_NONE };
+enum { RED_RHS = 0, RED_RESTART, RED_R0V, RED_TS, RED_UPDATE, RED_NONE, RED_DOT_OUT };
 enum { AX_PLAIN = 0, AX_PARTS, AX_R0V, AX_TS, AX_RHS, AX_RESTART };
 enum { PC_PLAIN = 0, PC_P, PC_S };
 
@@ -161,6 +161,7 @@ struct RedP {
     unsigned int *ticket;
     DevScal *sc;
     int kind;
+    double *out;                   /* RED_DOT_OUT: receives (re, im) of the dot */
 };
 
 /* Block-wide deterministic sum of NV doubles; result valid in thread 0. */
@@ -231,6 +232,10 @@ __device__ void reduce_finish(RedP red, double (&v)[NRED], double *sh)
             sc->rr = acc[0];
             sc->rho_prev = sc->rho;
             sc->rho = make_double2(acc[1], acc[2]);
+            break;
+        case RED_DOT_OUT:
+            red.out[0] = acc[0];
+            red.out[1] = acc[1];
             break;
         }
         *red.ticket = 0u;
@@ -1383,5 +1388,66 @@ extern "C" int gade_solver_flops(const gade_solver *s, double *apply_flops, doub
     if (!s) return fail(GADE_ERR_ARG, "gade_solver_flops: NULL solver");
     if (apply_flops) *apply_flops = s->apply_flops;
     if (precond_flops) *precond_flops = s->precond_flops;
+    return GADE_OK;
+}
+
+/* ------------------------------------------------------------------ */
+/* allocation-free operator apply + dot                                */
+/* ------------------------------------------------------------------ */
+/* Cross-CTA reduction scratch of gade_solver_apply_dot_noalloc: per-CTA
+ * partial sums followed by the arrival ticket.  It is a file-scope device
+ * array, so the library holds it on every GPU that loads it until exit and
+ * the entry point needs no allocation.  All calls share it. */
+#define GADE_NOALLOC_MAX_CTAS 16384
+static __device__ __align__(256) double g_noalloc_scratch[GADE_NOALLOC_MAX_CTAS * NRED + 32];
+
+#include <mutex>
+static std::mutex g_noalloc_mu;
+static double *g_noalloc_dev_ptr[256];   /* device address of the array, per device ordinal */
+
+extern "C" int gade_solver_apply_dot_noalloc(gade_solver *s, const void *x_dev, const void *r0_dev, void *y_dev,
+                                             void *dot_dev, void *stream)
+{
+    if (!s || !x_dev || !r0_dev || !y_dev || !dot_dev)
+        return fail(GADE_ERR_ARG, "gade_solver_apply_dot_noalloc: NULL argument");
+    if (!s->has_time) return fail(GADE_ERR_STATE, "gade_solver_apply_dot_noalloc: call gade_solver_set_time first");
+    if (s->device < 0 || s->device >= 256) return fail(GADE_ERR_ARG, "gade_solver_apply_dot_noalloc: device ordinal out of range");
+    const long long ncta = (long long)s->nchunk * s->nblk;
+    if (ncta > GADE_NOALLOC_MAX_CTAS)
+        return fail(GADE_ERR_ARG,
+                    "gade_solver_apply_dot_noalloc: problem needs %lld reduction slots, more than the %d of the "
+                    "library's fixed scratch array; use the allocating path (gade_solver_step/apply)",
+                    ncta, GADE_NOALLOC_MAX_CTAS);
+    CK(cudaSetDevice(s->device));
+    double *base = nullptr;
+    {
+        /* once per device, with that device current: the host-side symbol is
+           only a stand-in, the kernel needs the device address */
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!g_noalloc_dev_ptr[s->device]) {
+            void *ptr = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+            if (e != cudaSuccess || !ptr)
+                return fail(GADE_ERR_CUDA, "gade_solver_apply_dot_noalloc: cudaGetSymbolAddress failed: %s",
+                            cudaGetErrorString(e));
+            g_noalloc_dev_ptr[s->device] = (double *)ptr;
+        }
+        base = g_noalloc_dev_ptr[s->device];
+    }
+    cudaStream_t st = stream ? (cudaStream_t)stream : s->stream;
+    unsigned int *ticket = (unsigned int *)(base + (size_t)GADE_NOALLOC_MAX_CTAS * NRED);
+    /* the arrival ticket must start at zero */
+    CK(cudaMemsetAsync(ticket, 0, sizeof(unsigned int), st));
+    OpP P = op_params(s);
+    RedP red = {base, ticket, s->d_sc, RED_DOT_OUT, (double *)dot_dev};
+    VecP V = {};
+    V.out0 = y_dev;
+    V.in0 = r0_dev;
+    dim3 grid(s->nchunk, s->nblk);
+    int nt = s->RM;
+    size_t smem = sizeof(double2) * 9 * (size_t)s->CM + sizeof(double) * NRED * nt;
+    if (s->rc) k_apply<double, true><<<grid, nt, smem, st>>>(P, (const double2 *)x_dev, AX_R0V, V, red);
+    else k_apply<double, false><<<grid, nt, smem, st>>>(P, (const double2 *)x_dev, AX_R0V, V, red);
+    CKL();
     return GADE_OK;
 }

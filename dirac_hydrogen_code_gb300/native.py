@@ -70,6 +70,8 @@ _SIGS = {
     "gade_solver_kernel_times": (C.c_int, [C.c_void_p, C.POINTER(KernelTimes)]),
     "gade_probe_fp64_peak": (C.c_int, [C.c_int32, C.POINTER(C.c_double)]),
     "gade_solver_flops": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "gade_solver_apply_dot_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                C.c_void_p]),
 }
 
 
@@ -197,6 +199,13 @@ class Solver:
     def apply_device(self, x_ptr: int, y_ptr: int, stream: int = 0):
         _check(load_library().gade_solver_apply_device(self._h, C.c_void_p(x_ptr), C.c_void_p(y_ptr),
                                                        C.c_void_p(stream) if stream else None))
+
+    def apply_dot_noalloc(self, x_ptr: int, r0_ptr: int, y_ptr: int, dot_ptr: int, stream: int = 0):
+        """y = (S + H(t)) x and dot = <r0, y> on device buffers, without any
+        device allocation (scratch in a fixed array inside the library)."""
+        _check(load_library().gade_solver_apply_dot_noalloc(
+            self._h, C.c_void_p(x_ptr), C.c_void_p(r0_ptr), C.c_void_p(y_ptr), C.c_void_p(dot_ptr),
+            C.c_void_p(stream) if stream else None))
 
     def launch_count(self) -> int:
         return int(load_library().gade_solver_launch_count(self._h))

@@ -145,6 +145,24 @@ int gade_solver_kernel_times(gade_solver *s, gade_kernel_times *out);
  * preconditioner solve, counted exactly from the set-up structure. */
 int gade_solver_flops(const gade_solver *s, double *apply_flops, double *precond_flops);
 
+/* y = (S + H(t)) x and dot = sum_i conj(r0_i) y_i (2 doubles, re and im), all
+ * device pointers in HBM, with the tables of the last set_time/step; no
+ * counterpart in the reference.  For callers that may not allocate device
+ * memory once they are running: frameworks that own all GPU memory through
+ * their own pool and forbid other allocations after start-up, or loops on
+ * pipelined streams where cudaMalloc's implicit device synchronisation would
+ * stall them.  This entry point calls no cudaMalloc/cudaFree and no allocating
+ * library routine: its cross-block reduction scratch is a fixed 512 KB device
+ * array inside the library (16384 partial-sum slots), which every GPU that
+ * loads the library keeps until exit.  Problems that need more than 16384
+ * row-chunk x block work units are rejected with GADE_ERR_ARG.  The first call
+ * on each device looks up that array's device address; make that first call
+ * before any stream capture.  All calls share the array, so calls whose
+ * kernels overlap on the GPU race: order them on one stream.  Asynchronous on
+ * `stream` (NULL: the solver's stream). */
+int gade_solver_apply_dot_noalloc(gade_solver *s, const void *x_dev, const void *r0_dev, void *y_dev,
+                                  void *dot_dev, void *stream);
+
 /* Measured FP64 FMA throughput of a device in TFLOP/s (2 flops per DFMA),
  * from a dependent-chain-free FMA kernel timed with CUDA events. */
 int gade_probe_fp64_peak(int32_t device, double *tflops);
