@@ -130,11 +130,12 @@ struct DevScal {
     double tt;
     unsigned int err;      /* bit 0: a bounded mbarrier wait timed out */
     unsigned int pad0;
-    double pad[3];
+    double snorm;          /* x^H S x (mixed precision conservation check) */
+    double pad[2];
 };
 
-enum { RED_RHS = 0, RED_RESTART, RED_R0V, RED_TS, RED_UPDATE, RED_NONE, RED_DOT_OUT };
-enum { AX_PLAIN = 0, AX_PARTS, AX_R0V, AX_TS, AX_RHS, AX_RESTART };
+enum { RED_RHS = 0, RED_RESTART, RED_R0V, RED_TS, RED_UPDATE, RED_NONE, RED_DOT_OUT, RED_QB, RED_RES, RED_SNORM, RED_MIX };
+enum { AX_PLAIN = 0, AX_PARTS, AX_R0V, AX_TS, AX_RHS, AX_RESTART, AX_QB, AX_RES, AX_MIX };
 enum { PC_PLAIN = 0, PC_P, PC_S };
 
 #define NRED 4   /* values per partial: up to 4 doubles */
@@ -237,6 +238,21 @@ __device__ void reduce_finish(RedP red, double (&v)[NRED], double *sh)
             red.out[0] = acc[0];
             red.out[1] = acc[1];
             break;
+        case RED_QB:
+            sc->rhs_sqnorm = acc[0];
+            sc->snorm = acc[1];
+            break;
+        case RED_RES:
+            sc->rr = acc[0];
+            break;
+        case RED_SNORM:
+            sc->snorm = acc[0];
+            break;
+        case RED_MIX:
+            sc->rhs_sqnorm = acc[0];
+            sc->rr = acc[1];
+            sc->snorm = acc[2];
+            break;
         }
         *red.ticket = 0u;
     }
@@ -327,7 +343,9 @@ __global__ void __launch_bounds__(128) k_apply(OpP P, const typename Cx<R>::T *_
     extern __shared__ unsigned char smem_raw[];
     C *xr = (C *)smem_raw;                    /* [CM] */
     C *ub = xr + P.CM;                        /* [2][4][CM] double-buffered u, w, u', w' */
-    double *shred = (double *)(ub + 8 * P.CM); /* [NRED * blockDim] */
+    C *xs = ub + 8 * P.CM;                    /* [CM] AX_MIX: x_n slice   */
+    C *ds = xs + P.CM;                        /* [CM] AX_MIX: delta slice */
+    double *shred = (double *)(ds + P.CM);    /* [NRED * blockDim] */
 
     const int q = blockIdx.x, r = blockIdx.y, tid = threadIdx.x, nt = blockDim.x;
     const int B = P.B, W = P.W, CM = P.CM;
@@ -338,14 +356,31 @@ __global__ void __launch_bounds__(128) k_apply(OpP P, const typename Cx<R>::T *_
     const int *lcol = P.chunk_lcol + (size_t)q * W * P.RM;
     const C *xb = x + (size_t)r * B;
     /* rhs/parts modes need S x and H x apart; A x modes use D = S + i h dt/2 h0 */
-    const bool separate = (mode == AX_RHS || mode == AX_PARTS);
+    const bool separate = (mode == AX_RHS || mode == AX_PARTS || mode == AX_QB);
 
     for (int c = tid; c < ncols; c += nt) xr[c] = xb[cols[c]];
+    if (mode == AX_MIX) {
+        const C *xn = (const C *)V.in0 + (size_t)r * B, *dn = (const C *)V.in1 + (size_t)r * B;
+        for (int c = tid; c < ncols; c += nt) { xs[c] = xn[cols[c]]; ds[c] = dn[cols[c]]; }
+    }
     __syncthreads();
 
-    C accS = mk<C>(0, 0), accH = mk<C>(0, 0);
+    C accS = mk<C>(0, 0), accH = mk<C>(0, 0), accD = mk<C>(0, 0);
     if (i >= 0) {
-        if (separate) {
+        if (mode == AX_MIX) {
+            /* x = w = 2 x_n + delta: S x_n, S delta and (i h dt/2 h0) w */
+            const C *Se = (const C *)P.S_ell + (size_t)kk * W * B;
+            const C *He = (const C *)P.Hst_ell + (size_t)kk * W * B;
+            for (int j = 0; j < W; j++) {
+                const int lc = lcol[j * P.RM + tid];
+                if (lc >= 0) {
+                    const C sv = Se[(size_t)j * B + i];
+                    cfma(accS, sv, xs[lc]);
+                    cfma(accD, sv, ds[lc]);
+                    cfma(accH, He[(size_t)j * B + i], xr[lc]);
+                }
+            }
+        } else if (separate) {
             const C *Se = (const C *)P.S_ell + (size_t)kk * W * B;
             const C *He = (const C *)P.Hst_ell + (size_t)kk * W * B;
             for (int j = 0; j < W; j++) {
@@ -454,6 +489,32 @@ __global__ void __launch_bounds__(128) k_apply(OpP P, const typename Cx<R>::T *_
             v[1] = (double)rhs.x * rhs.x + (double)rhs.y * rhs.y;
             break;
         }
+        case AX_QB: {           /* q = -2 H x ; |S x - H x|^2 ; x^H S x  (mixed precision) */
+            const C qv = mk<C>(-2.0 * accH.x, -2.0 * accH.y);
+            ((C *)V.out0)[gi] = qv;
+            const C b = csub(accS, accH);
+            v[0] = (double)b.x * b.x + (double)b.y * b.y;
+            const C xi = x[gi];
+            v[1] = (double)xi.x * accS.x + (double)xi.y * accS.y;
+            break;
+        }
+        case AX_RES: {          /* r = q - A d ; |r|^2  (mixed precision) */
+            const C qv = ((const C *)V.in0)[gi];
+            const C rv = csub(qv, ax);
+            ((C *)V.out0)[gi] = rv;
+            v[0] = (double)rv.x * rv.x + (double)rv.y * rv.y;
+            break;
+        }
+        case AX_MIX: {          /* r = -S delta - H w ; b = S x_n - H w / 2 ; x_n^H S x_n */
+            const C rv = mk<C>(-accD.x - accH.x, -accD.y - accH.y);
+            ((C *)V.out0)[gi] = rv;
+            const C b = mk<C>(accS.x - 0.5 * accH.x, accS.y - 0.5 * accH.y);
+            v[0] = (double)b.x * b.x + (double)b.y * b.y;
+            v[1] = (double)rv.x * rv.x + (double)rv.y * rv.y;
+            const C xi = ((const C *)V.in0)[gi];
+            v[2] = (double)xi.x * accS.x + (double)xi.y * accS.y;
+            break;
+        }
         case AX_RESTART: {      /* r = rhs - A x ; r0 = r */
             const C rhs = ((const C *)V.in0)[gi];
             const C rv = csub(rhs, ax);
@@ -480,7 +541,7 @@ __global__ void __launch_bounds__(128) k_apply(OpP P, const typename Cx<R>::T *_
 struct PcT {
     int nblk, B, Bp, nch;
     const int *row_kidx, *ord;
-    const double2 *FL, *FU;        /* [nk][nch][CH] */
+    const void *FL, *FU;           /* [nk][nch][CH] complex of the kernel's precision */
 };
 
 __device__ __forceinline__ unsigned smem_u32(const void *p)
@@ -521,18 +582,20 @@ __device__ __forceinline__ void tma_bulk_load(void *dst, const void *src, unsign
 /* 4 warps per block row, one per SM sub-partition (each has its own FP64
  * unit): in every 32-row step warp w applies band terms d = 4w+1..4w+4 and
  * the inverse-block columns j = 8w..8w+7; partial sums meet in shared memory. */
-template <int BWP>
-__global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const double2 *__restrict__ in0,
-                                                     const double2 *__restrict__ in1, double2 *io,
-                                                     double2 *__restrict__ out, DevScal *sc)
+template <typename R, int BWP>
+__global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const typename Cx<R>::T *__restrict__ in0,
+                                                     const typename Cx<R>::T *__restrict__ in1,
+                                                     typename Cx<R>::T *io, typename Cx<R>::T *__restrict__ out,
+                                                     DevScal *sc)
 {
+    typedef typename Cx<R>::T C;
     constexpr int CH = 1024 + 32 * BWP;
     constexpr int DPW = BWP / 4;                 /* band terms per warp */
     extern __shared__ __align__(128) unsigned char smem_tma[];
-    double2 *fac = (double2 *)smem_tma;          /* [2][CH]  */
-    double2 *buf = fac + 2 * CH;                 /* [Bp]     */
-    double2 *pt = buf + Q.Bp;                    /* [4][32] partial t */
-    double2 *py = pt + 128;                      /* [4][32] partial y */
+    C *fac = (C *)smem_tma;          /* [2][CH]  */
+    C *buf = fac + 2 * CH;                 /* [Bp]     */
+    C *pt = buf + Q.Bp;                    /* [4][32] partial t */
+    C *py = pt + 128;                      /* [4][32] partial y */
     __shared__ __align__(8) uint64_t bar[2];
     __shared__ int all_ok;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -541,9 +604,9 @@ __global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const doub
     const int B = Q.B, Bp = Q.Bp, nch = Q.nch;
     const int kk = Q.row_kidx[r];
     const size_t off = (size_t)r * B;
-    const double2 *FL = Q.FL + (size_t)kk * nch * CH;
-    const double2 *FU = Q.FU + (size_t)kk * nch * CH;
-    const unsigned bytes = CH * sizeof(double2);
+    const C *FL = (const C *)Q.FL + (size_t)kk * nch * CH;
+    const C *FU = (const C *)Q.FU + (size_t)kk * nch * CH;
+    const unsigned bytes = CH * sizeof(C);
 
     if (tid == 0) {
         mbar_init(&bar[0], 1);
@@ -553,30 +616,30 @@ __global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const doub
         all_ok = 1;
     }
 
-    double2 beta = make_double2(0, 0), negw = make_double2(0, 0), nega = make_double2(0, 0);
+    C beta = mk<C>(0, 0), negw = mk<C>(0, 0), nega = mk<C>(0, 0);
     if (mode == PC_P) {
         const double2 a = cdiv(sc->rho, sc->rho_prev);
         const double2 b = cdiv(sc->alpha, sc->w);
-        beta = make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
-        negw = make_double2(-sc->w.x, -sc->w.y);
+        beta = mk<C>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+        negw = mk<C>(-sc->w.x, -sc->w.y);
     } else if (mode == PC_S) {
-        nega = make_double2(-sc->alpha.x, -sc->alpha.y);
+        nega = mk<C>(-sc->alpha.x, -sc->alpha.y);
     }
     for (int o = tid; o < Bp; o += 128) {
-        double2 val = make_double2(0, 0);
+        C val = mk<C>(0, 0);
         if (o < B) {
             const size_t gi = off + Q.ord[o];
             if (mode == PC_PLAIN) {
                 val = in0[gi];
             } else if (mode == PC_P) {
-                double2 t = io[gi];
+                C t = io[gi];
                 cfma(t, negw, in1[gi]);
-                double2 pv = in0[gi];
+                C pv = in0[gi];
                 cfma(pv, beta, t);
                 io[gi] = pv;
                 val = pv;
             } else {
-                double2 sv = in0[gi];
+                C sv = in0[gi];
                 cfma(sv, nega, in1[gi]);
                 io[gi] = sv;
                 val = sv;
@@ -594,7 +657,7 @@ __global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const doub
         if (tid == 0 && k + 1 < nk) {
             const int k1 = k + 1;
             const int c1 = k1 < nch ? k1 : nch - 1 - (k1 - nch);
-            const double2 *src = (k1 < nch ? FL : FU) + (size_t)c1 * CH;
+            const C *src = (k1 < nch ? FL : FU) + (size_t)c1 * CH;
             tma_bulk_load(fac + (k1 & 1) * CH, src, bytes, &bar[k1 & 1]);
         }
         unsigned spins = 0;
@@ -605,14 +668,14 @@ __global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const doub
         if (!ok) all_ok = 0;
         __syncthreads();
         if (!all_ok) break;
-        const double2 *F = fac + (k & 1) * CH;
+        const C *F = fac + (k & 1) * CH;
         const int o = 32 * c + lane;
         /* band terms of this warp */
-        double2 t = (wid == 0) ? buf[o] : make_double2(0, 0);
+        C t = (wid == 0) ? buf[o] : mk<C>(0, 0);
 #pragma unroll
         for (int q = 0; q < DPW; q++) {
             const int d = wid * DPW + q + 1;
-            double2 bv = F[1024 + (d - 1) * 32 + lane];
+            C bv = F[1024 + (d - 1) * 32 + lane];
             bv.x = -bv.x; bv.y = -bv.y;
             const int src = fwd ? (o - d >= 0 ? o - d : 0) : (o + d < Bp ? o + d : Bp - 1);
             cfma(t, bv, buf[src]);
@@ -620,21 +683,21 @@ __global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const doub
         pt[wid * 32 + lane] = t;
         __syncthreads();
         /* this warp's 8 columns of the inverse block */
-        double2 a0 = make_double2(0, 0), a1 = a0;
+        C a0 = mk<C>(0, 0), a1 = a0;
 #pragma unroll
         for (int q = 0; q < 8; q += 2) {
             const int j0 = wid * 8 + q, j1 = j0 + 1;
-            const double2 t0 = make_double2((pt[j0].x + pt[32 + j0].x) + (pt[64 + j0].x + pt[96 + j0].x),
+            const C t0 = mk<C>((pt[j0].x + pt[32 + j0].x) + (pt[64 + j0].x + pt[96 + j0].x),
                                             (pt[j0].y + pt[32 + j0].y) + (pt[64 + j0].y + pt[96 + j0].y));
-            const double2 t1 = make_double2((pt[j1].x + pt[32 + j1].x) + (pt[64 + j1].x + pt[96 + j1].x),
+            const C t1 = mk<C>((pt[j1].x + pt[32 + j1].x) + (pt[64 + j1].x + pt[96 + j1].x),
                                             (pt[j1].y + pt[32 + j1].y) + (pt[64 + j1].y + pt[96 + j1].y));
             cfma(a0, F[j0 * 32 + lane], t0);
             cfma(a1, F[j1 * 32 + lane], t1);
         }
-        py[wid * 32 + lane] = make_double2(a0.x + a1.x, a0.y + a1.y);
+        py[wid * 32 + lane] = mk<C>(a0.x + a1.x, a0.y + a1.y);
         __syncthreads();
         if (wid == 0)
-            buf[o] = make_double2((py[lane].x + py[32 + lane].x) + (py[64 + lane].x + py[96 + lane].x),
+            buf[o] = mk<C>((py[lane].x + py[32 + lane].x) + (py[64 + lane].x + py[96 + lane].x),
                                   (py[lane].y + py[32 + lane].y) + (py[64 + lane].y + py[96 + lane].y));
         __syncthreads();
     }
@@ -686,6 +749,91 @@ __global__ void k_update(long long n, typename Cx<R>::T *x, const typename Cx<R>
 }
 
 /* ------------------------------------------------------------------ */
+/* mixed precision: complex64 inner solves inside FP64 refinement      */
+/* ------------------------------------------------------------------ */
+/* delta = x - x_prev (linear extrapolation of the state) or 0; FP32 copies */
+__global__ void k_mixed_prep(long long n, const double2 *__restrict__ x, const double2 *__restrict__ xprev,
+                             int have_prev, double2 *__restrict__ d64, float2 *__restrict__ d32,
+                             double2 *__restrict__ w)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const double2 xv = x[i];
+        double2 d = make_double2(0, 0);
+        if (have_prev) { const double2 xp = xprev[i]; d = make_double2(xv.x - xp.x, xv.y - xp.y); }
+        d64[i] = d;
+        d32[i] = make_float2((float)d.x, (float)d.y);
+        w[i] = make_double2(2.0 * xv.x + d.x, 2.0 * xv.y + d.y);
+    }
+}
+
+/* inner BiCGSTAB start from the FP64 refinement residual:
+   e = 0, r = r0 = (complex64) rin, p = v = 0, |r|^2 */
+__global__ void k_inner_init(long long n, const double2 *__restrict__ rin, float2 *e, float2 *r, float2 *r0,
+                             float2 *p, float2 *v, RedP red)
+{
+    extern __shared__ unsigned char smem_raw[];
+    double *shred = (double *)smem_raw;
+    double acc[NRED] = {0, 0, 0, 0};
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const double2 rd = rin[i];
+        const float2 rv = make_float2((float)rd.x, (float)rd.y);
+        r[i] = rv; r0[i] = rv;
+        e[i] = make_float2(0, 0); p[i] = make_float2(0, 0); v[i] = make_float2(0, 0);
+        acc[0] += (double)rv.x * rv.x + (double)rv.y * rv.y;
+    }
+    acc[1] = acc[0];
+    reduce_finish(red, acc, shred);
+}
+
+/* delta += e (FP64), refresh the FP32 copy and w = 2 x_n + delta */
+__global__ void k_delta_add(long long n, double2 *__restrict__ d64, const float2 *__restrict__ e,
+                            float2 *__restrict__ d32, const double2 *__restrict__ x, double2 *__restrict__ w)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float2 ev = e[i];
+        double2 d = d64[i];
+        d.x += (double)ev.x; d.y += (double)ev.y;
+        d64[i] = d;
+        d32[i] = make_float2((float)d.x, (float)d.y);
+        const double2 xv = x[i];
+        w[i] = make_double2(2.0 * xv.x + d.x, 2.0 * xv.y + d.y);
+    }
+}
+
+/* x_prev = x ; x += delta (FP64) */
+__global__ void k_mixed_finish(long long n, double2 *__restrict__ x, double2 *__restrict__ xprev,
+                               const double2 *__restrict__ d64)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const double2 xv = x[i], d = d64[i];
+        xprev[i] = xv;
+        x[i] = make_double2(xv.x + d.x, xv.y + d.y);
+    }
+}
+
+/* x^H S x in FP64 over the block-diagonal overlap (norm-conservation check) */
+__global__ void k_snorm(int B, int W, const int *__restrict__ row_kidx, const int *__restrict__ ell_col,
+                        const double2 *__restrict__ S_ell, const double2 *__restrict__ x, RedP red)
+{
+    extern __shared__ unsigned char smem_raw[];
+    double *shred = (double *)smem_raw;
+    const int r = blockIdx.y, i = blockIdx.x * blockDim.x + threadIdx.x;
+    double acc[NRED] = {0, 0, 0, 0};
+    if (i < B) {
+        const int kk = row_kidx[r];
+        const double2 *xb = x + (size_t)r * B;
+        double2 sx = make_double2(0, 0);
+        for (int j = 0; j < W; j++) {
+            const int col = ell_col[(size_t)j * B + i];
+            if (col >= 0) cfma(sx, S_ell[((size_t)kk * W + j) * B + i], xb[col]);
+        }
+        const double2 xi = xb[i];
+        acc[0] = xi.x * sx.x + xi.y * sx.y;
+    }
+    reduce_finish(red, acc, shred);
+}
+
+/* ------------------------------------------------------------------ */
 /* solver object                                                       */
 /* ------------------------------------------------------------------ */
 struct gade_solver {
@@ -728,6 +876,15 @@ struct gade_solver {
     long long prof_n[3];
     double prof_ms[3];
     double apply_flops, precond_flops;   /* FP64 flops of one launch */
+    /* mixed precision (GADE_PREC_MIXED) */
+    void *d_M32, *d_S32, *d_H32, *d_D32;
+    void *d_a32[4];
+    void *d_FL32, *d_FU32;
+    float2 *x32, *d32, *q32, *r32, *e32, *ri32, *r032, *p32, *v32, *y32, *z32, *s32, *t32;
+    double2 *xprev, *delta64;
+    DevScal *d_sc2, *h_sc2;
+    int *d_ell_col;
+    int have_prev;
 };
 
 static void prof_begin(gade_solver *s, cudaStream_t st)
@@ -823,6 +980,7 @@ extern "C" void gade_solver_free(gade_solver *s)
     for (void *p : s->allocs) cudaFree(p);
     for (cudaEvent_t e : s->ev_pool) cudaEventDestroy(e);
     if (s->h_sc) cudaFreeHost(s->h_sc);
+    if (s->h_sc2) cudaFreeHost(s->h_sc2);
     if (s->h_coef) cudaFreeHost(s->h_coef);
     if (s->stream) cudaStreamDestroy(s->stream);
     cudaSetDevice(cur);
@@ -988,8 +1146,8 @@ extern "C" int gade_solver_create(const gade_problem *p, double dt, double h, in
         UP(s->d_FU, FU.data(), FU.size());
         size_t smem = sizeof(double2) * ((size_t)2 * CH + s->Bp + 256);
         if (smem > 220 * 1024) { gade_setup_release(su); gade_solver_free(s); return fail(GADE_ERR_ARG, "block dimension too large for the preconditioner"); }
-        cudaFuncSetAttribute(k_precond_tma<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaFuncSetAttribute(k_precond_tma<32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_precond_tma<double, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaFuncSetAttribute(k_precond_tma<double, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     }
     /* vectors */
     double2 **vecs[] = {&s->x, &s->rhs, &s->r, &s->r0, &s->p, &s->v, &s->y, &s->z, &s->s, &s->t, &s->tmp0, &s->tmp1};
@@ -1007,6 +1165,68 @@ extern "C" int gade_solver_create(const gade_problem *p, double dt, double h, in
     if (cudaMallocHost((void **)&s->h_sc, sizeof(DevScal)) != cudaSuccess ||
         cudaMallocHost((void **)&s->h_coef, sizeof(double2) * (size_t)s->lmax * 3) != cudaSuccess) {
         gade_setup_release(su); gade_solver_free(s); return fail(GADE_ERR_CUDA, "pinned allocation failed");
+    }
+    UP(s->d_ell_col, su->ell_col, WB);
+    if (precision == GADE_PREC_MIXED) {
+        /* FP32 copies of every operator and preconditioner table */
+        const int CH = 1024 + 32 * s->bwp;
+        if (s->rc) {
+            R4f *m; UP(m, (const R4f *)nullptr, (size_t)s->lmax * s->nk * WB); s->d_M32 = m;
+        } else {
+            C4<float2> *m; UP(m, (const C4<float2> *)nullptr, (size_t)s->lmax * s->nk * WB); s->d_M32 = m;
+        }
+        {
+            std::vector<float2> Sf((size_t)s->nk * WB), Hf((size_t)s->nk * WB), Df((size_t)s->nk * WB);
+            for (size_t e = 0; e < Sf.size(); e++) {
+                Sf[e] = make_float2((float)su->S_ell[e].re, (float)su->S_ell[e].im);
+                Hf[e] = make_float2((float)su->Hst_ell[e].re, (float)su->Hst_ell[e].im);
+                Df[e] = make_float2((float)(su->S_ell[e].re + su->Hst_ell[e].re), (float)(su->S_ell[e].im + su->Hst_ell[e].im));
+            }
+            float2 *d;
+            UP(d, Sf.data(), Sf.size()); s->d_S32 = d;
+            UP(d, Hf.data(), Hf.size()); s->d_H32 = d;
+            UP(d, Df.data(), Df.size()); s->d_D32 = d;
+        }
+        {
+            const gc64 *src[4] = {su->ang_a0, su->ang_a0k, su->ang_a1, su->ang_a1k};
+            for (int k = 0; k < 4; k++) {
+                if (s->rc) {
+                    std::vector<float> v((size_t)su->n_ang + 1);
+                    for (int64_t e = 0; e < su->n_ang; e++) v[e] = (float)src[k][e].im;
+                    float *d; UP(d, v.data(), su->n_ang); s->d_a32[k] = d;
+                } else {
+                    std::vector<float2> v((size_t)su->n_ang + 1);
+                    for (int64_t e = 0; e < su->n_ang; e++) v[e] = make_float2((float)src[k][e].re, (float)src[k][e].im);
+                    float2 *d; UP(d, v.data(), su->n_ang); s->d_a32[k] = d;
+                }
+            }
+        }
+        {
+            /* FP32 copies of the packed FP64 LU factors */
+            std::vector<double2> FL((size_t)s->nk * s->nch * CH), FU((size_t)s->nk * s->nch * CH);
+            CK(cudaMemcpy(FL.data(), s->d_FL, sizeof(double2) * FL.size(), cudaMemcpyDeviceToHost));
+            CK(cudaMemcpy(FU.data(), s->d_FU, sizeof(double2) * FU.size(), cudaMemcpyDeviceToHost));
+            std::vector<float2> FLf(FL.size()), FUf(FU.size());
+            for (size_t e = 0; e < FL.size(); e++) {
+                FLf[e] = make_float2((float)FL[e].x, (float)FL[e].y);
+                FUf[e] = make_float2((float)FU[e].x, (float)FU[e].y);
+            }
+            float2 *d;
+            UP(d, FLf.data(), FLf.size()); s->d_FL32 = d;
+            UP(d, FUf.data(), FUf.size()); s->d_FU32 = d;
+            size_t smem = sizeof(float2) * ((size_t)2 * CH + s->Bp + 256);
+            cudaFuncSetAttribute(k_precond_tma<float, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            cudaFuncSetAttribute(k_precond_tma<float, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        }
+        float2 **v32[] = {&s->x32, &s->d32, &s->q32, &s->r32, &s->e32, &s->ri32, &s->r032, &s->p32, &s->v32,
+                          &s->y32, &s->z32, &s->s32, &s->t32};
+        for (float2 **vp : v32) UP(*vp, (const float2 *)nullptr, (size_t)s->n);
+        UP(s->xprev, (const double2 *)nullptr, (size_t)s->n);
+        UP(s->delta64, (const double2 *)nullptr, (size_t)s->n);
+        UP(s->d_sc2, (const DevScal *)nullptr, 1);
+        if (cudaMallocHost((void **)&s->h_sc2, sizeof(DevScal)) != cudaSuccess) {
+            gade_setup_release(su); gade_solver_free(s); return fail(GADE_ERR_CUDA, "pinned allocation failed");
+        }
     }
     {
         /* exact FP64 flop count of one operator apply (2 per FMA) */
@@ -1049,7 +1269,7 @@ static int launch_apply(gade_solver *s, const double2 *x, int mode, VecP V, int 
     RedP red = {s->d_part, s->d_ticket, s->d_sc, redkind};
     dim3 grid(s->nchunk, s->nblk);
     int nt = s->RM;
-    size_t smem = sizeof(double2) * 9 * (size_t)s->CM + sizeof(double) * NRED * nt;
+    size_t smem = sizeof(double2) * 11 * (size_t)s->CM + sizeof(double) * NRED * nt;
     prof_begin(s, st);
     if (s->rc) k_apply<double, true><<<grid, nt, smem, st>>>(P, x, mode, V, red);
     else k_apply<double, false><<<grid, nt, smem, st>>>(P, x, mode, V, red);
@@ -1067,14 +1287,14 @@ static int launch_precond(gade_solver *s, int mode, const double2 *in0, const do
     const int CH = 1024 + 32 * s->bwp;
     size_t smem = sizeof(double2) * ((size_t)2 * CH + s->Bp + 256);
     prof_begin(s, st);
-    if (s->bwp == 16) k_precond_tma<16><<<s->nblk, 128, smem, st>>>(Q, mode, in0, in1, io, out, s->d_sc);
-    else k_precond_tma<32><<<s->nblk, 128, smem, st>>>(Q, mode, in0, in1, io, out, s->d_sc);
+    if (s->bwp == 16) k_precond_tma<double, 16><<<s->nblk, 128, smem, st>>>(Q, mode, in0, in1, io, out, s->d_sc);
+    else k_precond_tma<double, 32><<<s->nblk, 128, smem, st>>>(Q, mode, in0, in1, io, out, s->d_sc);
     prof_end(s, st, 1);
     CKL();
     return GADE_OK;
 }
 
-static int launch_tables(gade_solver *s, const double *ft)
+static int launch_tables(gade_solver *s, const double *ft, int which = 1)
 {
     /* c_a = SoL * (i h dt/2) * f_a, as in tools/solver.c:274 */
     const double hdt2 = s->h * s->dt / 2;
@@ -1097,12 +1317,22 @@ static int launch_tables(gade_solver *s, const double *ft)
     long long total = (long long)s->lmax * s->W * s->B;
     int nt = 256;
     long long grid = (total + nt - 1) / nt;
-    prof_begin(s, s->stream);
-    if (s->rc) k_tables<double, true><<<(unsigned)grid, nt, 0, s->stream>>>(T, s->d_coef);
-    else k_tables<double, false><<<(unsigned)grid, nt, 0, s->stream>>>(T, s->d_coef);
-    prof_end(s, s->stream, 2);
-    CKL();
-    s->has_time = 1;
+    if (which & 1) {            /* FP64 tables */
+        prof_begin(s, s->stream);
+        if (s->rc) k_tables<double, true><<<(unsigned)grid, nt, 0, s->stream>>>(T, s->d_coef);
+        else k_tables<double, false><<<(unsigned)grid, nt, 0, s->stream>>>(T, s->d_coef);
+        prof_end(s, s->stream, 2);
+        CKL();
+        s->has_time = 1;
+    }
+    if ((which & 2) && s->d_M32) {   /* FP32 tables (mixed precision) */
+        T.M = s->d_M32;
+        prof_begin(s, s->stream);
+        if (s->rc) k_tables<float, true><<<(unsigned)grid, nt, 0, s->stream>>>(T, s->d_coef);
+        else k_tables<float, false><<<(unsigned)grid, nt, 0, s->stream>>>(T, s->d_coef);
+        prof_end(s, s->stream, 2);
+        CKL();
+    }
     return GADE_OK;
 }
 
@@ -1122,7 +1352,7 @@ extern "C" int gade_solver_set_time(gade_solver *s, const double *ft)
 {
     if (!s || !ft) return fail(GADE_ERR_ARG, "gade_solver_set_time: NULL argument");
     CK(cudaSetDevice(s->device));
-    int rc = launch_tables(s, ft);
+    int rc = launch_tables(s, ft, 3);
     if (rc) return rc;
     CK(cudaStreamSynchronize(s->stream));
     return GADE_OK;
@@ -1135,6 +1365,7 @@ extern "C" int gade_solver_set_x(gade_solver *s, const double *x, int64_t n)
     CK(cudaSetDevice(s->device));
     CK(cudaMemcpyAsync(s->x, x, sizeof(double2) * (size_t)n, cudaMemcpyHostToDevice, s->stream));
     CK(cudaStreamSynchronize(s->stream));
+    s->have_prev = 0;            /* a new state has no extrapolation history */
     return GADE_OK;
 }
 
@@ -1197,12 +1428,183 @@ extern "C" int gade_solver_precond(gade_solver *s, const double *b, double *z)
 
 extern "C" int64_t gade_solver_launch_count(const gade_solver *s) { return s ? s->launches : -1; }
 
+static OpP op_params32(const gade_solver *s)
+{
+    OpP P = op_params(s);
+    P.ang_a0 = s->d_a32[0]; P.ang_a0k = s->d_a32[1]; P.ang_a1 = s->d_a32[2]; P.ang_a1k = s->d_a32[3];
+    P.M = s->d_M32; P.S_ell = s->d_S32; P.Hst_ell = s->d_H32; P.D_ell = s->d_D32;
+    return P;
+}
+
+static int launch_apply32(gade_solver *s, const float2 *x, int mode, VecP V, int redkind, DevScal *sc)
+{
+    OpP P = op_params32(s);
+    RedP red = {s->d_part, s->d_ticket, sc, redkind};
+    dim3 grid(s->nchunk, s->nblk);
+    int nt = s->RM;
+    size_t smem = sizeof(float2) * 11 * (size_t)s->CM + sizeof(double) * NRED * nt;
+    prof_begin(s, s->stream);
+    if (s->rc) k_apply<float, true><<<grid, nt, smem, s->stream>>>(P, x, mode, V, red);
+    else k_apply<float, false><<<grid, nt, smem, s->stream>>>(P, x, mode, V, red);
+    prof_end(s, s->stream, 0);
+    CKL();
+    return GADE_OK;
+}
+
+static int launch_precond32(gade_solver *s, int mode, const float2 *in0, const float2 *in1, float2 *io,
+                            float2 *out, DevScal *sc)
+{
+    PcT Q;
+    Q.nblk = s->nblk; Q.B = s->B; Q.Bp = s->Bp; Q.nch = s->nch;
+    Q.row_kidx = s->d_row_kidx; Q.ord = s->d_ord; Q.FL = s->d_FL32; Q.FU = s->d_FU32;
+    const int CH = 1024 + 32 * s->bwp;
+    size_t smem = sizeof(float2) * ((size_t)2 * CH + s->Bp + 256);
+    prof_begin(s, s->stream);
+    if (s->bwp == 16) k_precond_tma<float, 16><<<s->nblk, 128, smem, s->stream>>>(Q, mode, in0, in1, io, out, sc);
+    else k_precond_tma<float, 32><<<s->nblk, 128, smem, s->stream>>>(Q, mode, in0, in1, io, out, sc);
+    prof_end(s, s->stream, 1);
+    CKL();
+    return GADE_OK;
+}
+
+static int sync_scal2(gade_solver *s)
+{
+    CK(cudaMemcpyAsync(s->h_sc2, s->d_sc2, sizeof(DevScal), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    if (s->h_sc2->err) {
+        unsigned e = s->h_sc2->err;
+        CK(cudaMemsetAsync(&s->d_sc2->err, 0, sizeof(unsigned), s->stream));
+        return fail(GADE_ERR_CUDA, "device wait timed out (flags %u): TMA copy did not complete", e);
+    }
+    return GADE_OK;
+}
+
+#define MIXED_MAX_SWEEPS 8
+#define MIXED_INNER_TOL 1e-6
+
+/*
+ * Mixed-precision CN step.  With delta = x_{n+1} - x_n the CN residual is
+ *   r = (S x_n - H x_n) - (S + H)(x_n + delta) = q - A delta,  q = -2 H x_n,
+ * so the refinement never cancels against S x_n.  FP64 is kept for q, for
+ * every refinement residual q - A delta, for |b|, |r| and for the S-norm
+ * x^H S x; the correction comes from complex64 BiCGSTAB on A e = r with the
+ * FP32-rounded block-LU factors (FP64 LU on the host).  The inner recursive
+ * residual of e is accurate to ~1e-7 |r|, so once the FP64 residual r is
+ * small the inner estimate certifies |q - A (delta + e)| without another FP64
+ * operator pass; otherwise the FP64 residual is recomputed and refinement
+ * continues.  delta starts from the linear extrapolation x_n - x_{n-1}.
+ */
+static int mixed_step(gade_solver *s, const double *ft, int32_t maxit, double tol, gade_step_stats *stats)
+{
+    int rc;
+    gade_step_stats st = {};
+    const long long n = s->n;
+    const int grid = s->upd_grid, blk = s->upd_block;
+    const size_t rsm = sizeof(double) * NRED * blk;
+    if ((rc = launch_tables(s, ft, 3))) return rc;
+    prof_begin(s, s->stream);
+    k_mixed_prep<<<grid, blk, 0, s->stream>>>(n, s->x, s->xprev, s->have_prev, s->delta64, s->d32, s->tmp0);
+    prof_end(s, s->stream, 2);
+    CKL();
+    const double eps2 = 1e-12 * 1e-12;
+    const int maxit_in = maxit < 50 ? maxit : 50;
+    int sweep = 0, inner = 0, fp64_res = 0;
+    double rr = 0, b2 = 0, tol2 = 0;
+    bool done = false;
+    while (!done) {
+        /* one FP64 pass: r = q - A delta = -S delta - H (2 x_n + delta); the
+           first pass also gives |b|^2 (b = S x_n - H w/2 differs from the CN
+           right-hand side by H delta/2, ~1e-8 relative) and x_n^H S x_n */
+        VecP R = {};
+        R.out0 = s->r; R.in0 = s->x; R.in1 = s->delta64;
+        if ((rc = launch_apply(s, s->tmp0, AX_MIX, R, RED_MIX, s->stream))) return rc;
+        if ((rc = sync_scal(s))) return rc;
+        fp64_res++;
+        rr = s->h_sc->rr;
+        if (fp64_res == 1) {
+            b2 = s->h_sc->rhs_sqnorm;
+            st.snorm = s->h_sc->snorm;
+            tol2 = tol * tol * b2;
+            if (!std::isfinite(b2)) return fail(GADE_ERR_NUMERIC, "non-finite right-hand side");
+            if (b2 == 0) {
+                CK(cudaMemsetAsync(s->x, 0, sizeof(double2) * (size_t)n, s->stream));
+                CK(cudaStreamSynchronize(s->stream));
+                s->have_prev = 0;
+                if (stats) *stats = st;
+                return GADE_OK;
+            }
+        }
+        if (!std::isfinite(rr)) return fail(GADE_ERR_NUMERIC, "non-finite refinement residual");
+        if (rr < tol2 || sweep >= MIXED_MAX_SWEEPS || maxit_in <= 0) break;
+        sweep++;
+        {
+            RedP red = {s->d_part, s->d_ticket, s->d_sc2, RED_RHS};
+            prof_begin(s, s->stream);
+            k_inner_init<<<grid, blk, rsm, s->stream>>>(n, s->r, s->e32, s->ri32, s->r032, s->p32, s->v32, red);
+            prof_end(s, s->stream, 2);
+            CKL();
+        }
+        if ((rc = sync_scal2(s))) return rc;
+        const double r0in = s->h_sc2->r0_sqnorm;
+        /* run the cheap inner solve until its estimate of the outer residual
+           certifies the tolerance (the estimate is good to ~1e-7 |r|) */
+        const double tol_in2 = 0.25 * tol2;
+        double rin = r0in;
+        for (int it = 0; it < maxit_in; it++) {
+            if (fabs(s->h_sc2->rho.x) < eps2 * r0in) break;     /* breakdown: refine again */
+            if ((rc = launch_precond32(s, PC_P, s->ri32, s->v32, s->p32, s->y32, s->d_sc2))) return rc;
+            VecP A1 = {}; A1.out0 = s->v32; A1.in0 = s->r032;
+            if ((rc = launch_apply32(s, s->y32, AX_R0V, A1, RED_R0V, s->d_sc2))) return rc;
+            if ((rc = launch_precond32(s, PC_S, s->ri32, s->v32, s->s32, s->z32, s->d_sc2))) return rc;
+            VecP A2 = {}; A2.out0 = s->t32; A2.in0 = s->s32;
+            if ((rc = launch_apply32(s, s->z32, AX_TS, A2, RED_TS, s->d_sc2))) return rc;
+            {
+                RedP red = {s->d_part, s->d_ticket, s->d_sc2, RED_UPDATE};
+                prof_begin(s, s->stream);
+                k_update<float><<<grid, blk, rsm, s->stream>>>(n, s->e32, s->y32, s->z32, s->ri32, s->s32,
+                                                               s->t32, s->r032, red);
+                prof_end(s, s->stream, 2);
+                CKL();
+            }
+            if ((rc = sync_scal2(s))) return rc;
+            inner++;
+            rin = s->h_sc2->rr;
+            if (!(rin >= tol_in2)) break;
+        }
+        prof_begin(s, s->stream);
+        k_delta_add<<<grid, blk, 0, s->stream>>>(n, s->delta64, s->e32, s->d32, s->x, s->tmp0);
+        prof_end(s, s->stream, 2);
+        CKL();
+        const double est_err2 = 1e-14 * r0in;
+        if (std::isfinite(rin) && rin + est_err2 < 0.25 * tol2) {
+            rr = rin + est_err2;
+            done = true;
+        }
+    }
+    prof_begin(s, s->stream);
+    k_mixed_finish<<<grid, blk, 0, s->stream>>>(n, s->x, s->xprev, s->delta64);
+    prof_end(s, s->stream, 2);
+    CKL();
+    s->have_prev = 1;
+    st.iters = inner;
+    st.inner_iters = inner;
+    st.refinements = fp64_res;
+    st.true_residual = sqrt(rr / b2);
+    st.tol_error = st.true_residual;
+    if (stats) *stats = st;
+    if (!(rr < tol2) && maxit_in > 0)
+        return fail(GADE_ERR_NUMERIC, "mixed-precision refinement stalled at |r|/|b| = %.3e > tol %.3e after %d sweeps",
+                    sqrt(rr / b2), tol, sweep);
+    return GADE_OK;
+}
+
 extern "C" int gade_solver_step(gade_solver *s, const double *ft, int32_t maxit, double tol,
                                 gade_step_stats *stats)
 {
     if (!s || !ft) return fail(GADE_ERR_ARG, "gade_solver_step: NULL argument");
     if (maxit < 0) return fail(GADE_ERR_ARG, "gade_solver_step: maxit < 0");
     CK(cudaSetDevice(s->device));
+    if (s->prec == GADE_PREC_MIXED) return mixed_step(s, ft, maxit, tol, stats);
     int rc;
     gade_step_stats st = {};
     if ((rc = launch_tables(s, ft))) return rc;
@@ -1445,7 +1847,7 @@ extern "C" int gade_solver_apply_dot_noalloc(gade_solver *s, const void *x_dev, 
     V.in0 = r0_dev;
     dim3 grid(s->nchunk, s->nblk);
     int nt = s->RM;
-    size_t smem = sizeof(double2) * 9 * (size_t)s->CM + sizeof(double) * NRED * nt;
+    size_t smem = sizeof(double2) * 11 * (size_t)s->CM + sizeof(double) * NRED * nt;
     if (s->rc) k_apply<double, true><<<grid, nt, smem, st>>>(P, (const double2 *)x_dev, AX_R0V, V, red);
     else k_apply<double, false><<<grid, nt, smem, st>>>(P, (const double2 *)x_dev, AX_R0V, V, red);
     CKL();

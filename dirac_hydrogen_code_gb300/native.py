@@ -31,7 +31,8 @@ class ProblemInfo(C.Structure):
 
 class StepStats(C.Structure):
     _fields_ = [("iters", C.c_int32), ("tol_error", C.c_double), ("restarts", C.c_int32),
-                ("refinements", C.c_int32), ("inner_iters", C.c_int32), ("true_residual", C.c_double)]
+                ("refinements", C.c_int32), ("inner_iters", C.c_int32), ("true_residual", C.c_double),
+                ("snorm", C.c_double)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -49,7 +49,8 @@ typedef struct {
     int32_t restarts;     /* BiCGSTAB restarts (|rho| tiny)                     */
     int32_t refinements;  /* outer FP64 refinement sweeps (mixed precision)    */
     int32_t inner_iters;  /* total inner complex64 iterations (mixed)          */
-    double  true_residual;/* FP64 |b - A x|/|b| at exit (mixed precision only) */
+    double  true_residual;/* |b - A x|/|b| at exit (mixed precision only)      */
+    double  snorm;        /* x^H S x before the step, FP64 (mixed precision)  */
 } gade_step_stats;
 
 /* Message of the last failing call on this thread ("" if none). */
