@@ -261,6 +261,10 @@ def run_ours(args):
         "kernel_share": {"apply": kt["apply_ms"], "precond": kt["precond_ms"], "other": kt["other_ms"]},
     }
 
+    variants = None
+    if rank == 0 and not args.no_variants:
+        variants = mixed_variant(prob, params, info, T, args, device, torch, native, psi, fts, l2_flush)
+
     # CPU baseline on a bounded sample (rank 0, N=1)
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
@@ -283,6 +287,7 @@ def run_ours(args):
             "roofline": roof,
             "cpu_baseline": cpu,
             "clocks": clk,
+            "variants": variants,
         }
         print(json.dumps(line))
     if dist is not None:
@@ -291,6 +296,66 @@ def run_ours(args):
     prob.close()
     tmp.cleanup()
     return 0
+
+
+def _timed_steps(sol, fts, idx, steps, warmup, tol, stream, l2_flush, torch):
+    """Warm-up then `steps` CN steps timed with CUDA events on the solver's
+    stream (L2 flushed between steps, outside the events).  Returns
+    (ms_total, records, next index, kernel times)."""
+    for _ in range(warmup):
+        sol.step(fts[idx % len(fts)], MAXIT, tol)
+        idx += 1
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    recs = []
+    torch.cuda.synchronize()
+    sol.profile(True)
+    for k in range(steps):
+        with torch.cuda.stream(stream):
+            l2_flush.add_(1.0)
+            ev[k][0].record(stream)
+        recs.append(sol.step(fts[idx % len(fts)], MAXIT, tol))
+        with torch.cuda.stream(stream):
+            ev[k][1].record(stream)
+        idx += 1
+    torch.cuda.synchronize()
+    kt = sol.kernel_times()
+    sol.profile(False)
+    return sum(a.elapsed_time(b) for a, b in ev), recs, idx, kt
+
+
+def mixed_variant(prob, params, info, T, args, device, torch, native, psi, fts, l2_flush):
+    """Mixed precision (complex64 inner BiCGSTAB in FP64 refinement) against
+    plain FP64, both from psi0 over the same warm-up + timed steps at the
+    refinement tolerance 1e-10; error = relative S-norm and L2 of the final
+    state against the plain FP64 run at the configuration's tolerance."""
+    import numpy as np
+    from dirac_hydrogen_code_gb300.cn import step_times
+    dt, _ = step_times(T, params["Ntime"])
+    out = {}
+    finals = {}
+    for tag, prec, tol in (("fp64", "fp64", TOL), ("fp64_tol1e-10", "fp64", 1e-10), ("mixed_tol1e-10", "mixed", 1e-10)):
+        sol = native.Solver(prob, dt, 1.0, precision=prec, device=device)
+        sol.set_x(psi)
+        stream = torch.cuda.ExternalStream(sol.stream(), device=device)
+        ms, recs, _, kt = _timed_steps(sol, fts, 0, args.steps, args.warmup, tol, stream, l2_flush, torch)
+        finals[tag] = sol.get_x()
+        out[tag] = {"steps_per_s": args.steps / (ms / 1e3), "ms_per_step": ms / args.steps,
+                    "inner_iters_per_step": float(np.mean([r["inner_iters"] for r in recs])),
+                    "fp64_residual_passes_per_step": float(np.mean([r["refinements"] for r in recs])),
+                    "kernel_ms_per_step": {k: round(v / args.steps, 4) for k, v in kt.items() if k.endswith("_ms")}}
+        sol.close()
+    ref = finals["fp64"]
+    chk = native.Solver(prob, dt, 1.0, precision="fp64", device=device)
+    chk.set_time(fts[0])
+    _, sref, _ = chk.apply(ref, parts=True)
+    for tag in ("fp64_tol1e-10", "mixed_tol1e-10"):
+        e = finals[tag] - ref
+        _, se, _ = chk.apply(e, parts=True)
+        out[tag]["err_vs_fp64"] = {"s_norm_rel": float(np.sqrt(abs(np.vdot(e, se).real) / abs(np.vdot(ref, sref).real))),
+                                   "l2_rel": float(np.linalg.norm(e) / np.linalg.norm(ref))}
+    chk.close()
+    out["speedup_mixed_vs_fp64_at_1e-10"] = out["mixed_tol1e-10"]["steps_per_s"] / out["fp64_tol1e-10"]["steps_per_s"]
+    return out
 
 
 def _ncu_traffic():
@@ -306,6 +371,29 @@ def _ncu_traffic():
     return None
 
 
+def profile_only(args):
+    """Warm-up and timed steps of one precision, nothing else: a small,
+    deterministic launch sequence for profiler captures."""
+    import torch
+    from dirac_hydrogen_code_gb300 import native
+    from dirac_hydrogen_code_gb300.cn import pulse, step_times
+    native.load_library()
+    with tempfile.TemporaryDirectory() as d:
+        params, info, T = _gen(d)
+        prob = native.Problem(d, info["lmax"])
+        dt, steps = step_times(T, params["Ntime"])
+        sol = native.Solver(prob, dt, 1.0, precision=args.profile_precision, device=0)
+        tol = TOL if args.profile_precision == "fp64" else 1e-10
+        for k in range(args.warmup + args.steps):
+            sol.step(pulse(params["Intensity"], params["Omega"], params["Cycles"], steps[k][1]), MAXIT, tol)
+        torch.cuda.synchronize()
+        print(json.dumps({"profiled": args.profile_precision, "steps": args.warmup + args.steps,
+                          "launches": sol.launch_count()}))
+        sol.close()
+        prob.close()
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -314,11 +402,16 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=4)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-variants", action="store_true", help="skip the mixed-precision comparison")
+    ap.add_argument("--profile-precision", default=None, choices=["fp64", "mixed"],
+                    help="only run this precision's steps (for profiler captures)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile_precision:
+        return profile_only(args)
     return run_ours(args)
 
 

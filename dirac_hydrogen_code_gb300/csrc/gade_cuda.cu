@@ -336,7 +336,7 @@ __global__ void k_tables(TabP T, const double2 *__restrict__ coef)
 /* ------------------------------------------------------------------ */
 /* grid (nchunk, nblk); blockDim = RM (one thread per row of the chunk) */
 template <typename R, bool RC>
-__global__ void __launch_bounds__(128) k_apply(OpP P, const typename Cx<R>::T *__restrict__ x, int mode,
+__global__ void __launch_bounds__(256) k_apply(OpP P, const typename Cx<R>::T *__restrict__ x, int mode,
                                                VecP V, RedP red)
 {
     typedef typename Cx<R>::T C;
@@ -345,7 +345,8 @@ __global__ void __launch_bounds__(128) k_apply(OpP P, const typename Cx<R>::T *_
     C *ub = xr + P.CM;                        /* [2][4][CM] double-buffered u, w, u', w' */
     C *xs = ub + 8 * P.CM;                    /* [CM] AX_MIX: x_n slice   */
     C *ds = xs + P.CM;                        /* [CM] AX_MIX: delta slice */
-    double *shred = (double *)(ds + P.CM);    /* [NRED * blockDim] */
+    int *lcs = (int *)(ds + P.CM);            /* [W][RM] local column of each ELL slot */
+    double *shred = (double *)(lcs + P.W * P.RM); /* [NRED * blockDim] */
 
     const int q = blockIdx.x, r = blockIdx.y, tid = threadIdx.x, nt = blockDim.x;
     const int B = P.B, W = P.W, CM = P.CM;
@@ -353,8 +354,12 @@ __global__ void __launch_bounds__(128) k_apply(OpP P, const typename Cx<R>::T *_
     const int nrows = P.chunk_nrows[q], ncols = P.chunk_ncols[q];
     const int i = (tid < nrows) ? P.chunk_rows[q * P.RM + tid] : -1;
     const int *cols = P.chunk_cols + (size_t)q * CM;
-    const int *lcol = P.chunk_lcol + (size_t)q * W * P.RM;
+    const int *lcol = lcs;
     const C *xb = x + (size_t)r * B;
+    {
+        const int *gl = P.chunk_lcol + (size_t)q * W * P.RM;
+        for (int e = tid; e < W * P.RM; e += nt) lcs[e] = gl[e];
+    }
     /* rhs/parts modes need S x and H x apart; A x modes use D = S + i h dt/2 h0 */
     const bool separate = (mode == AX_RHS || mode == AX_PARTS || mode == AX_QB);
 
@@ -411,6 +416,7 @@ __global__ void __launch_bounds__(128) k_apply(OpP P, const typename Cx<R>::T *_
         for (int c = tid; c < ncols; c += nt) {
             const int gc = cols[c];
             C U = mk<C>(0, 0), Wv = mk<C>(0, 0), U1 = mk<C>(0, 0), W1 = mk<C>(0, 0);
+#pragma unroll 4
             for (int e = e0; e < e1; e++) {
                 const C xv = x[(size_t)P.ang_c[e] * B + gc];
                 if (RC) {
@@ -430,6 +436,7 @@ __global__ void __launch_bounds__(128) k_apply(OpP P, const typename Cx<R>::T *_
         __syncthreads();
         if (i >= 0) {
             const size_t base = ((size_t)l * P.nk + kk) * W * B;
+#pragma unroll 6
             for (int j = 0; j < W; j++) {
                 const int lc = lcol[j * P.RM + tid];
                 if (lc < 0) continue;
@@ -1020,7 +1027,19 @@ extern "C" int gade_solver_create(const gade_problem *p, double dt, double h, in
     int cs = choose_chunk_splines(p->nblk, p->blkdim, prop.multiProcessorCount);
     int rcode = gade_setup_build(p, dt, h, cs, &su, err, sizeof(err));
     if (rcode) return fail(rcode, "%s", err);
-    if (su->chunk_rows_max > 128) { gade_setup_release(su); return fail(GADE_ERR_ARG, "chunk too large"); }
+    if (su->chunk_rows_max > 128 || su->chunk_cols_max > 256) {
+        gade_setup_release(su);
+        return fail(GADE_ERR_ARG, "row chunk too large for the operator kernel (rows %d, columns %d)",
+                    su->chunk_rows_max, su->chunk_cols_max);
+    }
+    {
+        /* operator kernels may use more than the default 48 KB of dynamic shared memory */
+        const int lim = 160 * 1024;
+        cudaFuncSetAttribute(k_apply<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+    }
 
     gade_solver *s = new gade_solver();
     s->device = device;
@@ -1263,13 +1282,23 @@ static OpP op_params(const gade_solver *s)
     return P;
 }
 
+/* k_apply launch shape: one thread per output row and per gathered column */
+static void apply_dims(const gade_solver *s, size_t elem, int *nt, size_t *smem)
+{
+    int t = s->RM > s->CM ? s->RM : s->CM;
+    t = (t + 31) / 32 * 32;
+    *nt = t;
+    *smem = elem * 11 * (size_t)s->CM + sizeof(int) * (size_t)s->W * s->RM + sizeof(double) * NRED * t;
+}
+
 static int launch_apply(gade_solver *s, const double2 *x, int mode, VecP V, int redkind, cudaStream_t st)
 {
     OpP P = op_params(s);
     RedP red = {s->d_part, s->d_ticket, s->d_sc, redkind};
     dim3 grid(s->nchunk, s->nblk);
-    int nt = s->RM;
-    size_t smem = sizeof(double2) * 11 * (size_t)s->CM + sizeof(double) * NRED * nt;
+    int nt;
+    size_t smem;
+    apply_dims(s, sizeof(double2), &nt, &smem);
     prof_begin(s, st);
     if (s->rc) k_apply<double, true><<<grid, nt, smem, st>>>(P, x, mode, V, red);
     else k_apply<double, false><<<grid, nt, smem, st>>>(P, x, mode, V, red);
@@ -1441,8 +1470,9 @@ static int launch_apply32(gade_solver *s, const float2 *x, int mode, VecP V, int
     OpP P = op_params32(s);
     RedP red = {s->d_part, s->d_ticket, sc, redkind};
     dim3 grid(s->nchunk, s->nblk);
-    int nt = s->RM;
-    size_t smem = sizeof(float2) * 11 * (size_t)s->CM + sizeof(double) * NRED * nt;
+    int nt;
+    size_t smem;
+    apply_dims(s, sizeof(float2), &nt, &smem);
     prof_begin(s, s->stream);
     if (s->rc) k_apply<float, true><<<grid, nt, smem, s->stream>>>(P, x, mode, V, red);
     else k_apply<float, false><<<grid, nt, smem, s->stream>>>(P, x, mode, V, red);
@@ -1846,8 +1876,9 @@ extern "C" int gade_solver_apply_dot_noalloc(gade_solver *s, const void *x_dev, 
     V.out0 = y_dev;
     V.in0 = r0_dev;
     dim3 grid(s->nchunk, s->nblk);
-    int nt = s->RM;
-    size_t smem = sizeof(double2) * 11 * (size_t)s->CM + sizeof(double) * NRED * nt;
+    int nt;
+    size_t smem;
+    apply_dims(s, sizeof(double2), &nt, &smem);
     if (s->rc) k_apply<double, true><<<grid, nt, smem, st>>>(P, (const double2 *)x_dev, AX_R0V, V, red);
     else k_apply<double, false><<<grid, nt, smem, st>>>(P, (const double2 *)x_dev, AX_R0V, V, red);
     CKL();
