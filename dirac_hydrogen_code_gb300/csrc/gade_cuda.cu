@@ -35,6 +35,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "gade_internal.h"
@@ -144,7 +145,7 @@ enum { PC_PLAIN = 0, PC_P, PC_S };
 /* operator parameters                                                 */
 /* ------------------------------------------------------------------ */
 struct OpP {
-    int nblk, B, lmax, W, nk, RM, CM;
+    int nblk, B, lmax, W, nk, RM, CM, AM;   /* AM: max angular terms of one block row */
     const int *row_kidx, *act_ptr, *act_l, *ang_ptr, *ang_c;
     const void *ang_a0, *ang_a0k, *ang_a1, *ang_a1k;
     const int *chunk_nrows, *chunk_ncols, *chunk_rows, *chunk_cols, *chunk_lcol;
@@ -341,24 +342,40 @@ __global__ void __launch_bounds__(256) k_apply(OpP P, const typename Cx<R>::T *_
 {
     typedef typename Cx<R>::T C;
     extern __shared__ unsigned char smem_raw[];
+    /* G orders per gather phase: 2 (FP64) or 4 (FP32); u, w, u', w' of each */
+    constexpr int G = sizeof(R) == 8 ? 2 : 4;
     C *xr = (C *)smem_raw;                    /* [CM] */
-    C *ub = xr + P.CM;                        /* [2][4][CM] double-buffered u, w, u', w' */
-    C *xs = ub + 8 * P.CM;                    /* [CM] AX_MIX: x_n slice   */
+    C *ub = xr + P.CM;                        /* [G][4][CM] */
+    C *xs = ub + 4 * G * P.CM;                /* [CM] AX_MIX: x_n slice   */
     C *ds = xs + P.CM;                        /* [CM] AX_MIX: delta slice */
     int *lcs = (int *)(ds + P.CM);            /* [W][RM] local column of each ELL slot */
-    double *shred = (double *)(lcs + P.W * P.RM); /* [NRED * blockDim] */
+    int *angc = lcs + P.W * P.RM;             /* [AM] coupled block of each angular term of row r */
+    typedef typename std::conditional<RC, R, C>::type A;
+    A *ang = (A *)(angc + ((P.AM + 3) & ~3)); /* [4][AM] a0, a0 k_c, a1, a1 k_c (16-byte aligned) */
+    double *shred = (double *)(ang + 4 * P.AM); /* [NRED * blockDim] */
 
     const int q = blockIdx.x, r = blockIdx.y, tid = threadIdx.x, nt = blockDim.x;
     const int B = P.B, W = P.W, CM = P.CM;
     const int kk = P.row_kidx[r];
     const int nrows = P.chunk_nrows[q], ncols = P.chunk_ncols[q];
-    const int i = (tid < nrows) ? P.chunk_rows[q * P.RM + tid] : -1;
+    /* two threads per output row, each with half of the ELL slots */
+    const int half = tid / P.RM, trow = tid - half * P.RM;
+    const int i = (half < 2 && trow < nrows) ? P.chunk_rows[q * P.RM + trow] : -1;
+    const int jb = half == 0 ? 0 : (W + 1) / 2, je = half == 0 ? (W + 1) / 2 : W;
     const int *cols = P.chunk_cols + (size_t)q * CM;
     const int *lcol = lcs;
     const C *xb = x + (size_t)r * B;
     {
         const int *gl = P.chunk_lcol + (size_t)q * W * P.RM;
         for (int e = tid; e < W * P.RM; e += nt) lcs[e] = gl[e];
+    }
+    const int ea = P.ang_ptr[r * P.lmax], eb = P.ang_ptr[r * P.lmax + P.lmax];
+    for (int e = tid; e < eb - ea; e += nt) {
+        angc[e] = P.ang_c[ea + e];
+        ang[e] = ((const A *)P.ang_a0)[ea + e];
+        ang[P.AM + e] = ((const A *)P.ang_a0k)[ea + e];
+        ang[2 * P.AM + e] = ((const A *)P.ang_a1)[ea + e];
+        ang[3 * P.AM + e] = ((const A *)P.ang_a1k)[ea + e];
     }
     /* rhs/parts modes need S x and H x apart; A x modes use D = S + i h dt/2 h0 */
     const bool separate = (mode == AX_RHS || mode == AX_PARTS || mode == AX_QB);
@@ -376,8 +393,8 @@ __global__ void __launch_bounds__(256) k_apply(OpP P, const typename Cx<R>::T *_
             /* x = w = 2 x_n + delta: S x_n, S delta and (i h dt/2 h0) w */
             const C *Se = (const C *)P.S_ell + (size_t)kk * W * B;
             const C *He = (const C *)P.Hst_ell + (size_t)kk * W * B;
-            for (int j = 0; j < W; j++) {
-                const int lc = lcol[j * P.RM + tid];
+            for (int j = jb; j < je; j++) {
+                const int lc = lcol[j * P.RM + trow];
                 if (lc >= 0) {
                     const C sv = Se[(size_t)j * B + i];
                     cfma(accS, sv, xs[lc]);
@@ -388,8 +405,8 @@ __global__ void __launch_bounds__(256) k_apply(OpP P, const typename Cx<R>::T *_
         } else if (separate) {
             const C *Se = (const C *)P.S_ell + (size_t)kk * W * B;
             const C *He = (const C *)P.Hst_ell + (size_t)kk * W * B;
-            for (int j = 0; j < W; j++) {
-                const int lc = lcol[j * P.RM + tid];
+            for (int j = jb; j < je; j++) {
+                const int lc = lcol[j * P.RM + trow];
                 if (lc >= 0) {
                     const C xv = xr[lc];
                     cfma(accS, Se[(size_t)j * B + i], xv);
@@ -398,69 +415,87 @@ __global__ void __launch_bounds__(256) k_apply(OpP P, const typename Cx<R>::T *_
             }
         } else {
             const C *De = (const C *)P.D_ell + (size_t)kk * W * B;
-            for (int j = 0; j < W; j++) {
-                const int lc = lcol[j * P.RM + tid];
+            for (int j = jb; j < je; j++) {
+                const int lc = lcol[j * P.RM + trow];
                 if (lc >= 0) cfma(accS, De[(size_t)j * B + i], xr[lc]);
             }
         }
     }
 
-    int buf = 0;
-    for (int a = P.act_ptr[r]; a < P.act_ptr[r + 1]; a++, buf ^= 1) {
-        const int l = P.act_l[a];
-        const int e0 = P.ang_ptr[r * P.lmax + l], e1 = P.ang_ptr[r * P.lmax + l + 1];
-        C *u0 = ub + buf * 4 * CM, *u1 = u0 + CM, *u2 = u1 + CM, *u3 = u2 + CM;
-        /* gather into the buffer not read by the previous order's apply; one
-           barrier per order suffices (every thread finished apply(a-1) before
-           it gathered for a) */
-        for (int c = tid; c < ncols; c += nt) {
+    const int a_beg = P.act_ptr[r], a_end = P.act_ptr[r + 1];
+    for (int ag = a_beg; ag < a_end; ag += G) {
+        const int ng = a_end - ag < G ? a_end - ag : G;
+        __syncthreads();     /* staging done / previous group's apply done */
+        /* gather u, w, u', w' of ng orders at once: (order, column) items */
+        for (int item = tid; item < ng * ncols; item += nt) {
+            const int g = item / ncols, c = item - g * ncols;
+            const int l = P.act_l[ag + g];
+            const int e0 = P.ang_ptr[r * P.lmax + l] - ea, e1 = P.ang_ptr[r * P.lmax + l + 1] - ea;
             const int gc = cols[c];
             C U = mk<C>(0, 0), Wv = mk<C>(0, 0), U1 = mk<C>(0, 0), W1 = mk<C>(0, 0);
 #pragma unroll 4
             for (int e = e0; e < e1; e++) {
-                const C xv = x[(size_t)P.ang_c[e] * B + gc];
-                if (RC) {
-                    rfma(U, ((const R *)P.ang_a0)[e], xv);
-                    rfma(Wv, ((const R *)P.ang_a0k)[e], xv);
-                    rfma(U1, ((const R *)P.ang_a1)[e], xv);
-                    rfma(W1, ((const R *)P.ang_a1k)[e], xv);
+                const C xv = x[(size_t)angc[e] * B + gc];
+                if constexpr (RC) {
+                    rfma(U, ang[e], xv);
+                    rfma(Wv, ang[P.AM + e], xv);
+                    rfma(U1, ang[2 * P.AM + e], xv);
+                    rfma(W1, ang[3 * P.AM + e], xv);
                 } else {
-                    cfma(U, ((const C *)P.ang_a0)[e], xv);
-                    cfma(Wv, ((const C *)P.ang_a0k)[e], xv);
-                    cfma(U1, ((const C *)P.ang_a1)[e], xv);
-                    cfma(W1, ((const C *)P.ang_a1k)[e], xv);
+                    cfma(U, ang[e], xv);
+                    cfma(Wv, ang[P.AM + e], xv);
+                    cfma(U1, ang[2 * P.AM + e], xv);
+                    cfma(W1, ang[3 * P.AM + e], xv);
                 }
             }
-            u0[c] = U; u1[c] = Wv; u2[c] = U1; u3[c] = W1;
+            C *u = ub + g * 4 * CM;
+            u[c] = U; u[CM + c] = Wv; u[2 * CM + c] = U1; u[3 * CM + c] = W1;
         }
         __syncthreads();
         if (i >= 0) {
-            const size_t base = ((size_t)l * P.nk + kk) * W * B;
+            for (int g = 0; g < ng; g++) {
+                const int l = P.act_l[ag + g];
+                const C *u0 = ub + g * 4 * CM, *u1 = u0 + CM, *u2 = u1 + CM, *u3 = u2 + CM;
+                const size_t base = ((size_t)l * P.nk + kk) * W * B;
 #pragma unroll 6
-            for (int j = 0; j < W; j++) {
-                const int lc = lcol[j * P.RM + tid];
-                if (lc < 0) continue;
-                if (RC) {
-                    typedef typename R4<R>::T Q4;
-                    const Q4 m = ((const Q4 *)P.M)[base + (size_t)j * B + i];
-                    rfma(accH, m.a, u0[lc]);
-                    rfma(accH, m.b, u1[lc]);
-                    rfma(accH, m.c, u2[lc]);
-                    rfma(accH, m.d, u3[lc]);
-                } else {
-                    const C4<C> m = ((const C4<C> *)P.M)[base + (size_t)j * B + i];
-                    cfma(accH, m.a, u0[lc]);
-                    cfma(accH, m.b, u1[lc]);
-                    cfma(accH, m.c, u2[lc]);
-                    cfma(accH, m.d, u3[lc]);
+                for (int j = jb; j < je; j++) {
+                    const int lc = lcol[j * P.RM + trow];
+                    if (lc < 0) continue;
+                    if constexpr (RC) {
+                        typedef typename R4<R>::T Q4;
+                        const Q4 m = ((const Q4 *)P.M)[base + (size_t)j * B + i];
+                        rfma(accH, m.a, u0[lc]);
+                        rfma(accH, m.b, u1[lc]);
+                        rfma(accH, m.c, u2[lc]);
+                        rfma(accH, m.d, u3[lc]);
+                    } else {
+                        const C4<C> m = ((const C4<C> *)P.M)[base + (size_t)j * B + i];
+                        cfma(accH, m.a, u0[lc]);
+                        cfma(accH, m.b, u1[lc]);
+                        cfma(accH, m.c, u2[lc]);
+                        cfma(accH, m.d, u3[lc]);
+                    }
                 }
             }
         }
     }
 
+    /* combine the two halves of every row */
+    __syncthreads();
+    {
+        C *xch = (C *)shred;                  /* 3 per row; fits in the reduction buffer */
+        if (half == 1 && i >= 0) { xch[3 * trow] = accS; xch[3 * trow + 1] = accH; xch[3 * trow + 2] = accD; }
+        __syncthreads();
+        if (half == 0 && i >= 0) {
+            accS = cadd(accS, xch[3 * trow]);
+            accH = cadd(accH, xch[3 * trow + 1]);
+            accD = cadd(accD, xch[3 * trow + 2]);
+        }
+        __syncthreads();
+    }
     /* epilogue */
     double v[NRED] = {0, 0, 0, 0};
-    if (i >= 0) {
+    if (half == 0 && i >= 0) {
         const size_t gi = (size_t)r * B + i;
         const C ax = cadd(accH, accS);
         switch (mode) {
@@ -848,7 +883,7 @@ struct gade_solver {
     cudaStream_t stream;
     int prec, rc;
     long long n;
-    int nblk, B, lmax, W, nk, RM, CM, nchunk;
+    int nblk, B, lmax, W, nk, RM, CM, nchunk, AM;
     int bw, Bp, nch;
     double dt, h;
     /* operator tables */
@@ -1047,6 +1082,11 @@ extern "C" int gade_solver_create(const gade_problem *p, double dt, double h, in
     s->rc = p->real_coupling;
     s->n = p->n; s->nblk = p->nblk; s->B = p->blkdim; s->lmax = p->lmax;
     s->W = su->W; s->nk = su->nk; s->RM = su->chunk_rows_max; s->CM = su->chunk_cols_max;
+    s->AM = 1;
+    for (int r = 0; r < p->nblk; r++) {
+        int na = su->ang_ptr[(size_t)(r + 1) * p->lmax] - su->ang_ptr[(size_t)r * p->lmax];
+        if (na > s->AM) s->AM = na;
+    }
     s->nchunk = su->nchunk; s->bw = su->bw; s->Bp = su->Bp; s->nch = su->nch;
     s->dt = dt; s->h = h; s->blk_nnz = p->blk_nnz;
     if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
@@ -1273,6 +1313,7 @@ static OpP op_params(const gade_solver *s)
 {
     OpP P;
     P.nblk = s->nblk; P.B = s->B; P.lmax = s->lmax; P.W = s->W; P.nk = s->nk; P.RM = s->RM; P.CM = s->CM;
+    P.AM = s->AM;
     P.row_kidx = s->d_row_kidx; P.act_ptr = s->d_act_ptr; P.act_l = s->d_act_l;
     P.ang_ptr = s->d_ang_ptr; P.ang_c = s->d_ang_c;
     P.ang_a0 = s->d_ang_a0; P.ang_a0k = s->d_ang_a0k; P.ang_a1 = s->d_ang_a1; P.ang_a1k = s->d_ang_a1k;
@@ -1285,10 +1326,17 @@ static OpP op_params(const gade_solver *s)
 /* k_apply launch shape: one thread per output row and per gathered column */
 static void apply_dims(const gade_solver *s, size_t elem, int *nt, size_t *smem)
 {
-    int t = s->RM > s->CM ? s->RM : s->CM;
+    int t = 2 * s->RM > s->CM ? 2 * s->RM : s->CM;   /* two threads per row */
     t = (t + 31) / 32 * 32;
     *nt = t;
-    *smem = elem * 11 * (size_t)s->CM + sizeof(int) * (size_t)s->W * s->RM + sizeof(double) * NRED * t;
+    const size_t G = elem == sizeof(double2) ? 2 : 4;
+    const size_t areal = s->rc ? elem / 2 : elem;   /* one angular factor */
+    size_t b = elem * (3 + 4 * G) * (size_t)s->CM            /* xr, u-groups, xs, ds */
+             + sizeof(int) * (size_t)s->W * s->RM           /* ELL local columns */
+             + sizeof(int) * (size_t)((s->AM + 3) & ~3)     /* angular blocks */
+             + areal * 4 * (size_t)s->AM                    /* angular factors */
+             + sizeof(double) * NRED * t;                   /* reduction */
+    *smem = (b + 15) / 16 * 16;
 }
 
 static int launch_apply(gade_solver *s, const double2 *x, int mode, VecP V, int redkind, cudaStream_t st)
