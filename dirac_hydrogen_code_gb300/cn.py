@@ -1,5 +1,6 @@
 """Python host mirror of the reference time loop (tools/dirac_solver.c:496-636)
-running every step on the GPU through the C ABI.
+running every step on the GPU through the C ABI; ``run_batch`` advances many
+pulses together on one GPU.
 
 ``run()`` has the semantics of ``dirac_solver -t maxtime -l lmax -i E0
 -o omega -c cycles -n Ntime``: dt = maxtime/Ntime, the loop runs
@@ -84,3 +85,45 @@ def run(workdir: str, maxtime: float, lmax: int, E0: float, omega: float, cycles
                 for i in range(int(ntime)):
                     f.write("%d, %e, %d\n" % (itersarr[i], tolsarr[i], timearr[i]))
     return solver.get_x(), recs, solver
+
+
+def run_batch(problem: Problem, pulses: list[dict], tables: np.ndarray | None = None, tol: float = 1e-16,
+              maxit: int = 500, device: int = 0, max_steps: int | None = None, callback=None, **batch_kw):
+    """The reference time loop for many pulses at once on one GPU.
+
+    ``pulses``: dicts with E0, omega, cycles, ntime and optionally maxtime
+    (default cycles*2*pi/omega), i.e. one ``dirac_solver -t maxtime -i E0 -o
+    omega -c cycles -n ntime`` run each.  ``tables``: per-pulse radial tables
+    [npulse, 6, lmax, 4, blk_nnz] (``gen.pulse_tables``) or None when every
+    pulse has the Omega and Cycles the problem files were made with.  Each
+    pulse keeps its own float-accumulated time grid (Ntime or Ntime+1 steps);
+    a pulse whose grid has ended leaves the batch.  Returns (xs, records,
+    batch): final states (permuted order) and per-pulse step records."""
+    from .native import Batch
+    grids = []
+    for p in pulses:
+        maxtime = p.get("maxtime", p["cycles"] * 2 * math.pi / p["omega"])
+        grids.append(step_times(maxtime, p["ntime"]))
+    dts = [g[0] for g in grids]
+    batch = Batch(problem, dts, tables, device=device, **batch_kw)
+    nsteps = [len(g[1]) for g in grids]
+    total = max(nsteps)
+    if max_steps is not None:
+        total = min(total, max_steps)
+    recs = [[] for _ in pulses]
+    ft = np.zeros((len(pulses), 6), np.complex128)
+    for j in range(total):
+        active = np.array([j < n for n in nsteps], np.int32)
+        for k, p in enumerate(pulses):
+            if active[k]:
+                ft[k] = pulse(p["E0"], p["omega"], p["cycles"], grids[k][1][j][1])
+        stats = batch.step(ft, active, maxit=maxit, tol=tol)
+        for k in range(len(pulses)):
+            if active[k]:
+                it, t = grids[k][1][j]
+                stats[k].update(iter=it, time=t)
+                recs[k].append(stats[k])
+        if callback is not None:
+            callback(j, batch)
+    xs = [batch.get_x(k) for k in range(len(pulses))]
+    return xs, recs, batch

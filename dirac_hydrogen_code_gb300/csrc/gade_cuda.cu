@@ -132,11 +132,19 @@ struct DevScal {
     unsigned int err;      /* bit 0: a bounded mbarrier wait timed out */
     unsigned int pad0;
     double snorm;          /* x^H S x (mixed precision conservation check) */
-    double pad[2];
+    /* device-side iteration control (batched pulses; ctl = 1): the reduction
+       epilogues advance state / iter exactly as the host loop of the single
+       solver does, and every predicated kernel of a pulse whose state is not
+       the one it waits for returns at entry */
+    double tol2rel;        /* tol^2: converged when rr < tol2rel * rhs_sqnorm */
+    int ctl, state, iter, maxit, restarts, pad1;
 };
 
-enum { RED_RHS = 0, RED_RESTART, RED_R0V, RED_TS, RED_UPDATE, RED_NONE, RED_DOT_OUT, RED_QB, RED_RES, RED_SNORM, RED_MIX };
-enum { AX_PLAIN = 0, AX_PARTS, AX_R0V, AX_TS, AX_RHS, AX_RESTART, AX_QB, AX_RES, AX_MIX };
+enum { ST_RUN = 0, ST_DONE, ST_ZERO, ST_RESTART, ST_BAD };
+enum { PRED_NONE = 0, PRED_RUN, PRED_RESTART };
+
+enum { RED_RHS = 0, RED_RESTART, RED_R0V, RED_TS, RED_UPDATE, RED_NONE, RED_DOT_OUT, RED_MIX };
+enum { AX_PLAIN = 0, AX_PARTS, AX_R0V, AX_TS, AX_RHS, AX_RESTART, AX_MIX };
 enum { PC_PLAIN = 0, PC_P, PC_S };
 
 #define NRED 4   /* values per partial: up to 4 doubles */
@@ -149,8 +157,12 @@ struct OpP {
     const int *row_kidx, *act_ptr, *act_l, *ang_ptr, *ang_c;
     const void *ang_a0, *ang_a0k, *ang_a1, *ang_a1k;
     const int *chunk_nrows, *chunk_ncols, *chunk_rows, *chunk_cols, *chunk_lcol;
-    const void *M;             /* [lmax][nk][W][B] */
-    const void *S_ell, *Hst_ell, *D_ell;
+    const void *M;             /* [pulse][lmax][nk][W][B] */
+    const void *S_ell;         /* [nk][W][B], shared by all pulses */
+    const void *Hst_ell, *D_ell;   /* [pulse][nk][W][B] (depend on dt) */
+    const int *plist;          /* grid x -> pulse (NULL: pulse 0) */
+    long long vstride;         /* complex elements per pulse of every vector */
+    size_t mstride, dstride;   /* elements per pulse of M and of Hst / D */
 };
 
 struct VecP {
@@ -159,12 +171,26 @@ struct VecP {
 };
 
 struct RedP {
-    double *part;                  /* [nCTA][NRED] */
-    unsigned int *ticket;
-    DevScal *sc;
+    double *part;                  /* [pulse][nCTA][NRED] */
+    unsigned int *ticket;          /* [pulse] */
+    DevScal *sc;                   /* [pulse] */
     int kind;
     double *out;                   /* RED_DOT_OUT: receives (re, im) of the dot */
+    size_t pstride;                /* partials per pulse */
+    int pred;                      /* PRED_*: which pulse state the launch works on */
 };
+
+/* Move the reduction targets to pulse `pulse`; false when the pulse's state
+   says this launch has nothing to do (uniform over the CTA). */
+__device__ __forceinline__ bool red_select(RedP &red, int pulse)
+{
+    red.sc += pulse;
+    red.ticket += pulse;
+    red.part += (size_t)pulse * red.pstride;
+    if (red.pred == PRED_NONE) return true;
+    const int st = *(volatile const int *)&red.sc->state;
+    return red.pred == PRED_RUN ? st == ST_RUN : st == ST_RESTART;
+}
 
 /* Block-wide deterministic sum of NV doubles; result valid in thread 0. */
 template <int NV>
@@ -183,13 +209,12 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double *sh)
     __syncthreads();
 }
 
-/* Per-CTA partials + last-CTA finalisation (fixed summation order). */
-__device__ void reduce_finish(RedP red, double (&v)[NRED], double *sh)
+/* Per-CTA partials + last-CTA finalisation (fixed summation order).
+   ncta / cta: the CTAs of one pulse and this CTA's index among them. */
+__device__ void reduce_finish(RedP red, double (&v)[NRED], double *sh, unsigned ncta, unsigned cta)
 {
     __shared__ bool am_last;
     const int tid = threadIdx.x, nt = blockDim.x;
-    const unsigned ncta = gridDim.x * gridDim.y;
-    const unsigned cta = blockIdx.y * gridDim.x + blockIdx.x;
     block_sum<NRED>(v, sh);
     if (tid == 0) {
         for (int k = 0; k < NRED; k++) red.part[(size_t)cta * NRED + k] = v[k];
@@ -215,11 +240,21 @@ __device__ void reduce_finish(RedP red, double (&v)[NRED], double *sh)
             sc->rho_prev = make_double2(1.0, 0.0);
             sc->alpha = make_double2(1.0, 0.0);
             sc->w = make_double2(1.0, 0.0);
+            if (sc->ctl) {
+                /* the early exits of the host loop (tools/bicgstab.c:176-189) */
+                sc->iter = 0;
+                sc->restarts = 0;
+                if (!isfinite(acc[0]) || !isfinite(acc[1])) sc->state = ST_BAD;
+                else if (acc[1] == 0.0) sc->state = ST_ZERO;
+                else if (acc[0] < sc->tol2rel * acc[1] || sc->maxit <= 0) sc->state = ST_DONE;
+                else sc->state = ST_RUN;
+            }
             break;
         case RED_RESTART:
             sc->r0_sqnorm = acc[0];
             sc->rr = acc[0];
             sc->rho = make_double2(acc[0], 0.0);
+            if (sc->ctl) { sc->restarts++; sc->state = ST_RUN; }
             break;
         case RED_R0V:
             sc->r0v = make_double2(acc[0], acc[1]);
@@ -234,20 +269,18 @@ __device__ void reduce_finish(RedP red, double (&v)[NRED], double *sh)
             sc->rr = acc[0];
             sc->rho_prev = sc->rho;
             sc->rho = make_double2(acc[1], acc[2]);
+            if (sc->ctl) {
+                /* convergence, iteration limit, then the restart test that
+                   opens the next iteration (tools/bicgstab.c:205-212,287-293) */
+                if (!isfinite(acc[0])) sc->state = ST_BAD;
+                else if (acc[0] < sc->tol2rel * sc->rhs_sqnorm) sc->state = ST_DONE;
+                else if (++sc->iter >= sc->maxit) sc->state = ST_DONE;
+                else if (fabs(acc[1]) < (1e-12 * 1e-12) * sc->r0_sqnorm) sc->state = ST_RESTART;
+            }
             break;
         case RED_DOT_OUT:
             red.out[0] = acc[0];
             red.out[1] = acc[1];
-            break;
-        case RED_QB:
-            sc->rhs_sqnorm = acc[0];
-            sc->snorm = acc[1];
-            break;
-        case RED_RES:
-            sc->rr = acc[0];
-            break;
-        case RED_SNORM:
-            sc->snorm = acc[0];
             break;
         case RED_MIX:
             sc->rhs_sqnorm = acc[0];
@@ -265,8 +298,10 @@ __device__ void reduce_finish(RedP red, double (&v)[NRED], double *sh)
 struct TabP {
     int lmax, nk, W, B, blk_nnz;
     const int *kvals, *ell_pos;
-    const void *g, *gt;           /* [lmax][3][4][blk_nnz] (a in the l-parity set) */
-    void *M;                      /* [lmax][nk][W][B] */
+    const void *g, *gt;           /* [pulse][lmax][3][4][blk_nnz] (a in the l-parity set) */
+    void *M;                      /* [pulse][lmax][nk][W][B] */
+    const int *plist;             /* grid y -> pulse (NULL: pulse 0) */
+    size_t gstride, mstride;      /* elements per pulse of g / gt and of M */
 };
 
 /* coef[l*3 + ia]: SoL * i h dt/2 * f_a for a = (l%2+1)%2 + 2 ia.
@@ -278,6 +313,19 @@ __global__ void k_tables(TabP T, const double2 *__restrict__ coef)
     const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     const long long per_l = (long long)T.W * T.B;
     if (tid >= per_l * T.lmax) return;
+    {
+        const int pulse = T.plist ? T.plist[blockIdx.y] : 0;
+        coef += (size_t)pulse * T.lmax * 3;
+        if (RC) {
+            T.g = (const double *)T.g + (size_t)pulse * T.gstride;
+            T.gt = (const double *)T.gt + (size_t)pulse * T.gstride;
+            T.M = (typename R4<R>::T *)T.M + (size_t)pulse * T.mstride;
+        } else {
+            T.g = (const double2 *)T.g + (size_t)pulse * T.gstride;
+            T.gt = (const double2 *)T.gt + (size_t)pulse * T.gstride;
+            T.M = (C4<C> *)T.M + (size_t)pulse * T.mstride;
+        }
+    }
     const int l = (int)(tid / per_l);
     const int slot = (int)(tid % per_l);      /* j*B + i */
     const int k = T.ell_pos[slot];
@@ -354,7 +402,24 @@ __global__ void __launch_bounds__(256) k_apply(OpP P, const typename Cx<R>::T *_
     A *ang = (A *)(angc + ((P.AM + 3) & ~3)); /* [4][AM] a0, a0 k_c, a1, a1 k_c (16-byte aligned) */
     double *shred = (double *)(ang + 4 * P.AM); /* [NRED * blockDim] */
 
-    const int q = blockIdx.x, r = blockIdx.y, tid = threadIdx.x, nt = blockDim.x;
+    /* grid (pulse slot, chunk, block row): the slots of one chunk run side by
+       side, so the shared maps and angular tables come from L2 for all but one */
+    const int pulse = P.plist ? P.plist[blockIdx.x] : 0;
+    if (!red_select(red, pulse)) return;
+    {
+        const long long vo = (long long)pulse * P.vstride;
+        x += vo;
+        if (V.out0) V.out0 = (C *)V.out0 + vo;
+        if (V.out1) V.out1 = (C *)V.out1 + vo;
+        if (V.out2) V.out2 = (C *)V.out2 + vo;
+        if (V.in0) V.in0 = (const C *)V.in0 + vo;
+        if (V.in1) V.in1 = (const C *)V.in1 + vo;
+        if (RC) P.M = (const typename R4<R>::T *)P.M + (size_t)pulse * P.mstride;
+        else P.M = (const C4<C> *)P.M + (size_t)pulse * P.mstride;
+        P.Hst_ell = (const C *)P.Hst_ell + (size_t)pulse * P.dstride;
+        P.D_ell = (const C *)P.D_ell + (size_t)pulse * P.dstride;
+    }
+    const int q = blockIdx.y, r = blockIdx.z, tid = threadIdx.x, nt = blockDim.x;
     const int B = P.B, W = P.W, CM = P.CM;
     const int kk = P.row_kidx[r];
     const int nrows = P.chunk_nrows[q], ncols = P.chunk_ncols[q];
@@ -378,7 +443,7 @@ __global__ void __launch_bounds__(256) k_apply(OpP P, const typename Cx<R>::T *_
         ang[3 * P.AM + e] = ((const A *)P.ang_a1k)[ea + e];
     }
     /* rhs/parts modes need S x and H x apart; A x modes use D = S + i h dt/2 h0 */
-    const bool separate = (mode == AX_RHS || mode == AX_PARTS || mode == AX_QB);
+    const bool separate = (mode == AX_RHS || mode == AX_PARTS);
 
     for (int c = tid; c < ncols; c += nt) xr[c] = xb[cols[c]];
     if (mode == AX_MIX) {
@@ -531,22 +596,6 @@ __global__ void __launch_bounds__(256) k_apply(OpP P, const typename Cx<R>::T *_
             v[1] = (double)rhs.x * rhs.x + (double)rhs.y * rhs.y;
             break;
         }
-        case AX_QB: {           /* q = -2 H x ; |S x - H x|^2 ; x^H S x  (mixed precision) */
-            const C qv = mk<C>(-2.0 * accH.x, -2.0 * accH.y);
-            ((C *)V.out0)[gi] = qv;
-            const C b = csub(accS, accH);
-            v[0] = (double)b.x * b.x + (double)b.y * b.y;
-            const C xi = x[gi];
-            v[1] = (double)xi.x * accS.x + (double)xi.y * accS.y;
-            break;
-        }
-        case AX_RES: {          /* r = q - A d ; |r|^2  (mixed precision) */
-            const C qv = ((const C *)V.in0)[gi];
-            const C rv = csub(qv, ax);
-            ((C *)V.out0)[gi] = rv;
-            v[0] = (double)rv.x * rv.x + (double)rv.y * rv.y;
-            break;
-        }
         case AX_MIX: {          /* r = -S delta - H w ; b = S x_n - H w / 2 ; x_n^H S x_n */
             const C rv = mk<C>(-accD.x - accH.x, -accD.y - accH.y);
             ((C *)V.out0)[gi] = rv;
@@ -567,7 +616,7 @@ __global__ void __launch_bounds__(256) k_apply(OpP P, const typename Cx<R>::T *_
         }
         }
     }
-    if (red.kind != RED_NONE) reduce_finish(red, v, shred);
+    if (red.kind != RED_NONE) reduce_finish(red, v, shred, gridDim.y * gridDim.z, blockIdx.z * gridDim.y + blockIdx.y);
 }
 
 /* ------------------------------------------------------------------ */
@@ -583,7 +632,11 @@ __global__ void __launch_bounds__(256) k_apply(OpP P, const typename Cx<R>::T *_
 struct PcT {
     int nblk, B, Bp, nch;
     const int *row_kidx, *ord;
-    const void *FL, *FU;           /* [nk][nch][CH] complex of the kernel's precision */
+    const void *FL, *FU;           /* [pulse][nk][nch][CH] complex of the kernel's precision */
+    const int *plist;              /* grid x -> pulse (NULL: pulse 0) */
+    long long vstride;             /* complex elements per pulse of every vector */
+    size_t fstride;                /* complex elements per pulse of FL / FU */
+    int pred;                      /* PRED_* */
 };
 
 __device__ __forceinline__ unsigned smem_u32(const void *p)
@@ -641,13 +694,26 @@ __global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const type
     __shared__ __align__(8) uint64_t bar[2];
     __shared__ int all_ok;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    const int r = blockIdx.x;
+    const int r = blockIdx.y;
     if (r >= Q.nblk) return;
+    const int pulse = Q.plist ? Q.plist[blockIdx.x] : 0;
+    sc += pulse;
+    if (Q.pred != PRED_NONE) {
+        const int st = *(volatile const int *)&sc->state;
+        if (Q.pred == PRED_RUN ? st != ST_RUN : st != ST_RESTART) return;
+    }
+    {
+        const long long vo = (long long)pulse * Q.vstride;
+        in0 += vo;
+        if (in1) in1 += vo;
+        if (io) io += vo;
+        out += vo;
+    }
     const int B = Q.B, Bp = Q.Bp, nch = Q.nch;
     const int kk = Q.row_kidx[r];
     const size_t off = (size_t)r * B;
-    const C *FL = (const C *)Q.FL + (size_t)kk * nch * CH;
-    const C *FU = (const C *)Q.FU + (size_t)kk * nch * CH;
+    const C *FL = (const C *)Q.FL + (size_t)pulse * Q.fstride + (size_t)kk * nch * CH;
+    const C *FU = (const C *)Q.FU + (size_t)pulse * Q.fstride + (size_t)kk * nch * CH;
     const unsigned bytes = CH * sizeof(C);
 
     if (tid == 0) {
@@ -762,15 +828,23 @@ __global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const type
 /* ------------------------------------------------------------------ */
 /* x += alpha y + w z ; r = s - w t ; |r|^2, <r0, r>                    */
 /* ------------------------------------------------------------------ */
+/* grid (CTAs per pulse, pulse slot); plist maps the slot to the pulse and
+   n is also the per-pulse vector stride */
 template <typename R>
 __global__ void k_update(long long n, typename Cx<R>::T *x, const typename Cx<R>::T *__restrict__ y,
                          const typename Cx<R>::T *__restrict__ z, typename Cx<R>::T *r,
                          const typename Cx<R>::T *__restrict__ s, const typename Cx<R>::T *__restrict__ t,
-                         const typename Cx<R>::T *__restrict__ r0, RedP red)
+                         const typename Cx<R>::T *__restrict__ r0, RedP red, const int *plist)
 {
     typedef typename Cx<R>::T C;
     extern __shared__ unsigned char smem_raw[];
     double *shred = (double *)smem_raw;
+    const int pulse = plist ? plist[blockIdx.y] : 0;
+    if (!red_select(red, pulse)) return;
+    {
+        const long long vo = (long long)pulse * n;
+        x += vo; y += vo; z += vo; r += vo; s += vo; t += vo; r0 += vo;
+    }
     const double2 al = red.sc->alpha, w = red.sc->w;
     const C a = mk<C>(al.x, al.y), wc = mk<C>(w.x, w.y), nw = mk<C>(-w.x, -w.y);
     double v[NRED] = {0, 0, 0, 0};
@@ -787,7 +861,7 @@ __global__ void k_update(long long n, typename Cx<R>::T *x, const typename Cx<R>
         v[1] += (double)q.x * rv.x + (double)q.y * rv.y;
         v[2] += (double)q.x * rv.y - (double)q.y * rv.x;
     }
-    reduce_finish(red, v, shred);
+    reduce_finish(red, v, shred, gridDim.x, blockIdx.x);
 }
 
 /* ------------------------------------------------------------------ */
@@ -824,7 +898,7 @@ __global__ void k_inner_init(long long n, const double2 *__restrict__ rin, float
         acc[0] += (double)rv.x * rv.x + (double)rv.y * rv.y;
     }
     acc[1] = acc[0];
-    reduce_finish(red, acc, shred);
+    reduce_finish(red, acc, shred, gridDim.x, blockIdx.x);
 }
 
 /* delta += e (FP64), refresh the FP32 copy and w = 2 x_n + delta */
@@ -853,28 +927,6 @@ __global__ void k_mixed_finish(long long n, double2 *__restrict__ x, double2 *__
     }
 }
 
-/* x^H S x in FP64 over the block-diagonal overlap (norm-conservation check) */
-__global__ void k_snorm(int B, int W, const int *__restrict__ row_kidx, const int *__restrict__ ell_col,
-                        const double2 *__restrict__ S_ell, const double2 *__restrict__ x, RedP red)
-{
-    extern __shared__ unsigned char smem_raw[];
-    double *shred = (double *)smem_raw;
-    const int r = blockIdx.y, i = blockIdx.x * blockDim.x + threadIdx.x;
-    double acc[NRED] = {0, 0, 0, 0};
-    if (i < B) {
-        const int kk = row_kidx[r];
-        const double2 *xb = x + (size_t)r * B;
-        double2 sx = make_double2(0, 0);
-        for (int j = 0; j < W; j++) {
-            const int col = ell_col[(size_t)j * B + i];
-            if (col >= 0) cfma(sx, S_ell[((size_t)kk * W + j) * B + i], xb[col]);
-        }
-        const double2 xi = xb[i];
-        acc[0] = xi.x * sx.x + xi.y * sx.y;
-    }
-    reduce_finish(red, acc, shred);
-}
-
 /* ------------------------------------------------------------------ */
 /* solver object                                                       */
 /* ------------------------------------------------------------------ */
@@ -882,10 +934,16 @@ struct gade_solver {
     int device;
     cudaStream_t stream;
     int prec, rc;
-    long long n;
+    long long n;                /* unknowns of one pulse (also the per-pulse vector stride) */
     int nblk, B, lmax, W, nk, RM, CM, nchunk, AM;
     int bw, Bp, nch;
-    double dt, h;
+    double dt, h;               /* dt of pulse 0 */
+    /* pulses: every per-pulse array holds npulse slices; kernels run over
+       the nslot pulses listed in d_plist (NULL: pulse 0 alone) */
+    int npulse, nslot, cs;
+    int *d_plist;
+    size_t mstride, dstride, fstride, gstride, pstride;
+    std::vector<double> dts;
     /* operator tables */
     int *d_row_kidx, *d_act_ptr, *d_act_l, *d_ang_ptr, *d_ang_c;
     void *d_ang_a0, *d_ang_a0k, *d_ang_a1, *d_ang_a1k;
@@ -896,13 +954,13 @@ struct gade_solver {
     int blk_nnz;
     /* preconditioner */
     int *d_ord;
-    void *d_Lb, *d_Ub, *d_Linv, *d_Uinv;
     double2 *d_FL, *d_FU;       /* chunk-packed factors for the TMA kernel */
     int bwp;
     /* vectors */
     double2 *x, *rhs, *r, *r0, *p, *v, *y, *z, *s, *t, *tmp0, *tmp1;
     /* reductions */
     double *d_part;
+    size_t part_cap;            /* doubles allocated in d_part */
     unsigned int *d_ticket;
     DevScal *d_sc, *h_sc;
     double2 *d_coef, *h_coef;
@@ -925,7 +983,6 @@ struct gade_solver {
     float2 *x32, *d32, *q32, *r32, *e32, *ri32, *r032, *p32, *v32, *y32, *z32, *s32, *t32;
     double2 *xprev, *delta64;
     DevScal *d_sc2, *h_sc2;
-    int *d_ell_col;
     int have_prev;
 };
 
@@ -976,6 +1033,14 @@ static int dev_upload(gade_solver *s, T **d, const T *h, size_t count)
     else CK(cudaMemset(p, 0, bytes));
     *d = (T *)p;
     return GADE_OK;
+}
+
+/* frees one allocation made by dev_upload (used when re-chunking) */
+static void dev_release(gade_solver *s, void *p)
+{
+    if (!p) return;
+    for (size_t k = 0; k < s->allocs.size(); k++)
+        if (s->allocs[k] == p) { cudaFree(p); s->allocs.erase(s->allocs.begin() + k); return; }
 }
 
 #define UP(dst, src, cnt) do { int rc_ = dev_upload(s, &(dst), (src), (size_t)(cnt)); if (rc_) { gade_solver_free(s); return rc_; } } while (0)
@@ -1042,31 +1107,123 @@ static int choose_chunk_splines(int nblk, int B, int nsm)
     return cs;
 }
 
-extern "C" int gade_solver_create(const gade_problem *p, double dt, double h, int32_t precision,
-                                  int32_t device, gade_solver **out)
+/* row-chunk layout of the operator kernel (pattern only: shared by all
+   pulses); replaces an earlier layout */
+static int set_chunking(gade_solver *s, const gade_setup *su)
 {
-    if (!p || !out) return fail(GADE_ERR_ARG, "gade_solver_create: NULL argument");
+    if (su->chunk_rows_max > 128 || su->chunk_cols_max > 256)
+        return fail(GADE_ERR_ARG, "row chunk too large for the operator kernel (rows %d, columns %d)",
+                    su->chunk_rows_max, su->chunk_cols_max);
+    int *old[5] = {s->d_chunk_nrows, s->d_chunk_ncols, s->d_chunk_rows, s->d_chunk_cols, s->d_chunk_lcol};
+    for (int *p : old) dev_release(s, p);
+    s->RM = su->chunk_rows_max; s->CM = su->chunk_cols_max; s->nchunk = su->nchunk;
+    int rc;
+    if ((rc = dev_upload(s, &s->d_chunk_nrows, su->chunk_nrows, s->nchunk))) return rc;
+    if ((rc = dev_upload(s, &s->d_chunk_ncols, su->chunk_ncols, s->nchunk))) return rc;
+    if ((rc = dev_upload(s, &s->d_chunk_rows, su->chunk_rows, (size_t)s->nchunk * s->RM))) return rc;
+    if ((rc = dev_upload(s, &s->d_chunk_cols, su->chunk_cols, (size_t)s->nchunk * s->CM))) return rc;
+    if ((rc = dev_upload(s, &s->d_chunk_lcol, su->chunk_lcol, (size_t)s->nchunk * s->W * s->RM))) return rc;
+    /* reduction partials: one slot per CTA of a pulse */
+    size_t max_cta = (size_t)s->nchunk * s->nblk;
+    if ((size_t)s->upd_grid > max_cta) max_cta = s->upd_grid;
+    s->pstride = max_cta * NRED;
+    if (s->pstride * s->npulse > s->part_cap) {
+        dev_release(s, s->d_part);
+        s->d_part = nullptr;
+        if ((rc = dev_upload(s, &s->d_part, (const double *)nullptr, s->pstride * s->npulse))) return rc;
+        s->part_cap = s->pstride * s->npulse;
+    }
+    s->cs = su->chunk_splines;
+    /* exact FP64 flop count of one operator apply (2 per FMA) */
+    const double fma_c = s->rc ? 2.0 : 4.0;     /* FMAs of one coupling term */
+    double fmas = 4.0 * (double)s->blk_nnz * s->nblk;             /* diagonal blocks (A x modes) */
+    double cols = 0;
+    for (int q = 0; q < s->nchunk; q++) cols += su->chunk_ncols[q];
+    for (int r = 0; r < s->nblk; r++)
+        for (int a = su->act_ptr[r]; a < su->act_ptr[r + 1]; a++) {
+            int l = su->act_l[a];
+            double ne = su->ang_ptr[r * s->lmax + l + 1] - su->ang_ptr[r * s->lmax + l];
+            fmas += 4.0 * fma_c * ne * cols;                       /* gather u, w, u', w' */
+            fmas += 4.0 * fma_c * (double)s->blk_nnz;              /* radial tables */
+        }
+    s->apply_flops = 2.0 * fmas;
+    return GADE_OK;
+}
+
+/* chunk-packed block-LU factors of one pulse: [nk][nch][Linv | masked band] */
+static void pack_factors(const gade_setup *su, int nk, int nch, int bw, int bwp, int B, int Bp,
+                         double2 *FL, double2 *FU)
+{
+    const int CH = 1024 + 32 * bwp;
+    for (int kk = 0; kk < nk; kk++)
+        for (int c = 0; c < nch; c++) {
+            double2 *fl = FL + ((size_t)kk * nch + c) * CH;
+            double2 *fu = FU + ((size_t)kk * nch + c) * CH;
+            memcpy(fl, su->Linv + ((size_t)kk * nch + c) * 1024, 1024 * sizeof(double2));
+            memcpy(fu, su->Uinv + ((size_t)kk * nch + c) * 1024, 1024 * sizeof(double2));
+            for (int d = 1; d <= bwp; d++)
+                for (int lane = 0; lane < 32; lane++) {
+                    int o = 32 * c + lane;
+                    double2 lv = make_double2(0, 0), uv = make_double2(0, 0);
+                    if (d <= bw && o - d >= 0 && o - d < 32 * c) {
+                        gc64 v = su->Lb[((size_t)kk * bw + d - 1) * Bp + o];
+                        lv = make_double2(v.re, v.im);
+                    }
+                    if (d <= bw && o + d < B && o + d >= 32 * (c + 1)) {
+                        gc64 v = su->Ub[((size_t)kk * bw + d - 1) * Bp + o];
+                        uv = make_double2(v.re, v.im);
+                    }
+                    fl[1024 + (d - 1) * 32 + lane] = lv;
+                    fu[1024 + (d - 1) * 32 + lane] = uv;
+                }
+        }
+}
+
+/*
+ * Shared by gade_solver_create (one pulse) and gade_batch_create (npulse
+ * pulses on one set of angular tables, h0 and S).  Pulse k has its own time
+ * step dts[k], radial tables (gext slice k, or the problem's own when gext is
+ * NULL) and therefore its own D = S + i h dt/2 h0 and block-LU factors.
+ */
+static int solver_create(const gade_problem *p, int npulse, const double *dts, const double *gext, double h,
+                         int32_t precision, int32_t device, int cs_req, gade_solver **out)
+{
+    if (!p || !out || !dts) return fail(GADE_ERR_ARG, "solver create: NULL argument");
     *out = nullptr;
     if (precision != GADE_PREC_FP64 && precision != GADE_PREC_MIXED)
-        return fail(GADE_ERR_ARG, "gade_solver_create: unknown precision %d", precision);
-    if (!(dt > 0) || !std::isfinite(dt)) return fail(GADE_ERR_ARG, "gade_solver_create: dt must be finite and > 0");
+        return fail(GADE_ERR_ARG, "unknown precision %d", precision);
+    if (npulse < 1) return fail(GADE_ERR_ARG, "at least one pulse is needed");
+    for (int k = 0; k < npulse; k++)
+        if (!(dts[k] > 0) || !std::isfinite(dts[k])) return fail(GADE_ERR_ARG, "dt of pulse %d must be finite and > 0", k);
     int ndev = 0;
     CK(cudaGetDeviceCount(&ndev));
-    if (device < 0 || device >= ndev) return fail(GADE_ERR_ARG, "gade_solver_create: no CUDA device %d", device);
+    if (device < 0 || device >= ndev) return fail(GADE_ERR_ARG, "no CUDA device %d", device);
     CK(cudaSetDevice(device));
     cudaDeviceProp prop;
     CK(cudaGetDeviceProperties(&prop, device));
 
+    const size_t bn = (size_t)p->blk_nnz;
+    std::vector<int32_t> tpos;
+    if (gext) {
+        /* external radial tables: same class (real or complex) as the problem's,
+           transposed on the shared pattern like the loader does */
+        tpos.resize(bn);
+        if (gade_problem_transpose_map(p, tpos.data()))
+            return fail(GADE_ERR_FORMAT, "base pattern is not structurally symmetric");
+        if (p->real_coupling) {
+            const size_t cnt = (size_t)npulse * 6 * p->lmax * 4 * bn;
+            for (size_t e = 0; e < cnt; e++)
+                if (gext[2 * e + 1] != 0.0 || !std::isfinite(gext[2 * e]))
+                    return fail(GADE_ERR_ARG, "radial tables of pulse %zu must be real and finite like the problem's",
+                                e / ((size_t)6 * p->lmax * 4 * bn));
+        }
+    }
+
     char err[1024] = {0};
     gade_setup *su = nullptr;
-    int cs = choose_chunk_splines(p->nblk, p->blkdim, prop.multiProcessorCount);
-    int rcode = gade_setup_build(p, dt, h, cs, &su, err, sizeof(err));
+    int cs = cs_req > 0 ? cs_req : choose_chunk_splines(p->nblk, p->blkdim, prop.multiProcessorCount);
+    int rcode = gade_setup_build(p, dts[0], h, cs, &su, err, sizeof(err));
     if (rcode) return fail(rcode, "%s", err);
-    if (su->chunk_rows_max > 128 || su->chunk_cols_max > 256) {
-        gade_setup_release(su);
-        return fail(GADE_ERR_ARG, "row chunk too large for the operator kernel (rows %d, columns %d)",
-                    su->chunk_rows_max, su->chunk_cols_max);
-    }
     {
         /* operator kernels may use more than the default 48 KB of dynamic shared memory */
         const int lim = 160 * 1024;
@@ -1081,19 +1238,44 @@ extern "C" int gade_solver_create(const gade_problem *p, double dt, double h, in
     s->prec = precision;
     s->rc = p->real_coupling;
     s->n = p->n; s->nblk = p->nblk; s->B = p->blkdim; s->lmax = p->lmax;
-    s->W = su->W; s->nk = su->nk; s->RM = su->chunk_rows_max; s->CM = su->chunk_cols_max;
+    s->W = su->W; s->nk = su->nk;
+    s->npulse = npulse; s->nslot = 1;
+    s->dts.assign(dts, dts + npulse);
     s->AM = 1;
     for (int r = 0; r < p->nblk; r++) {
         int na = su->ang_ptr[(size_t)(r + 1) * p->lmax] - su->ang_ptr[(size_t)r * p->lmax];
         if (na > s->AM) s->AM = na;
     }
-    s->nchunk = su->nchunk; s->bw = su->bw; s->Bp = su->Bp; s->nch = su->nch;
-    s->dt = dt; s->h = h; s->blk_nnz = p->blk_nnz;
+    s->bw = su->bw; s->Bp = su->Bp; s->nch = su->nch;
+    s->dt = dts[0]; s->h = h; s->blk_nnz = p->blk_nnz;
+    s->upd_block = 256;
+    {
+        /* vector kernels: at most two CTAs per SM, no more than one thread per element */
+        long long need = (s->n + s->upd_block - 1) / s->upd_block;
+        s->upd_grid = 2 * prop.multiProcessorCount;
+        if (need < s->upd_grid) s->upd_grid = (int)(need > 0 ? need : 1);
+    }
     if (cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) != cudaSuccess) {
         gade_setup_release(su); delete s; return fail(GADE_ERR_CUDA, "stream creation failed");
     }
+#undef UP
+#define UP(dst, src, cnt) do { int rc_ = dev_upload(s, &(dst), (src), (size_t)(cnt)); if (rc_) { gade_setup_release(su); gade_solver_free(s); return rc_; } } while (0)
     const size_t WB = (size_t)s->W * s->B;
+    const size_t NP = (size_t)npulse;
+    s->mstride = (size_t)s->lmax * s->nk * WB;
+    s->dstride = (size_t)s->nk * WB;
+    s->gstride = (size_t)s->lmax * 3 * 4 * bn;
+    s->bwp = s->bw <= 16 ? 16 : 32;
+    if (s->bw > 32) { gade_setup_release(su); gade_solver_free(s); return fail(GADE_ERR_ARG, "preconditioner band %d wider than 32 is not supported", s->bw); }
+    const int CH = 1024 + 32 * s->bwp;
+    s->fstride = (size_t)s->nk * s->nch * CH;
 
+    if (npulse > 1) {
+        std::vector<int> ident(npulse);
+        for (int k = 0; k < npulse; k++) ident[k] = k;
+        UP(s->d_plist, ident.data(), npulse);
+        s->nslot = npulse;
+    }
     UP(s->d_row_kidx, su->row_kidx, s->nblk);
     UP(s->d_act_ptr, su->act_ptr, s->nblk + 1);
     UP(s->d_act_l, su->act_l, su->n_act);
@@ -1112,201 +1294,186 @@ extern "C" int gade_solver_create(const gade_problem *p, double dt, double h, in
             }
         }
     }
-    UP(s->d_chunk_nrows, su->chunk_nrows, s->nchunk);
-    UP(s->d_chunk_ncols, su->chunk_ncols, s->nchunk);
-    UP(s->d_chunk_rows, su->chunk_rows, (size_t)s->nchunk * s->RM);
-    UP(s->d_chunk_cols, su->chunk_cols, (size_t)s->nchunk * s->CM);
-    UP(s->d_chunk_lcol, su->chunk_lcol, (size_t)s->nchunk * s->W * s->RM);
     {
-        double2 *d;
-        UP(d, (const double2 *)su->S_ell, (size_t)s->nk * WB); s->d_S_ell = d;
-        UP(d, (const double2 *)su->Hst_ell, (size_t)s->nk * WB); s->d_Hst_ell = d;
-        std::vector<double2> D((size_t)s->nk * WB);
-        for (size_t e = 0; e < D.size(); e++)
-            D[e] = make_double2(su->S_ell[e].re + su->Hst_ell[e].re, su->S_ell[e].im + su->Hst_ell[e].im);
-        UP(d, D.data(), D.size()); s->d_D_ell = d;
+        int rc = set_chunking(s, su);
+        if (rc) { gade_setup_release(su); gade_solver_free(s); return rc; }
     }
     UP(s->d_kvals, su->kvals, s->nk);
     UP(s->d_ell_pos, su->ell_pos, WB);
-    {
-        /* radial tables of the three pulse components used by each l */
-        const size_t bn = (size_t)p->blk_nnz;
-        const size_t cnt = (size_t)s->lmax * 3 * 4 * bn;
-        if (s->rc) {
-            std::vector<double> g(cnt), gt(cnt);
-            for (int l = 0; l < s->lmax; l++)
-                for (int ia = 0; ia < 3; ia++) {
-                    int a = (l % 2 + 1) % 2 + 2 * ia;
-                    for (int q = 0; q < 4; q++)
-                        for (size_t k = 0; k < bn; k++) {
-                            size_t src = (((size_t)a * s->lmax + l) * 4 + q) * bn + k;
-                            size_t dst = (((size_t)l * 3 + ia) * 4 + q) * bn + k;
-                            g[dst] = p->g[src].re; gt[dst] = p->gt[src].re;
-                        }
-                }
-            double *d; UP(d, g.data(), cnt); s->d_g = d; UP(d, gt.data(), cnt); s->d_gt = d;
-        } else {
-            std::vector<double2> g(cnt), gt(cnt);
-            for (int l = 0; l < s->lmax; l++)
-                for (int ia = 0; ia < 3; ia++) {
-                    int a = (l % 2 + 1) % 2 + 2 * ia;
-                    for (int q = 0; q < 4; q++)
-                        for (size_t k = 0; k < bn; k++) {
-                            size_t src = (((size_t)a * s->lmax + l) * 4 + q) * bn + k;
-                            size_t dst = (((size_t)l * 3 + ia) * 4 + q) * bn + k;
-                            g[dst] = make_double2(p->g[src].re, p->g[src].im);
-                            gt[dst] = make_double2(p->gt[src].re, p->gt[src].im);
-                        }
-                }
-            double2 *d; UP(d, g.data(), cnt); s->d_g = d; UP(d, gt.data(), cnt); s->d_gt = d;
-        }
-        size_t mcount = (size_t)s->lmax * s->nk * WB;
-        if (s->rc) { R4d *d; UP(d, (const R4d *)nullptr, mcount); s->d_M = d; }
-        else { C4<double2> *d; UP(d, (const C4<double2> *)nullptr, mcount); s->d_M = d; }
-    }
-    /* preconditioner */
     UP(s->d_ord, su->ord, s->B);
     {
         double2 *d;
-        UP(d, (const double2 *)su->Lb, (size_t)s->nk * s->bw * s->Bp); s->d_Lb = d;
-        UP(d, (const double2 *)su->Ub, (size_t)s->nk * s->bw * s->Bp); s->d_Ub = d;
-        UP(d, (const double2 *)su->Linv, (size_t)s->nk * s->nch * 1024); s->d_Linv = d;
-        UP(d, (const double2 *)su->Uinv, (size_t)s->nk * s->nch * 1024); s->d_Uinv = d;
+        UP(d, (const double2 *)su->S_ell, (size_t)s->nk * WB); s->d_S_ell = d;
+        UP(d, (const double2 *)nullptr, NP * s->dstride); s->d_Hst_ell = d;
+        UP(d, (const double2 *)nullptr, NP * s->dstride); s->d_D_ell = d;
+        UP(s->d_FL, (const double2 *)nullptr, NP * s->fstride);
+        UP(s->d_FU, (const double2 *)nullptr, NP * s->fstride);
+        if (s->rc) { double *g; UP(g, (const double *)nullptr, NP * s->gstride); s->d_g = g; UP(g, (const double *)nullptr, NP * s->gstride); s->d_gt = g; }
+        else { double2 *g; UP(g, (const double2 *)nullptr, NP * s->gstride); s->d_g = g; UP(g, (const double2 *)nullptr, NP * s->gstride); s->d_gt = g; }
+        if (s->rc) { R4d *m; UP(m, (const R4d *)nullptr, NP * s->mstride); s->d_M = m; }
+        else { C4<double2> *m; UP(m, (const C4<double2> *)nullptr, NP * s->mstride); s->d_M = m; }
+    }
+    const bool mixed = precision == GADE_PREC_MIXED;
+    if (mixed) {
+        if (s->rc) { R4f *m; UP(m, (const R4f *)nullptr, NP * s->mstride); s->d_M32 = m; }
+        else { C4<float2> *m; UP(m, (const C4<float2> *)nullptr, NP * s->mstride); s->d_M32 = m; }
+        std::vector<float2> Sf((size_t)s->nk * WB);
+        for (size_t e = 0; e < Sf.size(); e++) Sf[e] = make_float2((float)su->S_ell[e].re, (float)su->S_ell[e].im);
+        float2 *d;
+        UP(d, Sf.data(), Sf.size()); s->d_S32 = d;
+        UP(d, (const float2 *)nullptr, NP * s->dstride); s->d_H32 = d;
+        UP(d, (const float2 *)nullptr, NP * s->dstride); s->d_D32 = d;
+        UP(d, (const float2 *)nullptr, NP * s->fstride); s->d_FL32 = d;
+        UP(d, (const float2 *)nullptr, NP * s->fstride); s->d_FU32 = d;
+        const gc64 *src[4] = {su->ang_a0, su->ang_a0k, su->ang_a1, su->ang_a1k};
+        for (int k = 0; k < 4; k++) {
+            if (s->rc) {
+                std::vector<float> v((size_t)su->n_ang + 1);
+                for (int64_t e = 0; e < su->n_ang; e++) v[e] = (float)src[k][e].im;
+                float *dd; UP(dd, v.data(), su->n_ang); s->d_a32[k] = dd;
+            } else {
+                std::vector<float2> v((size_t)su->n_ang + 1);
+                for (int64_t e = 0; e < su->n_ang; e++) v[e] = make_float2((float)src[k][e].re, (float)src[k][e].im);
+                float2 *dd; UP(dd, v.data(), su->n_ang); s->d_a32[k] = dd;
+            }
+        }
     }
     {
-        /* chunk-packed factors: [nk][nch][Linv | masked band] */
-        s->bwp = s->bw <= 16 ? 16 : 32;
-        if (s->bw > 32) { gade_setup_release(su); gade_solver_free(s); return fail(GADE_ERR_ARG, "preconditioner band %d wider than 32 is not supported", s->bw); }
-        const int CH = 1024 + 32 * s->bwp;
-        std::vector<double2> FL((size_t)s->nk * s->nch * CH), FU((size_t)s->nk * s->nch * CH);
-        for (int kk = 0; kk < s->nk; kk++)
-            for (int c = 0; c < s->nch; c++) {
-                double2 *fl = &FL[((size_t)kk * s->nch + c) * CH];
-                double2 *fu = &FU[((size_t)kk * s->nch + c) * CH];
-                memcpy(fl, su->Linv + ((size_t)kk * s->nch + c) * 1024, 1024 * sizeof(double2));
-                memcpy(fu, su->Uinv + ((size_t)kk * s->nch + c) * 1024, 1024 * sizeof(double2));
-                for (int d = 1; d <= s->bwp; d++)
-                    for (int lane = 0; lane < 32; lane++) {
-                        int o = 32 * c + lane;
-                        double2 lv = make_double2(0, 0), uv = make_double2(0, 0);
-                        if (d <= s->bw && o - d >= 0 && o - d < 32 * c) {
-                            gc64 v = su->Lb[((size_t)kk * s->bw + d - 1) * s->Bp + o];
-                            lv = make_double2(v.re, v.im);
-                        }
-                        if (d <= s->bw && o + d < s->B && o + d >= 32 * (c + 1)) {
-                            gc64 v = su->Ub[((size_t)kk * s->bw + d - 1) * s->Bp + o];
-                            uv = make_double2(v.re, v.im);
-                        }
-                        fl[1024 + (d - 1) * 32 + lane] = lv;
-                        fu[1024 + (d - 1) * 32 + lane] = uv;
-                    }
-            }
-        UP(s->d_FL, FL.data(), FL.size());
-        UP(s->d_FU, FU.data(), FU.size());
         size_t smem = sizeof(double2) * ((size_t)2 * CH + s->Bp + 256);
         if (smem > 220 * 1024) { gade_setup_release(su); gade_solver_free(s); return fail(GADE_ERR_ARG, "block dimension too large for the preconditioner"); }
         cudaFuncSetAttribute(k_precond_tma<double, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         cudaFuncSetAttribute(k_precond_tma<double, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        size_t smem32 = sizeof(float2) * ((size_t)2 * CH + s->Bp + 256);
+        cudaFuncSetAttribute(k_precond_tma<float, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem32);
+        cudaFuncSetAttribute(k_precond_tma<float, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem32);
     }
-    /* vectors */
-    double2 **vecs[] = {&s->x, &s->rhs, &s->r, &s->r0, &s->p, &s->v, &s->y, &s->z, &s->s, &s->t, &s->tmp0, &s->tmp1};
-    for (double2 **vp : vecs) UP(*vp, (const double2 *)nullptr, (size_t)s->n);
-    CK(cudaMemcpy(s->x, p->psi0, sizeof(double2) * (size_t)s->n, cudaMemcpyHostToDevice));
-    /* reductions */
-    s->upd_block = 256;
-    s->upd_grid = 2 * prop.multiProcessorCount;
-    size_t max_cta = (size_t)s->nchunk * s->nblk;
-    if ((size_t)s->upd_grid > max_cta) max_cta = s->upd_grid;
-    UP(s->d_part, (const double *)nullptr, max_cta * NRED);
-    UP(s->d_ticket, (const unsigned *)nullptr, 1);
-    UP(s->d_sc, (const DevScal *)nullptr, 1);
-    UP(s->d_coef, (const double2 *)nullptr, (size_t)s->lmax * 3);
-    if (cudaMallocHost((void **)&s->h_sc, sizeof(DevScal)) != cudaSuccess ||
-        cudaMallocHost((void **)&s->h_coef, sizeof(double2) * (size_t)s->lmax * 3) != cudaSuccess) {
-        gade_setup_release(su); gade_solver_free(s); return fail(GADE_ERR_CUDA, "pinned allocation failed");
-    }
-    UP(s->d_ell_col, su->ell_col, WB);
-    if (precision == GADE_PREC_MIXED) {
-        /* FP32 copies of every operator and preconditioner table */
-        const int CH = 1024 + 32 * s->bwp;
-        if (s->rc) {
-            R4f *m; UP(m, (const R4f *)nullptr, (size_t)s->lmax * s->nk * WB); s->d_M32 = m;
-        } else {
-            C4<float2> *m; UP(m, (const C4<float2> *)nullptr, (size_t)s->lmax * s->nk * WB); s->d_M32 = m;
-        }
-        {
-            std::vector<float2> Sf((size_t)s->nk * WB), Hf((size_t)s->nk * WB), Df((size_t)s->nk * WB);
-            for (size_t e = 0; e < Sf.size(); e++) {
-                Sf[e] = make_float2((float)su->S_ell[e].re, (float)su->S_ell[e].im);
-                Hf[e] = make_float2((float)su->Hst_ell[e].re, (float)su->Hst_ell[e].im);
-                Df[e] = make_float2((float)(su->S_ell[e].re + su->Hst_ell[e].re), (float)(su->S_ell[e].im + su->Hst_ell[e].im));
-            }
-            float2 *d;
-            UP(d, Sf.data(), Sf.size()); s->d_S32 = d;
-            UP(d, Hf.data(), Hf.size()); s->d_H32 = d;
-            UP(d, Df.data(), Df.size()); s->d_D32 = d;
-        }
-        {
-            const gc64 *src[4] = {su->ang_a0, su->ang_a0k, su->ang_a1, su->ang_a1k};
-            for (int k = 0; k < 4; k++) {
-                if (s->rc) {
-                    std::vector<float> v((size_t)su->n_ang + 1);
-                    for (int64_t e = 0; e < su->n_ang; e++) v[e] = (float)src[k][e].im;
-                    float *d; UP(d, v.data(), su->n_ang); s->d_a32[k] = d;
-                } else {
-                    std::vector<float2> v((size_t)su->n_ang + 1);
-                    for (int64_t e = 0; e < su->n_ang; e++) v[e] = make_float2((float)src[k][e].re, (float)src[k][e].im);
-                    float2 *d; UP(d, v.data(), su->n_ang); s->d_a32[k] = d;
+    /* per-pulse slices: dt-dependent D, i h dt/2 h0 and LU factors; radial tables */
+    {
+        std::vector<double2> D(s->dstride), FL(s->fstride), FU(s->fstride);
+        std::vector<float2> Hf, Df, FLf, FUf;
+        if (mixed) { Hf.resize(s->dstride); Df.resize(s->dstride); FLf.resize(s->fstride); FUf.resize(s->fstride); }
+        std::vector<double> gr, gtr;
+        std::vector<double2> gc, gtc;
+        if (s->rc) { gr.resize(s->gstride); gtr.resize(s->gstride); }
+        else { gc.resize(s->gstride); gtc.resize(s->gstride); }
+        std::vector<gc64> gtmp;
+        for (int k = 0; k < npulse; k++) {
+            gade_setup *sk = su;
+            if (k > 0) {
+                sk = nullptr;
+                rcode = gade_setup_build(p, dts[k], h, cs, &sk, err, sizeof(err));
+                if (rcode) { gade_setup_release(su); gade_solver_free(s); return fail(rcode, "pulse %d: %s", k, err); }
+                if (sk->bw != su->bw || sk->nk != su->nk || sk->nch != su->nch ||
+                    memcmp(sk->ord, su->ord, sizeof(int32_t) * s->B) != 0) {
+                    gade_setup_release(sk); gade_setup_release(su); gade_solver_free(s);
+                    return fail(GADE_ERR_ARG, "pulse %d: preconditioner ordering differs from pulse 0", k);
                 }
             }
-        }
-        {
-            /* FP32 copies of the packed FP64 LU factors */
-            std::vector<double2> FL((size_t)s->nk * s->nch * CH), FU((size_t)s->nk * s->nch * CH);
-            CK(cudaMemcpy(FL.data(), s->d_FL, sizeof(double2) * FL.size(), cudaMemcpyDeviceToHost));
-            CK(cudaMemcpy(FU.data(), s->d_FU, sizeof(double2) * FU.size(), cudaMemcpyDeviceToHost));
-            std::vector<float2> FLf(FL.size()), FUf(FU.size());
-            for (size_t e = 0; e < FL.size(); e++) {
-                FLf[e] = make_float2((float)FL[e].x, (float)FL[e].y);
-                FUf[e] = make_float2((float)FU[e].x, (float)FU[e].y);
+            for (size_t e = 0; e < s->dstride; e++)
+                D[e] = make_double2(sk->S_ell[e].re + sk->Hst_ell[e].re, sk->S_ell[e].im + sk->Hst_ell[e].im);
+            pack_factors(sk, s->nk, s->nch, s->bw, s->bwp, s->B, s->Bp, FL.data(), FU.data());
+            cudaError_t ce = cudaMemcpy((double2 *)s->d_Hst_ell + k * s->dstride, sk->Hst_ell, sizeof(double2) * s->dstride, cudaMemcpyHostToDevice);
+            if (ce == cudaSuccess) ce = cudaMemcpy((double2 *)s->d_D_ell + k * s->dstride, D.data(), sizeof(double2) * s->dstride, cudaMemcpyHostToDevice);
+            if (ce == cudaSuccess) ce = cudaMemcpy(s->d_FL + k * s->fstride, FL.data(), sizeof(double2) * s->fstride, cudaMemcpyHostToDevice);
+            if (ce == cudaSuccess) ce = cudaMemcpy(s->d_FU + k * s->fstride, FU.data(), sizeof(double2) * s->fstride, cudaMemcpyHostToDevice);
+            if (ce == cudaSuccess && mixed) {
+                for (size_t e = 0; e < s->dstride; e++) {
+                    Hf[e] = make_float2((float)sk->Hst_ell[e].re, (float)sk->Hst_ell[e].im);
+                    Df[e] = make_float2((float)D[e].x, (float)D[e].y);
+                }
+                for (size_t e = 0; e < s->fstride; e++) {
+                    FLf[e] = make_float2((float)FL[e].x, (float)FL[e].y);
+                    FUf[e] = make_float2((float)FU[e].x, (float)FU[e].y);
+                }
+                ce = cudaMemcpy((float2 *)s->d_H32 + k * s->dstride, Hf.data(), sizeof(float2) * s->dstride, cudaMemcpyHostToDevice);
+                if (ce == cudaSuccess) ce = cudaMemcpy((float2 *)s->d_D32 + k * s->dstride, Df.data(), sizeof(float2) * s->dstride, cudaMemcpyHostToDevice);
+                if (ce == cudaSuccess) ce = cudaMemcpy((float2 *)s->d_FL32 + k * s->fstride, FLf.data(), sizeof(float2) * s->fstride, cudaMemcpyHostToDevice);
+                if (ce == cudaSuccess) ce = cudaMemcpy((float2 *)s->d_FU32 + k * s->fstride, FUf.data(), sizeof(float2) * s->fstride, cudaMemcpyHostToDevice);
             }
-            float2 *d;
-            UP(d, FLf.data(), FLf.size()); s->d_FL32 = d;
-            UP(d, FUf.data(), FUf.size()); s->d_FU32 = d;
-            size_t smem = sizeof(float2) * ((size_t)2 * CH + s->Bp + 256);
-            cudaFuncSetAttribute(k_precond_tma<float, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            cudaFuncSetAttribute(k_precond_tma<float, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (sk != su) gade_setup_release(sk);
+            /* radial tables of the three pulse components used by each l */
+            const gc64 *g = p->g, *gt = p->gt;
+            if (gext) {
+                const size_t per = (size_t)6 * s->lmax * 4 * bn;
+                g = (const gc64 *)(gext + 2 * per * k);
+                gtmp.resize(per);
+                for (size_t blk = 0; blk < (size_t)6 * s->lmax * 4; blk++)
+                    for (size_t e = 0; e < bn; e++) {
+                        const gc64 v = g[blk * bn + e];
+                        gtmp[blk * bn + tpos[e]] = gc64{v.re, -v.im};
+                    }
+                gt = gtmp.data();
+            }
+            for (int l = 0; l < s->lmax; l++)
+                for (int ia = 0; ia < 3; ia++) {
+                    int a = (l % 2 + 1) % 2 + 2 * ia;
+                    for (int q = 0; q < 4; q++)
+                        for (size_t e = 0; e < bn; e++) {
+                            size_t src = (((size_t)a * s->lmax + l) * 4 + q) * bn + e;
+                            size_t dst = (((size_t)l * 3 + ia) * 4 + q) * bn + e;
+                            if (s->rc) { gr[dst] = g[src].re; gtr[dst] = gt[src].re; }
+                            else { gc[dst] = make_double2(g[src].re, g[src].im); gtc[dst] = make_double2(gt[src].re, gt[src].im); }
+                        }
+                }
+            if (ce == cudaSuccess) {
+                if (s->rc) {
+                    ce = cudaMemcpy((double *)s->d_g + k * s->gstride, gr.data(), sizeof(double) * s->gstride, cudaMemcpyHostToDevice);
+                    if (ce == cudaSuccess) ce = cudaMemcpy((double *)s->d_gt + k * s->gstride, gtr.data(), sizeof(double) * s->gstride, cudaMemcpyHostToDevice);
+                } else {
+                    ce = cudaMemcpy((double2 *)s->d_g + k * s->gstride, gc.data(), sizeof(double2) * s->gstride, cudaMemcpyHostToDevice);
+                    if (ce == cudaSuccess) ce = cudaMemcpy((double2 *)s->d_gt + k * s->gstride, gtc.data(), sizeof(double2) * s->gstride, cudaMemcpyHostToDevice);
+                }
+            }
+            if (ce != cudaSuccess) {
+                gade_setup_release(su); gade_solver_free(s);
+                return fail(GADE_ERR_CUDA, "upload of pulse %d failed: %s", k, cudaGetErrorString(ce));
+            }
         }
+    }
+    /* vectors: every pulse starts from psi0 */
+    double2 **vecs[] = {&s->x, &s->rhs, &s->r, &s->r0, &s->p, &s->v, &s->y, &s->z, &s->s, &s->t, &s->tmp0, &s->tmp1};
+    for (double2 **vp : vecs) UP(*vp, (const double2 *)nullptr, NP * s->n);
+    for (int k = 0; k < npulse; k++)
+        CK(cudaMemcpy(s->x + (size_t)k * s->n, p->psi0, sizeof(double2) * (size_t)s->n, cudaMemcpyHostToDevice));
+    /* reductions */
+    UP(s->d_ticket, (const unsigned *)nullptr, NP);
+    UP(s->d_sc, (const DevScal *)nullptr, NP);
+    UP(s->d_coef, (const double2 *)nullptr, NP * s->lmax * 3);
+    if (cudaMallocHost((void **)&s->h_sc, sizeof(DevScal) * NP) != cudaSuccess ||
+        cudaMallocHost((void **)&s->h_coef, sizeof(double2) * NP * s->lmax * 3) != cudaSuccess) {
+        gade_setup_release(su); gade_solver_free(s); return fail(GADE_ERR_CUDA, "pinned allocation failed");
+    }
+    memset(s->h_sc, 0, sizeof(DevScal) * NP);
+    if (mixed) {
         float2 **v32[] = {&s->x32, &s->d32, &s->q32, &s->r32, &s->e32, &s->ri32, &s->r032, &s->p32, &s->v32,
                           &s->y32, &s->z32, &s->s32, &s->t32};
-        for (float2 **vp : v32) UP(*vp, (const float2 *)nullptr, (size_t)s->n);
-        UP(s->xprev, (const double2 *)nullptr, (size_t)s->n);
-        UP(s->delta64, (const double2 *)nullptr, (size_t)s->n);
-        UP(s->d_sc2, (const DevScal *)nullptr, 1);
-        if (cudaMallocHost((void **)&s->h_sc2, sizeof(DevScal)) != cudaSuccess) {
+        for (float2 **vp : v32) UP(*vp, (const float2 *)nullptr, NP * s->n);
+        UP(s->xprev, (const double2 *)nullptr, NP * s->n);
+        UP(s->delta64, (const double2 *)nullptr, NP * s->n);
+        UP(s->d_sc2, (const DevScal *)nullptr, NP);
+        if (cudaMallocHost((void **)&s->h_sc2, sizeof(DevScal) * NP) != cudaSuccess) {
             gade_setup_release(su); gade_solver_free(s); return fail(GADE_ERR_CUDA, "pinned allocation failed");
         }
+        memset(s->h_sc2, 0, sizeof(DevScal) * NP);
     }
-    {
-        /* exact FP64 flop count of one operator apply (2 per FMA) */
-        const double fma_c = s->rc ? 2.0 : 4.0;     /* FMAs of one coupling term */
-        double fmas = 4.0 * (double)p->blk_nnz * s->nblk;             /* diagonal blocks (A x modes) */
-        for (int r = 0; r < s->nblk; r++)
-            for (int a = su->act_ptr[r]; a < su->act_ptr[r + 1]; a++) {
-                int l = su->act_l[a];
-                double ne = su->ang_ptr[r * s->lmax + l + 1] - su->ang_ptr[r * s->lmax + l];
-                double cols = 0;
-                for (int q = 0; q < s->nchunk; q++) cols += su->chunk_ncols[q];
-                fmas += 4.0 * fma_c * ne * cols;                       /* gather u, w, u', w' */
-                fmas += 4.0 * fma_c * (double)p->blk_nnz;              /* radial tables */
-            }
-        s->apply_flops = 2.0 * fmas;
-        /* block solves: per lane and chunk, bw band terms + 32 inverse terms, 2 sweeps */
-        s->precond_flops = 2.0 * 4.0 * (double)s->nblk * 32.0 * s->nch * 2.0 * (s->bwp + 32);
-    }
+    /* block solves: per lane and chunk, bw band terms + 32 inverse terms, 2 sweeps */
+    s->precond_flops = 2.0 * 4.0 * (double)s->nblk * 32.0 * s->nch * 2.0 * (s->bwp + 32);
     gade_setup_release(su);
+#undef UP
+#define UP(dst, src, cnt) do { int rc_ = dev_upload(s, &(dst), (src), (size_t)(cnt)); if (rc_) { gade_solver_free(s); return rc_; } } while (0)
     *out = s;
     return GADE_OK;
+}
+
+extern "C" int gade_solver_create(const gade_problem *p, double dt, double h, int32_t precision,
+                                  int32_t device, gade_solver **out)
+{
+    if (!p || !out) return fail(GADE_ERR_ARG, "gade_solver_create: NULL argument");
+    *out = nullptr;
+    if (precision != GADE_PREC_FP64 && precision != GADE_PREC_MIXED)
+        return fail(GADE_ERR_ARG, "gade_solver_create: unknown precision %d", precision);
+    if (!(dt > 0) || !std::isfinite(dt)) return fail(GADE_ERR_ARG, "gade_solver_create: dt must be finite and > 0");
+    return solver_create(p, 1, &dt, nullptr, h, precision, device, 0, out);
 }
 
 static OpP op_params(const gade_solver *s)
@@ -1320,7 +1487,16 @@ static OpP op_params(const gade_solver *s)
     P.chunk_nrows = s->d_chunk_nrows; P.chunk_ncols = s->d_chunk_ncols; P.chunk_rows = s->d_chunk_rows;
     P.chunk_cols = s->d_chunk_cols; P.chunk_lcol = s->d_chunk_lcol;
     P.M = s->d_M; P.S_ell = s->d_S_ell; P.Hst_ell = s->d_Hst_ell; P.D_ell = s->d_D_ell;
+    P.plist = s->d_plist; P.vstride = s->n; P.mstride = s->mstride; P.dstride = s->dstride;
     return P;
+}
+
+static RedP make_red(const gade_solver *s, DevScal *sc, int kind, int pred)
+{
+    RedP r;
+    r.part = s->d_part; r.ticket = s->d_ticket; r.sc = sc; r.kind = kind; r.out = nullptr;
+    r.pstride = s->pstride; r.pred = pred;
+    return r;
 }
 
 /* k_apply launch shape: one thread per output row and per gathered column */
@@ -1339,11 +1515,12 @@ static void apply_dims(const gade_solver *s, size_t elem, int *nt, size_t *smem)
     *smem = (b + 15) / 16 * 16;
 }
 
-static int launch_apply(gade_solver *s, const double2 *x, int mode, VecP V, int redkind, cudaStream_t st)
+static int launch_apply(gade_solver *s, const double2 *x, int mode, VecP V, int redkind, cudaStream_t st,
+                        int pred = PRED_NONE)
 {
     OpP P = op_params(s);
-    RedP red = {s->d_part, s->d_ticket, s->d_sc, redkind};
-    dim3 grid(s->nchunk, s->nblk);
+    RedP red = make_red(s, s->d_sc, redkind, pred);
+    dim3 grid(s->nslot, s->nchunk, s->nblk);
     int nt;
     size_t smem;
     apply_dims(s, sizeof(double2), &nt, &smem);
@@ -1355,62 +1532,85 @@ static int launch_apply(gade_solver *s, const double2 *x, int mode, VecP V, int 
     return GADE_OK;
 }
 
-static int launch_precond(gade_solver *s, int mode, const double2 *in0, const double2 *in1, double2 *io,
-                          double2 *out, cudaStream_t st)
+static PcT pc_params(const gade_solver *s, const void *FL, const void *FU, int pred)
 {
     PcT Q;
     Q.nblk = s->nblk; Q.B = s->B; Q.Bp = s->Bp; Q.nch = s->nch;
-    Q.row_kidx = s->d_row_kidx; Q.ord = s->d_ord; Q.FL = s->d_FL; Q.FU = s->d_FU;
+    Q.row_kidx = s->d_row_kidx; Q.ord = s->d_ord; Q.FL = FL; Q.FU = FU;
+    Q.plist = s->d_plist; Q.vstride = s->n; Q.fstride = s->fstride; Q.pred = pred;
+    return Q;
+}
+
+static int launch_precond(gade_solver *s, int mode, const double2 *in0, const double2 *in1, double2 *io,
+                          double2 *out, cudaStream_t st, int pred = PRED_NONE)
+{
+    PcT Q = pc_params(s, s->d_FL, s->d_FU, pred);
     const int CH = 1024 + 32 * s->bwp;
     size_t smem = sizeof(double2) * ((size_t)2 * CH + s->Bp + 256);
+    dim3 grid(s->nslot, s->nblk);
     prof_begin(s, st);
-    if (s->bwp == 16) k_precond_tma<double, 16><<<s->nblk, 128, smem, st>>>(Q, mode, in0, in1, io, out, s->d_sc);
-    else k_precond_tma<double, 32><<<s->nblk, 128, smem, st>>>(Q, mode, in0, in1, io, out, s->d_sc);
+    if (s->bwp == 16) k_precond_tma<double, 16><<<grid, 128, smem, st>>>(Q, mode, in0, in1, io, out, s->d_sc);
+    else k_precond_tma<double, 32><<<grid, 128, smem, st>>>(Q, mode, in0, in1, io, out, s->d_sc);
     prof_end(s, st, 1);
     CKL();
     return GADE_OK;
 }
 
-static int launch_tables(gade_solver *s, const double *ft, int which = 1)
+/* coefficients of pulse k: c_a = SoL * (i h dt_k/2) * f_a, as in tools/solver.c:274 */
+static int fill_coef(gade_solver *s, int k, const double *ft)
 {
-    /* c_a = SoL * (i h dt/2) * f_a, as in tools/solver.c:274 */
-    const double hdt2 = s->h * s->dt / 2;
+    const double hdt2 = s->h * s->dts[k] / 2;
+    double2 *c = s->h_coef + (size_t)k * s->lmax * 3;
     for (int l = 0; l < s->lmax; l++)
         for (int ia = 0; ia < 3; ia++) {
             int a = (l % 2 + 1) % 2 + 2 * ia;
             double fr = ft[2 * a], fi = ft[2 * a + 1];
             /* (SoL * (0 + i hdt2)) * (fr + i fi) */
             double cr = 0.0 * SOL, ci = SOL * hdt2;
-            s->h_coef[l * 3 + ia] = make_double2(cr * fr - ci * fi, cr * fi + ci * fr);
+            c[l * 3 + ia] = make_double2(cr * fr - ci * fi, cr * fi + ci * fr);
         }
     if (s->rc)
         for (int a = 0; a < 6; a++)
             if (ft[2 * a + 1] != 0.0)
                 return fail(GADE_ERR_ARG, "pulse factor f_%d has an imaginary part; the real-coupling tables need real f(t)", a);
-    CK(cudaMemcpyAsync(s->d_coef, s->h_coef, sizeof(double2) * (size_t)s->lmax * 3, cudaMemcpyHostToDevice, s->stream));
+    return GADE_OK;
+}
+
+/* per-step radial tables of the listed pulses from d_coef (which: 1 FP64, 2 FP32) */
+static int launch_table_kernels(gade_solver *s, int which, cudaStream_t st)
+{
     TabP T;
     T.lmax = s->lmax; T.nk = s->nk; T.W = s->W; T.B = s->B; T.blk_nnz = s->blk_nnz;
     T.kvals = s->d_kvals; T.ell_pos = s->d_ell_pos; T.g = s->d_g; T.gt = s->d_gt; T.M = s->d_M;
+    T.plist = s->d_plist; T.gstride = s->gstride; T.mstride = s->mstride;
     long long total = (long long)s->lmax * s->W * s->B;
     int nt = 256;
-    long long grid = (total + nt - 1) / nt;
+    dim3 grid((unsigned)((total + nt - 1) / nt), s->nslot);
     if (which & 1) {            /* FP64 tables */
-        prof_begin(s, s->stream);
-        if (s->rc) k_tables<double, true><<<(unsigned)grid, nt, 0, s->stream>>>(T, s->d_coef);
-        else k_tables<double, false><<<(unsigned)grid, nt, 0, s->stream>>>(T, s->d_coef);
-        prof_end(s, s->stream, 2);
+        prof_begin(s, st);
+        if (s->rc) k_tables<double, true><<<grid, nt, 0, st>>>(T, s->d_coef);
+        else k_tables<double, false><<<grid, nt, 0, st>>>(T, s->d_coef);
+        prof_end(s, st, 2);
         CKL();
         s->has_time = 1;
     }
     if ((which & 2) && s->d_M32) {   /* FP32 tables (mixed precision) */
         T.M = s->d_M32;
-        prof_begin(s, s->stream);
-        if (s->rc) k_tables<float, true><<<(unsigned)grid, nt, 0, s->stream>>>(T, s->d_coef);
-        else k_tables<float, false><<<(unsigned)grid, nt, 0, s->stream>>>(T, s->d_coef);
-        prof_end(s, s->stream, 2);
+        prof_begin(s, st);
+        if (s->rc) k_tables<float, true><<<grid, nt, 0, st>>>(T, s->d_coef);
+        else k_tables<float, false><<<grid, nt, 0, st>>>(T, s->d_coef);
+        prof_end(s, st, 2);
         CKL();
     }
     return GADE_OK;
+}
+
+static int launch_tables(gade_solver *s, const double *ft, int which = 1)
+{
+    int rc = fill_coef(s, 0, ft);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(s->d_coef, s->h_coef, sizeof(double2) * (size_t)s->lmax * 3, cudaMemcpyHostToDevice, s->stream));
+    return launch_table_kernels(s, which, s->stream);
 }
 
 static int sync_scal(gade_solver *s)
@@ -1513,11 +1713,12 @@ static OpP op_params32(const gade_solver *s)
     return P;
 }
 
-static int launch_apply32(gade_solver *s, const float2 *x, int mode, VecP V, int redkind, DevScal *sc)
+static int launch_apply32(gade_solver *s, const float2 *x, int mode, VecP V, int redkind, DevScal *sc,
+                          int pred = PRED_NONE)
 {
     OpP P = op_params32(s);
-    RedP red = {s->d_part, s->d_ticket, sc, redkind};
-    dim3 grid(s->nchunk, s->nblk);
+    RedP red = make_red(s, sc, redkind, pred);
+    dim3 grid(s->nslot, s->nchunk, s->nblk);
     int nt;
     size_t smem;
     apply_dims(s, sizeof(float2), &nt, &smem);
@@ -1530,16 +1731,15 @@ static int launch_apply32(gade_solver *s, const float2 *x, int mode, VecP V, int
 }
 
 static int launch_precond32(gade_solver *s, int mode, const float2 *in0, const float2 *in1, float2 *io,
-                            float2 *out, DevScal *sc)
+                            float2 *out, DevScal *sc, int pred = PRED_NONE)
 {
-    PcT Q;
-    Q.nblk = s->nblk; Q.B = s->B; Q.Bp = s->Bp; Q.nch = s->nch;
-    Q.row_kidx = s->d_row_kidx; Q.ord = s->d_ord; Q.FL = s->d_FL32; Q.FU = s->d_FU32;
+    PcT Q = pc_params(s, s->d_FL32, s->d_FU32, pred);
     const int CH = 1024 + 32 * s->bwp;
     size_t smem = sizeof(float2) * ((size_t)2 * CH + s->Bp + 256);
+    dim3 grid(s->nslot, s->nblk);
     prof_begin(s, s->stream);
-    if (s->bwp == 16) k_precond_tma<float, 16><<<s->nblk, 128, smem, s->stream>>>(Q, mode, in0, in1, io, out, sc);
-    else k_precond_tma<float, 32><<<s->nblk, 128, smem, s->stream>>>(Q, mode, in0, in1, io, out, sc);
+    if (s->bwp == 16) k_precond_tma<float, 16><<<grid, 128, smem, s->stream>>>(Q, mode, in0, in1, io, out, sc);
+    else k_precond_tma<float, 32><<<grid, 128, smem, s->stream>>>(Q, mode, in0, in1, io, out, sc);
     prof_end(s, s->stream, 1);
     CKL();
     return GADE_OK;
@@ -1616,7 +1816,7 @@ static int mixed_step(gade_solver *s, const double *ft, int32_t maxit, double to
         if (rr < tol2 || sweep >= MIXED_MAX_SWEEPS || maxit_in <= 0) break;
         sweep++;
         {
-            RedP red = {s->d_part, s->d_ticket, s->d_sc2, RED_RHS};
+            RedP red = make_red(s, s->d_sc2, RED_RHS, PRED_NONE);
             prof_begin(s, s->stream);
             k_inner_init<<<grid, blk, rsm, s->stream>>>(n, s->r, s->e32, s->ri32, s->r032, s->p32, s->v32, red);
             prof_end(s, s->stream, 2);
@@ -1637,10 +1837,10 @@ static int mixed_step(gade_solver *s, const double *ft, int32_t maxit, double to
             VecP A2 = {}; A2.out0 = s->t32; A2.in0 = s->s32;
             if ((rc = launch_apply32(s, s->z32, AX_TS, A2, RED_TS, s->d_sc2))) return rc;
             {
-                RedP red = {s->d_part, s->d_ticket, s->d_sc2, RED_UPDATE};
+                RedP red = make_red(s, s->d_sc2, RED_UPDATE, PRED_NONE);
                 prof_begin(s, s->stream);
                 k_update<float><<<grid, blk, rsm, s->stream>>>(n, s->e32, s->y32, s->z32, s->ri32, s->s32,
-                                                               s->t32, s->r032, red);
+                                                               s->t32, s->r032, red, nullptr);
                 prof_end(s, s->stream, 2);
                 CKL();
             }
@@ -1735,10 +1935,10 @@ extern "C" int gade_solver_step(gade_solver *s, const double *ft, int32_t maxit,
         if ((rc = launch_apply(s, s->z, AX_TS, A2, RED_TS, s->stream))) return rc;
         /* x += alpha y + w z; r = s - w t; |r|^2; rho = <r0, r> */
         {
-            RedP red = {s->d_part, s->d_ticket, s->d_sc, RED_UPDATE};
+            RedP red = make_red(s, s->d_sc, RED_UPDATE, PRED_NONE);
             prof_begin(s, s->stream);
             k_update<double><<<s->upd_grid, s->upd_block, sizeof(double) * NRED * s->upd_block, s->stream>>>(
-                s->n, s->x, s->y, s->z, s->r, s->s, s->t, s->r0, red);
+                s->n, s->x, s->y, s->z, s->r, s->s, s->t, s->r0, red, nullptr);
             prof_end(s, s->stream, 2);
             CKL();
         }
@@ -1919,11 +2119,12 @@ extern "C" int gade_solver_apply_dot_noalloc(gade_solver *s, const void *x_dev, 
     /* the arrival ticket must start at zero */
     CK(cudaMemsetAsync(ticket, 0, sizeof(unsigned int), st));
     OpP P = op_params(s);
-    RedP red = {base, ticket, s->d_sc, RED_DOT_OUT, (double *)dot_dev};
+    RedP red = make_red(s, s->d_sc, RED_DOT_OUT, PRED_NONE);
+    red.part = base; red.ticket = ticket; red.out = (double *)dot_dev;
     VecP V = {};
     V.out0 = y_dev;
     V.in0 = r0_dev;
-    dim3 grid(s->nchunk, s->nblk);
+    dim3 grid(1, s->nchunk, s->nblk);
     int nt;
     size_t smem;
     apply_dims(s, sizeof(double2), &nt, &smem);
@@ -1932,3 +2133,347 @@ extern "C" int gade_solver_apply_dot_noalloc(gade_solver *s, const void *x_dev, 
     CKL();
     return GADE_OK;
 }
+
+/* ------------------------------------------------------------------ */
+/* batched pulses                                                      */
+/* ------------------------------------------------------------------ */
+/*
+ * A batch holds npulse Crank-Nicolson problems on one set of angular tables,
+ * h0 and S; each pulse has its own dt, radial tables g and block-LU factors.
+ * Every kernel runs over the pulses of the launch list (grid x = pulse slot),
+ * and BiCGSTAB's control (convergence, iteration limit, restart test) lives
+ * in the reduction epilogues, so a step is a fixed kernel sequence: the
+ * tables, the right-hand side and K predicated iterations, captured once as
+ * a CUDA graph and replayed.  The host reads the pulse states after each
+ * replay and replays the iteration graph (preceded by the predicated restart
+ * launch when a pulse asks for one) until no pulse is running.  A pulse
+ * whose time grid has ended leaves the launch list (graphs are re-captured),
+ * so finished pulses cost nothing.
+ */
+struct gade_batch {
+    gade_solver *s;
+    std::vector<int> list;          /* pulses of the current launch list */
+    int kiter, kfixed;              /* iterations per captured launch; fixed value or 0 (adaptive) */
+    int kwin, kwin_steps;           /* largest iteration count since the last shrink, steps since */
+    double tol_c;
+    int maxit_c;
+    int use_graphs;
+    cudaGraphExec_t g_first, g_iter, g_restart;
+    long long replays, steps;
+    float tune_ms[4];
+    int tune_cs[4], ntune;
+};
+
+static void batch_drop_graphs(gade_batch *b)
+{
+    if (b->g_first) cudaGraphExecDestroy(b->g_first);
+    if (b->g_iter) cudaGraphExecDestroy(b->g_iter);
+    if (b->g_restart) cudaGraphExecDestroy(b->g_restart);
+    b->g_first = b->g_iter = b->g_restart = nullptr;
+}
+
+/* K predicated BiCGSTAB iterations of every listed pulse still running */
+static int batch_seq_iters(gade_batch *b, int K, cudaStream_t st)
+{
+    gade_solver *s = b->s;
+    int rc;
+    const size_t rsm = sizeof(double) * NRED * s->upd_block;
+    for (int it = 0; it < K; it++) {
+        if ((rc = launch_precond(s, PC_P, s->r, s->v, s->p, s->y, st, PRED_RUN))) return rc;
+        VecP A1 = {}; A1.out0 = s->v; A1.in0 = s->r0;
+        if ((rc = launch_apply(s, s->y, AX_R0V, A1, RED_R0V, st, PRED_RUN))) return rc;
+        if ((rc = launch_precond(s, PC_S, s->r, s->v, s->s, s->z, st, PRED_RUN))) return rc;
+        VecP A2 = {}; A2.out0 = s->t; A2.in0 = s->s;
+        if ((rc = launch_apply(s, s->z, AX_TS, A2, RED_TS, st, PRED_RUN))) return rc;
+        RedP red = make_red(s, s->d_sc, RED_UPDATE, PRED_RUN);
+        k_update<double><<<dim3(s->upd_grid, s->nslot), s->upd_block, rsm, st>>>(
+            s->n, s->x, s->y, s->z, s->r, s->s, s->t, s->r0, red, s->d_plist);
+        CKL();
+    }
+    return GADE_OK;
+}
+
+static int batch_seq_first(gade_batch *b, cudaStream_t st)
+{
+    gade_solver *s = b->s;
+    int rc;
+    if ((rc = launch_table_kernels(s, 1, st))) return rc;
+    VecP V = {};
+    V.out0 = s->rhs; V.out1 = s->r; V.out2 = s->r0;
+    if ((rc = launch_apply(s, s->x, AX_RHS, V, RED_RHS, st, PRED_NONE))) return rc;
+    return batch_seq_iters(b, b->kiter, st);
+}
+
+static int batch_seq_restart(gade_batch *b, cudaStream_t st)
+{
+    gade_solver *s = b->s;
+    VecP R = {};
+    R.in0 = s->rhs; R.out1 = s->r; R.out2 = s->r0;
+    return launch_apply(s, s->x, AX_RESTART, R, RED_RESTART, st, PRED_RESTART);
+}
+
+/* which: 0 first, 1 iterations, 2 restart */
+static int batch_run_seq(gade_batch *b, int which)
+{
+    cudaStream_t st = b->s->stream;
+    switch (which) {
+    case 0: return batch_seq_first(b, st);
+    case 1: return batch_seq_iters(b, b->kiter, st);
+    default: return batch_seq_restart(b, st);
+    }
+}
+
+static int batch_launch(gade_batch *b, int which)
+{
+    gade_solver *s = b->s;
+    b->replays++;
+    if (!b->use_graphs) return batch_run_seq(b, which);
+    cudaGraphExec_t *slot = which == 0 ? &b->g_first : which == 1 ? &b->g_iter : &b->g_restart;
+    if (!*slot) {
+        cudaGraph_t g = nullptr;
+        CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+        int rc = batch_run_seq(b, which);
+        cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
+        if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+        if (ce != cudaSuccess) return fail(GADE_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(ce));
+        ce = cudaGraphInstantiate(slot, g, 0);
+        cudaGraphDestroy(g);
+        if (ce != cudaSuccess) { *slot = nullptr; return fail(GADE_ERR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(ce)); }
+    }
+    CK(cudaGraphLaunch(*slot, s->stream));
+    return GADE_OK;
+}
+
+static int batch_set_list(gade_batch *b, const std::vector<int> &list)
+{
+    gade_solver *s = b->s;
+    if (list == b->list) return GADE_OK;
+    CK(cudaMemcpyAsync(s->d_plist, list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    b->list = list;
+    s->nslot = (int)list.size();
+    batch_drop_graphs(b);
+    return GADE_OK;
+}
+
+/* Candidate row-chunk sizes, each timed on one batched operator apply (the
+   step's dominant kernel) over all pulses; the fastest is kept. */
+static int batch_autotune(gade_batch *b, const gade_problem *p)
+{
+    gade_solver *s = b->s;
+    const int cand[4] = {16, 32, 48, 64};
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1));
+    float best = 1e30f;
+    gade_setup *keep = nullptr;
+    char err[1024];
+    b->ntune = 0;
+    const bool mixed = s->prec == GADE_PREC_MIXED;
+    for (int c = 0; c < 4; c++) {
+        gade_setup *su = nullptr;
+        int rc = gade_setup_build(p, s->dts[0], s->h, cand[c], &su, err, sizeof(err));
+        if (rc) { cudaEventDestroy(e0); cudaEventDestroy(e1); return fail(rc, "%s", err); }
+        if (b->ntune > 0 && su->chunk_splines == b->tune_cs[b->ntune - 1]) { gade_setup_release(su); continue; }
+        if (su->chunk_rows_max > 128 || su->chunk_cols_max > 256) { gade_setup_release(su); continue; }
+        if ((rc = set_chunking(s, su))) { gade_setup_release(su); cudaEventDestroy(e0); cudaEventDestroy(e1); return rc; }
+        VecP V = {}; V.in0 = s->r0;
+        float ms = 0;
+        for (int rep = 0; rep < 4; rep++) {
+            if (rep == 1) CK(cudaEventRecord(e0, s->stream));
+            if (mixed) { V.out0 = s->v32; V.in0 = s->r032; rc = launch_apply32(s, s->y32, AX_R0V, V, RED_R0V, s->d_sc); }
+            else { V.out0 = s->tmp1; rc = launch_apply(s, s->y, AX_R0V, V, RED_R0V, s->stream); }
+            if (rc) { gade_setup_release(su); cudaEventDestroy(e0); cudaEventDestroy(e1); return rc; }
+        }
+        CK(cudaEventRecord(e1, s->stream));
+        CK(cudaEventSynchronize(e1));
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        ms /= 3;
+        b->tune_cs[b->ntune] = su->chunk_splines;
+        b->tune_ms[b->ntune] = ms;
+        b->ntune++;
+        if (ms < best) { best = ms; if (keep) gade_setup_release(keep); keep = su; }
+        else gade_setup_release(su);
+    }
+    cudaEventDestroy(e0); cudaEventDestroy(e1);
+    if (!keep) return fail(GADE_ERR_ARG, "no row-chunk size fits the operator kernel");
+    int rc = set_chunking(s, keep);
+    gade_setup_release(keep);
+    return rc;
+}
+
+extern "C" int gade_batch_create(const gade_problem *p, int32_t npulse, const double *dt, const double *g,
+                                 double h, int32_t precision, int32_t device, const gade_batch_options *opt,
+                                 gade_batch **out)
+{
+    if (!p || !dt || !out) return fail(GADE_ERR_ARG, "gade_batch_create: NULL argument");
+    *out = nullptr;
+    if (npulse < 1 || npulse > 65535) return fail(GADE_ERR_ARG, "gade_batch_create: npulse %d out of range", npulse);
+    if (precision != GADE_PREC_FP64)
+        return fail(GADE_ERR_ARG, "gade_batch_create: precision %d is not available for batches", precision);
+    gade_batch_options o = {0, 0, 1};
+    if (opt) o = *opt;
+    if (o.chunk_splines < 0 || o.chunk_splines > 64 || o.iters_per_launch < 0 || o.iters_per_launch > 64)
+        return fail(GADE_ERR_ARG, "gade_batch_create: option out of range");
+    gade_solver *s = nullptr;
+    int rc = solver_create(p, npulse, dt, g, h, precision, device, o.chunk_splines, &s);
+    if (rc) return rc;
+    if (npulse == 1) {
+        /* a batch always runs from a launch list, even with one pulse */
+        int zero = 0;
+        if ((rc = dev_upload(s, &s->d_plist, &zero, 1))) { gade_solver_free(s); return rc; }
+    }
+    gade_batch *b = new gade_batch();
+    b->s = s;
+    b->kfixed = o.iters_per_launch;
+    b->kiter = o.iters_per_launch > 0 ? o.iters_per_launch : 4;
+    b->use_graphs = o.use_graphs != 0;
+    b->tol_c = -1; b->maxit_c = -1;
+    for (int k = 0; k < npulse; k++) b->list.push_back(k);
+    s->nslot = npulse;
+    if (o.chunk_splines == 0 && (rc = batch_autotune(b, p))) { gade_batch_free(b); return rc; }
+    *out = b;
+    return GADE_OK;
+}
+
+extern "C" void gade_batch_free(gade_batch *b)
+{
+    if (!b) return;
+    if (b->s) { cudaSetDevice(b->s->device); cudaStreamSynchronize(b->s->stream); }
+    batch_drop_graphs(b);
+    gade_solver_free(b->s);
+    delete b;
+}
+
+extern "C" int gade_batch_set_x(gade_batch *b, int32_t pulse, const double *x, int64_t n)
+{
+    if (!b || !x) return fail(GADE_ERR_ARG, "gade_batch_set_x: NULL argument");
+    gade_solver *s = b->s;
+    if (pulse < 0 || pulse >= s->npulse) return fail(GADE_ERR_ARG, "gade_batch_set_x: no pulse %d", pulse);
+    if (n != s->n) return fail(GADE_ERR_ARG, "gade_batch_set_x: size %lld != %lld", (long long)n, s->n);
+    CK(cudaSetDevice(s->device));
+    CK(cudaMemcpyAsync(s->x + (size_t)pulse * s->n, x, sizeof(double2) * (size_t)n, cudaMemcpyHostToDevice, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return GADE_OK;
+}
+
+extern "C" int gade_batch_get_x(gade_batch *b, int32_t pulse, double *x, int64_t n)
+{
+    if (!b || !x) return fail(GADE_ERR_ARG, "gade_batch_get_x: NULL argument");
+    gade_solver *s = b->s;
+    if (pulse < 0 || pulse >= s->npulse) return fail(GADE_ERR_ARG, "gade_batch_get_x: no pulse %d", pulse);
+    if (n != s->n) return fail(GADE_ERR_ARG, "gade_batch_get_x: size %lld != %lld", (long long)n, s->n);
+    CK(cudaSetDevice(s->device));
+    CK(cudaMemcpyAsync(x, s->x + (size_t)pulse * s->n, sizeof(double2) * (size_t)n, cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return GADE_OK;
+}
+
+extern "C" int gade_batch_step(gade_batch *b, const int32_t *active, const double *ft, int32_t maxit, double tol,
+                               gade_step_stats *stats)
+{
+    if (!b || !ft) return fail(GADE_ERR_ARG, "gade_batch_step: NULL argument");
+    if (maxit < 0) return fail(GADE_ERR_ARG, "gade_batch_step: maxit < 0");
+    if (!(tol >= 0) || !std::isfinite(tol)) return fail(GADE_ERR_ARG, "gade_batch_step: tol must be finite and >= 0");
+    gade_solver *s = b->s;
+    CK(cudaSetDevice(s->device));
+    std::vector<int> list;
+    for (int k = 0; k < s->npulse; k++)
+        if (!active || active[k]) list.push_back(k);
+    if (stats)
+        for (int k = 0; k < s->npulse; k++) stats[k] = gade_step_stats{};
+    if (list.empty()) return GADE_OK;
+    int rc;
+    for (int k : list)
+        if ((rc = fill_coef(s, k, ft + 12 * (size_t)k))) {
+            char msg[512];
+            snprintf(msg, sizeof(msg), "%s", gade_last_error());
+            return fail(rc, "pulse %d: %s", k, msg);
+        }
+    if ((rc = batch_set_list(b, list))) return rc;
+    if (tol != b->tol_c || maxit != b->maxit_c) {
+        /* control values of every pulse (the rest of each record is reset by
+           the right-hand-side reduction of the step) */
+        for (int k = 0; k < s->npulse; k++) {
+            DevScal &d = s->h_sc[k];
+            d = DevScal{};
+            d.ctl = 1; d.tol2rel = tol * tol; d.maxit = maxit;
+        }
+        CK(cudaMemcpyAsync(s->d_sc, s->h_sc, sizeof(DevScal) * s->npulse, cudaMemcpyHostToDevice, s->stream));
+        b->tol_c = tol; b->maxit_c = maxit;
+    }
+    CK(cudaMemcpyAsync(s->d_coef, s->h_coef, sizeof(double2) * (size_t)s->npulse * s->lmax * 3,
+                       cudaMemcpyHostToDevice, s->stream));
+    if ((rc = batch_launch(b, 0))) return rc;
+    /* every replay advances each running pulse by at least one iteration, so
+       the loop ends within maxit replays */
+    int kmax = 0;
+    for (long long guard = 0;; guard++) {
+        CK(cudaMemcpyAsync(s->h_sc, s->d_sc, sizeof(DevScal) * s->npulse, cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        int nrun = 0, nrestart = 0;
+        for (int k : list) {
+            const DevScal &d = s->h_sc[k];
+            if (d.err) {
+                CK(cudaMemsetAsync(&s->d_sc[k].err, 0, sizeof(unsigned), s->stream));
+                return fail(GADE_ERR_CUDA, "pulse %d: device wait timed out (flags %u): TMA copy did not complete", k, d.err);
+            }
+            if (d.state == ST_BAD) return fail(GADE_ERR_NUMERIC, "pulse %d: BiCGSTAB residual became non-finite at iteration %d", k, d.iter);
+            if (d.state == ST_RUN) nrun++;
+            if (d.state == ST_RESTART) nrestart++;
+            if (d.iter > kmax) kmax = d.iter;
+        }
+        if (!nrun && !nrestart) break;
+        if (guard > (long long)maxit + 2) return fail(GADE_ERR_STATE, "gade_batch_step: iteration control did not terminate");
+        if (nrestart && (rc = batch_launch(b, 2))) return rc;
+        if ((rc = batch_launch(b, 1))) return rc;
+    }
+    for (int k : list) {
+        const DevScal &d = s->h_sc[k];
+        gade_step_stats st = {};
+        if (d.state == ST_ZERO) {
+            CK(cudaMemsetAsync(s->x + (size_t)k * s->n, 0, sizeof(double2) * (size_t)s->n, s->stream));
+        } else {
+            st.iters = d.iter;
+            st.tol_error = sqrt(d.rr / d.rhs_sqnorm);
+            st.restarts = d.restarts;
+        }
+        if (stats) stats[k] = st;
+    }
+    CK(cudaStreamSynchronize(s->stream));
+    b->steps++;
+    /* iterations per captured launch: large enough that most steps need one
+       replay, shrunk only after 32 steps with fewer iterations */
+    if (!b->kfixed) {
+        int want = kmax + 1 > 1 ? kmax + 1 : 1;
+        if (want > 64) want = 64;
+        if (want > b->kwin) b->kwin = want;
+        b->kwin_steps++;
+        if (want > b->kiter || (b->kwin_steps >= 32 && b->kwin < b->kiter)) {
+            b->kiter = want > b->kiter ? want : b->kwin;
+            b->kwin = 0; b->kwin_steps = 0;
+            batch_drop_graphs(b);
+        } else if (b->kwin_steps >= 32) {
+            b->kwin = 0; b->kwin_steps = 0;
+        }
+    }
+    return GADE_OK;
+}
+
+extern "C" int gade_batch_get_info(const gade_batch *b, gade_batch_info *info)
+{
+    if (!b || !info) return fail(GADE_ERR_ARG, "gade_batch_get_info: NULL argument");
+    const gade_solver *s = b->s;
+    *info = gade_batch_info{};
+    info->npulse = s->npulse;
+    info->active = (int32_t)b->list.size();
+    info->chunk_splines = s->cs;
+    info->iters_per_launch = b->kiter;
+    info->graph_replays = b->replays;
+    info->steps = b->steps;
+    info->ntune = b->ntune;
+    for (int k = 0; k < b->ntune && k < 4; k++) { info->tune_cs[k] = b->tune_cs[k]; info->tune_ms[k] = b->tune_ms[k]; }
+    info->apply_flops = s->apply_flops;
+    return GADE_OK;
+}
+
+extern "C" void *gade_batch_stream(const gade_batch *b) { return b && b->s ? (void *)b->s->stream : nullptr; }

@@ -331,6 +331,17 @@ static int band_lu(gc64 *band, int B, int bw)
     return 0;
 }
 
+int gade_problem_transpose_map(const gade_problem *p, int32_t *tpos)
+{
+    for (int32_t r = 0; r < p->blkdim; r++)
+        for (int32_t k = p->g_Ap[r]; k < p->g_Ap[r + 1]; k++) {
+            int32_t pos = csr_find(p->g_Ap, p->g_Ai, p->g_Ai[k], r);
+            if (pos < 0) return 1;
+            tpos[k] = pos;
+        }
+    return 0;
+}
+
 int gade_setup_build(const gade_problem *p, double dt, double h, int chunk_splines,
                      gade_setup **out, char *err, size_t len)
 {
@@ -369,6 +380,7 @@ int gade_setup_build(const gade_problem *p, double dt, double h, int chunk_splin
         int half = (B % 2 == 0) ? B / 2 : B;
         int cs = chunk_splines > 0 ? chunk_splines : 64;
         if (cs > half) cs = half;
+        s->chunk_splines = cs;
         int rows_per = (B % 2 == 0) ? 2 * cs : cs;
         s->nchunk = (half + cs - 1) / cs;
         s->chunk_rows_max = rows_per;

@@ -48,6 +48,7 @@ typedef struct gade_setup {
     int32_t *ell_col;             /* [W][B] column or -1                  */
     /* row chunks: every block row is split into the same nchunk row sets */
     int nchunk, chunk_rows_max, chunk_cols_max;
+    int chunk_splines;            /* splines (of each half) per row chunk  */
     int32_t *chunk_nrows, *chunk_ncols;    /* [nchunk]                     */
     int32_t *chunk_rows;          /* [nchunk][chunk_rows_max] row (or -1) */
     int32_t *chunk_cols;          /* [nchunk][chunk_cols_max] col (or -1) */
@@ -78,6 +79,9 @@ void gade_problem_release(gade_problem *p);
 int gade_setup_build(const gade_problem *p, double dt, double h, int chunk_splines,
                      gade_setup **out, char *err, size_t errlen);
 void gade_setup_release(gade_setup *s);
+/* tpos[k]: CSR position of the transpose of base-pattern entry k; nonzero
+   when the pattern is not structurally symmetric */
+int gade_problem_transpose_map(const gade_problem *p, int32_t *tpos);
 
 /* kappa of an angular index, tools/solver_common.c:87-94 */
 int gade_ik(int i);

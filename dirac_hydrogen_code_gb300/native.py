@@ -44,6 +44,17 @@ class KernelTimes(C.Structure):
                 ("other_launches", C.c_int64), ("other_ms", C.c_double)]
 
 
+class BatchOptions(C.Structure):
+    _fields_ = [("chunk_splines", C.c_int32), ("iters_per_launch", C.c_int32), ("use_graphs", C.c_int32)]
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [("npulse", C.c_int32), ("active", C.c_int32), ("chunk_splines", C.c_int32),
+                ("iters_per_launch", C.c_int32), ("graph_replays", C.c_int64), ("steps", C.c_int64),
+                ("ntune", C.c_int32), ("tune_cs", C.c_int32 * 4), ("tune_ms", C.c_float * 4),
+                ("apply_flops", C.c_double)]
+
+
 _LIB = None
 
 # every entry point of include/gade.h with its ctypes signature
@@ -73,6 +84,15 @@ _SIGS = {
     "gade_solver_flops": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "gade_solver_apply_dot_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                                 C.c_void_p]),
+    "gade_batch_create": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_double, C.c_int32,
+                                    C.c_int32, C.POINTER(BatchOptions), C.POINTER(C.c_void_p)]),
+    "gade_batch_free": (None, [C.c_void_p]),
+    "gade_batch_set_x": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64]),
+    "gade_batch_get_x": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_int64]),
+    "gade_batch_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_double,
+                                  C.POINTER(StepStats)]),
+    "gade_batch_get_info": (C.c_int, [C.c_void_p, C.POINTER(BatchInfo)]),
+    "gade_batch_stream": (C.c_void_p, [C.c_void_p]),
 }
 
 
@@ -255,3 +275,82 @@ def fp64_peak_tflops(device: int = 0) -> float:
     v = C.c_double()
     _check(load_library().gade_probe_fp64_peak(int(device), C.byref(v)))
     return v.value
+
+
+class Batch:
+    """Many pulses on one problem's angular tables, h0 and S (gade_batch_*).
+
+    ``dts``: time step of each pulse; ``g``: None (all pulses use the
+    problem's radial tables) or a complex128 array [npulse, 6, lmax, 4,
+    blk_nnz] in the loader's layout (see ``gen.pulse_tables``)."""
+
+    def __init__(self, problem: Problem, dts, g: np.ndarray | None = None, h: float = 1.0,
+                 precision: str = "fp64", device: int = 0, chunk_splines: int = 0,
+                 iters_per_launch: int = 0, use_graphs: bool = True):
+        lib = load_library()
+        prec = {"fp64": GADE_PREC_FP64, "mixed": GADE_PREC_MIXED}[precision]
+        dts = np.ascontiguousarray(dts, dtype=np.float64)
+        self.npulse = int(dts.size)
+        gp = None
+        if g is not None:
+            g = _cbuf(g)
+            info = problem.info
+            want = (self.npulse, 6, info["lmax"], 4, info["blk_nnz"])
+            if g.shape != want:
+                raise ValueError(f"radial tables must have shape {want}, got {g.shape}")
+            gp = g.ctypes.data
+        opt = BatchOptions(int(chunk_splines), int(iters_per_launch), 1 if use_graphs else 0)
+        hb = C.c_void_p()
+        _check(lib.gade_batch_create(problem._h, self.npulse, dts.ctypes.data, gp, float(h), prec, int(device),
+                                     C.byref(opt), C.byref(hb)))
+        self._h = hb
+        self.n = problem.n
+        self.problem = problem
+
+    def set_x(self, pulse: int, x: np.ndarray):
+        x = _cbuf(x)
+        if x.shape != (self.n,):
+            raise ValueError(f"state must have {self.n} entries")
+        _check(load_library().gade_batch_set_x(self._h, int(pulse), x.ctypes.data, self.n))
+
+    def get_x(self, pulse: int) -> np.ndarray:
+        x = np.empty(self.n, np.complex128)
+        _check(load_library().gade_batch_get_x(self._h, int(pulse), x.ctypes.data, self.n))
+        return x
+
+    def step(self, ft: np.ndarray, active=None, maxit: int = 500, tol: float = 1e-16) -> list[dict]:
+        """ft: complex128 [npulse, 6]; active: bool/int [npulse] or None (all)."""
+        ft = _cbuf(ft)
+        if ft.shape != (self.npulse, 6):
+            raise ValueError(f"pulse factors must have shape ({self.npulse}, 6)")
+        act = None
+        if active is not None:
+            act = np.ascontiguousarray(active, dtype=np.int32)
+            if act.shape != (self.npulse,):
+                raise ValueError("active must have one entry per pulse")
+        st = (StepStats * self.npulse)()
+        _check(load_library().gade_batch_step(self._h, act.ctypes.data if act is not None else None,
+                                              ft.ctypes.data, int(maxit), float(tol), st))
+        return [st[k].as_dict() for k in range(self.npulse)]
+
+    def info(self) -> dict:
+        bi = BatchInfo()
+        _check(load_library().gade_batch_get_info(self._h, C.byref(bi)))
+        out = {k: getattr(bi, k) for k, _ in BatchInfo._fields_}
+        out["tune_cs"] = list(bi.tune_cs)[:bi.ntune]
+        out["tune_ms"] = list(bi.tune_ms)[:bi.ntune]
+        return out
+
+    def stream(self) -> int:
+        return int(load_library().gade_batch_stream(self._h) or 0)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load_library().gade_batch_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -168,6 +168,57 @@ int gade_solver_apply_dot_noalloc(gade_solver *s, const void *x_dev, const void 
  * from a dependent-chain-free FMA kernel timed with CUDA events. */
 int gade_probe_fp64_peak(int32_t device, double *tflops);
 
+/* ---- batched pulses (no counterpart in the reference) ----------------
+ * Many independent pulses advance together: the reference runs one
+ * dirac_solver process per pulse (tools/dirac_solver.c:496-636), each with
+ * its own dt = T/Ntime and its own radial tables g (they depend on Omega and
+ * Cycles through the Bessel arguments), on the same angular tables, h0 and S.
+ * A batch holds all of them on one GPU; every kernel of a step runs over all
+ * pulses still in the launch list, and each step is replayed from captured
+ * CUDA graphs with BiCGSTAB's control on the device.  Results of pulse k are
+ * those of a gade_solver made with dt[k] and g slice k. */
+typedef struct gade_batch gade_batch;
+
+typedef struct {
+    int32_t chunk_splines;     /* operator row-chunk size in splines, 16..64; 0: autotune */
+    int32_t iters_per_launch;  /* BiCGSTAB iterations per graph replay, 1..64; 0: adaptive */
+    int32_t use_graphs;        /* nonzero: replay captured CUDA graphs; 0: direct launches */
+} gade_batch_options;
+
+typedef struct {
+    int32_t npulse, active;    /* pulses held; pulses in the current launch list */
+    int32_t chunk_splines;     /* row-chunk size in use */
+    int32_t iters_per_launch;  /* current iterations per graph replay */
+    int64_t graph_replays, steps;
+    int32_t ntune;             /* autotuner candidates timed */
+    int32_t tune_cs[4];        /* candidate chunk sizes */
+    float tune_ms[4];          /* their batched operator-apply times */
+    double apply_flops;        /* FP64 flops of one operator apply of one pulse */
+} gade_batch_info;
+
+/* npulse pulses on problem p.  dt[k]: time step of pulse k.  g: NULL (every
+ * pulse uses p's radial tables) or npulse slices of the loader's layout,
+ * [k][a<6][l<lmax][q<4][blk_nnz] complex128 (re, im), q = g0..g3 of
+ * g<q>a<a>l<l>.csr in the base pattern's CSR order; they must be real when
+ * p's are.  precision: GADE_PREC_FP64.  opt may be NULL (autotune, adaptive,
+ * graphs).  Every pulse starts from psi0. */
+int gade_batch_create(const gade_problem *p, int32_t npulse, const double *dt, const double *g, double h,
+                      int32_t precision, int32_t device, const gade_batch_options *opt, gade_batch **out);
+void gade_batch_free(gade_batch *b);
+int gade_batch_set_x(gade_batch *b, int32_t pulse, const double *x, int64_t n);
+int gade_batch_get_x(gade_batch *b, int32_t pulse, double *x, int64_t n);
+
+/* One CN step of every pulse k with active[k] != 0 (active NULL: all), with
+ * pulse factors ft[k*12 .. k*12+11] as in gade_solver_step.  Pulses that
+ * leave the active set leave the launch list (retired pulses cost nothing).
+ * stats (may be NULL) receives npulse records; inactive pulses get zeros.
+ * Returns the first failing pulse's error. */
+int gade_batch_step(gade_batch *b, const int32_t *active, const double *ft, int32_t maxit, double tol,
+                    gade_step_stats *stats);
+int gade_batch_get_info(const gade_batch *b, gade_batch_info *info);
+/* The cudaStream_t (as void*) on which the batch's work is ordered. */
+void *gade_batch_stream(const gade_batch *b);
+
 #ifdef __cplusplus
 }
 #endif
