@@ -137,11 +137,42 @@ struct DevScal {
        solver does, and every predicated kernel of a pulse whose state is not
        the one it waits for returns at entry */
     double tol2rel;        /* tol^2: converged when rr < tol2rel * rhs_sqnorm */
-    int ctl, state, iter, maxit, restarts, pad1;
+    int ctl;               /* 0 host control; 1 BiCGSTAB / refinement record; 2 inner-solve record */
+    int state, iter, maxit, restarts;
+    /* mixed precision, refinement record: the inner solve's pending
+       correction, sweeps and FP64 residual passes so far, inner iterations
+       summed over sweeps, inner iteration limit, stall flag */
+    int pending, sweeps, refinements, inner_total, maxit_in, stalled;
+    double tol2abs;        /* inner-solve record: absolute target for |r|^2 */
 };
 
 enum { ST_RUN = 0, ST_DONE, ST_ZERO, ST_RESTART, ST_BAD };
-enum { PRED_NONE = 0, PRED_RUN, PRED_RESTART };
+/* launch predicates on a pulse's records: a = the refinement / BiCGSTAB
+   record, b = the inner-solve record */
+enum { PRED_NONE = 0, PRED_RUN, PRED_RESTART, PRED_MIX, PRED_FIN, PRED_DONE };
+
+#define MIXED_MAX_SWEEPS 8
+#define MIXED_INNER_TOL 1e-6
+
+__device__ __forceinline__ bool pred_ok(int pred, const DevScal *a, const DevScal *b)
+{
+    if (pred == PRED_NONE) return true;
+    const int st = *(volatile const int *)&a->state;
+    switch (pred) {
+    case PRED_RUN: return st == ST_RUN;
+    case PRED_RESTART: return st == ST_RESTART;
+    case PRED_MIX: return st == ST_RUN && *(volatile const int *)&a->pending == 0;
+    case PRED_FIN: return *(volatile const int *)&a->pending != 0 && *(volatile const int *)&b->state != ST_RUN;
+    default: return st == ST_DONE;
+    }
+}
+
+/* predicate of kernels without a reduction */
+struct BPred {
+    const int *plist;              /* grid y -> pulse (NULL: pulse 0) */
+    DevScal *a, *b;                /* [pulse] records */
+    int pred;
+};
 
 enum { RED_RHS = 0, RED_RESTART, RED_R0V, RED_TS, RED_UPDATE, RED_NONE, RED_DOT_OUT, RED_MIX };
 enum { AX_PLAIN = 0, AX_PARTS, AX_R0V, AX_TS, AX_RHS, AX_RESTART, AX_MIX };
@@ -178,6 +209,7 @@ struct RedP {
     double *out;                   /* RED_DOT_OUT: receives (re, im) of the dot */
     size_t pstride;                /* partials per pulse */
     int pred;                      /* PRED_*: which pulse state the launch works on */
+    DevScal *pa, *pb;              /* [pulse] predicate record (NULL: sc) and second record */
 };
 
 /* Move the reduction targets to pulse `pulse`; false when the pulse's state
@@ -187,9 +219,9 @@ __device__ __forceinline__ bool red_select(RedP &red, int pulse)
     red.sc += pulse;
     red.ticket += pulse;
     red.part += (size_t)pulse * red.pstride;
-    if (red.pred == PRED_NONE) return true;
-    const int st = *(volatile const int *)&red.sc->state;
-    return red.pred == PRED_RUN ? st == ST_RUN : st == ST_RESTART;
+    if (red.pa) red.pa += pulse;
+    if (red.pb) red.pb += pulse;
+    return pred_ok(red.pred, red.pa ? red.pa : red.sc, red.pb ? red.pb : red.sc);
 }
 
 /* Block-wide deterministic sum of NV doubles; result valid in thread 0. */
@@ -240,7 +272,7 @@ __device__ void reduce_finish(RedP red, double (&v)[NRED], double *sh, unsigned 
             sc->rho_prev = make_double2(1.0, 0.0);
             sc->alpha = make_double2(1.0, 0.0);
             sc->w = make_double2(1.0, 0.0);
-            if (sc->ctl) {
+            if (sc->ctl == 1) {
                 /* the early exits of the host loop (tools/bicgstab.c:176-189) */
                 sc->iter = 0;
                 sc->restarts = 0;
@@ -248,13 +280,19 @@ __device__ void reduce_finish(RedP red, double (&v)[NRED], double *sh, unsigned 
                 else if (acc[1] == 0.0) sc->state = ST_ZERO;
                 else if (acc[0] < sc->tol2rel * acc[1] || sc->maxit <= 0) sc->state = ST_DONE;
                 else sc->state = ST_RUN;
+            } else if (sc->ctl == 2) {
+                /* inner solve started from the refinement residual; its
+                   correction is now pending on the refinement record */
+                sc->iter = 0;
+                red.pa->pending = 1;
+                sc->state = (sc->maxit <= 0 || fabs(acc[0]) < (1e-12 * 1e-12) * acc[0]) ? ST_DONE : ST_RUN;
             }
             break;
         case RED_RESTART:
             sc->r0_sqnorm = acc[0];
             sc->rr = acc[0];
             sc->rho = make_double2(acc[0], 0.0);
-            if (sc->ctl) { sc->restarts++; sc->state = ST_RUN; }
+            if (sc->ctl == 1) { sc->restarts++; sc->state = ST_RUN; }
             break;
         case RED_R0V:
             sc->r0v = make_double2(acc[0], acc[1]);
@@ -269,13 +307,20 @@ __device__ void reduce_finish(RedP red, double (&v)[NRED], double *sh, unsigned 
             sc->rr = acc[0];
             sc->rho_prev = sc->rho;
             sc->rho = make_double2(acc[1], acc[2]);
-            if (sc->ctl) {
+            if (sc->ctl == 1) {
                 /* convergence, iteration limit, then the restart test that
                    opens the next iteration (tools/bicgstab.c:205-212,287-293) */
                 if (!isfinite(acc[0])) sc->state = ST_BAD;
                 else if (acc[0] < sc->tol2rel * sc->rhs_sqnorm) sc->state = ST_DONE;
                 else if (++sc->iter >= sc->maxit) sc->state = ST_DONE;
                 else if (fabs(acc[1]) < (1e-12 * 1e-12) * sc->r0_sqnorm) sc->state = ST_RESTART;
+            } else if (sc->ctl == 2) {
+                /* inner solve: stop at the target (or a non-finite value),
+                   at the iteration limit, or on breakdown; refinement follows */
+                sc->iter++;
+                if (!(acc[0] >= sc->tol2abs)) sc->state = ST_DONE;
+                else if (sc->iter >= sc->maxit) sc->state = ST_DONE;
+                else if (fabs(acc[1]) < (1e-12 * 1e-12) * sc->r0_sqnorm) sc->state = ST_DONE;
             }
             break;
         case RED_DOT_OUT:
@@ -283,9 +328,29 @@ __device__ void reduce_finish(RedP red, double (&v)[NRED], double *sh, unsigned 
             red.out[1] = acc[1];
             break;
         case RED_MIX:
-            sc->rhs_sqnorm = acc[0];
-            sc->rr = acc[1];
-            sc->snorm = acc[2];
+            if (sc->ctl != 1) {
+                sc->rhs_sqnorm = acc[0];
+                sc->rr = acc[1];
+                sc->snorm = acc[2];
+            } else {
+                /* the refinement loop's tests after each FP64 residual pass */
+                const int first = sc->refinements == 0;
+                sc->refinements++;
+                sc->rr = acc[1];
+                if (first) { sc->rhs_sqnorm = acc[0]; sc->snorm = acc[2]; }
+                const double b2 = sc->rhs_sqnorm, tol2 = sc->tol2rel * b2;
+                if (first && !isfinite(b2)) sc->state = ST_BAD;
+                else if (first && b2 == 0.0) sc->state = ST_ZERO;
+                else if (!isfinite(acc[1])) sc->state = ST_BAD;
+                else if (acc[1] < tol2) sc->state = ST_DONE;
+                else if (sc->sweeps >= MIXED_MAX_SWEEPS || sc->maxit_in <= 0) {
+                    sc->state = ST_DONE;
+                    sc->stalled = sc->maxit_in > 0;
+                } else {
+                    sc->sweeps++;
+                    red.pb->tol2abs = 0.25 * tol2;
+                }
+            }
             break;
         }
         *red.ticket = 0u;
@@ -867,11 +932,37 @@ __global__ void k_update(long long n, typename Cx<R>::T *x, const typename Cx<R>
 /* ------------------------------------------------------------------ */
 /* mixed precision: complex64 inner solves inside FP64 refinement      */
 /* ------------------------------------------------------------------ */
-/* delta = x - x_prev (linear extrapolation of the state) or 0; FP32 copies */
-__global__ void k_mixed_prep(long long n, const double2 *__restrict__ x, const double2 *__restrict__ xprev,
-                             int have_prev, double2 *__restrict__ d64, float2 *__restrict__ d32,
-                             double2 *__restrict__ w)
+/* Per-pulse base of the mixed-precision vector kernels: grid (CTAs per
+   pulse, pulse slot), n is also the per-pulse stride.  Returns the pulse or
+   -1 when the predicate says the launch has nothing to do for it. */
+__device__ __forceinline__ int bp_select(BPred &bp)
 {
+    const int pulse = bp.plist ? bp.plist[blockIdx.y] : 0;
+    if (bp.a) bp.a += pulse;
+    if (bp.b) bp.b += pulse;
+    return pred_ok(bp.pred, bp.a, bp.b) ? pulse : -1;
+}
+
+/* delta = x - x_prev (linear extrapolation of the state) or 0; FP32 copies.
+   hprev[pulse] (or have_prev when hprev is NULL) says whether x_prev exists.
+   Under device control the first CTA also opens the step's records. */
+__global__ void k_mixed_prep(long long n, const double2 *__restrict__ x, const double2 *__restrict__ xprev,
+                             int have_prev, const int *__restrict__ hprev, double2 *__restrict__ d64,
+                             float2 *__restrict__ d32, double2 *__restrict__ w, BPred bp)
+{
+    const int pulse = bp_select(bp);
+    if (pulse < 0) return;
+    {
+        const long long vo = (long long)pulse * n;
+        x += vo; xprev += vo; d64 += vo; d32 += vo; w += vo;
+    }
+    if (hprev) have_prev = hprev[pulse];
+    if (blockIdx.x == 0 && threadIdx.x == 0 && bp.a && bp.a->ctl == 1) {
+        DevScal *a = bp.a;
+        a->state = ST_RUN; a->pending = 0; a->sweeps = 0; a->refinements = 0; a->inner_total = 0;
+        a->stalled = 0;
+        bp.b->state = ST_DONE;
+    }
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const double2 xv = x[i];
         double2 d = make_double2(0, 0);
@@ -885,10 +976,16 @@ __global__ void k_mixed_prep(long long n, const double2 *__restrict__ x, const d
 /* inner BiCGSTAB start from the FP64 refinement residual:
    e = 0, r = r0 = (complex64) rin, p = v = 0, |r|^2 */
 __global__ void k_inner_init(long long n, const double2 *__restrict__ rin, float2 *e, float2 *r, float2 *r0,
-                             float2 *p, float2 *v, RedP red)
+                             float2 *p, float2 *v, RedP red, const int *plist)
 {
     extern __shared__ unsigned char smem_raw[];
     double *shred = (double *)smem_raw;
+    const int pulse = plist ? plist[blockIdx.y] : 0;
+    if (!red_select(red, pulse)) return;
+    {
+        const long long vo = (long long)pulse * n;
+        rin += vo; e += vo; r += vo; r0 += vo; p += vo; v += vo;
+    }
     double acc[NRED] = {0, 0, 0, 0};
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const double2 rd = rin[i];
@@ -903,8 +1000,15 @@ __global__ void k_inner_init(long long n, const double2 *__restrict__ rin, float
 
 /* delta += e (FP64), refresh the FP32 copy and w = 2 x_n + delta */
 __global__ void k_delta_add(long long n, double2 *__restrict__ d64, const float2 *__restrict__ e,
-                            float2 *__restrict__ d32, const double2 *__restrict__ x, double2 *__restrict__ w)
+                            float2 *__restrict__ d32, const double2 *__restrict__ x, double2 *__restrict__ w,
+                            BPred bp)
 {
+    const int pulse = bp_select(bp);
+    if (pulse < 0) return;
+    {
+        const long long vo = (long long)pulse * n;
+        d64 += vo; e += vo; d32 += vo; x += vo; w += vo;
+    }
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const float2 ev = e[i];
         double2 d = d64[i];
@@ -916,14 +1020,41 @@ __global__ void k_delta_add(long long n, double2 *__restrict__ d64, const float2
     }
 }
 
-/* x_prev = x ; x += delta (FP64) */
+/* x_prev = x ; x += delta (FP64); the pulse now has an x_prev */
 __global__ void k_mixed_finish(long long n, double2 *__restrict__ x, double2 *__restrict__ xprev,
-                               const double2 *__restrict__ d64)
+                               const double2 *__restrict__ d64, int *hprev, BPred bp)
 {
+    const int pulse = bp_select(bp);
+    if (pulse < 0) return;
+    {
+        const long long vo = (long long)pulse * n;
+        x += vo; xprev += vo; d64 += vo;
+    }
+    if (hprev && blockIdx.x == 0 && threadIdx.x == 0) hprev[pulse] = 1;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const double2 xv = x[i], d = d64[i];
         xprev[i] = xv;
         x[i] = make_double2(xv.x + d.x, xv.y + d.y);
+    }
+}
+
+/* After an inner solve and its delta update (device control): the inner
+   estimate of the outer residual certifies the step when it is below the
+   tolerance with margin (the host rule of the single-pulse mixed step);
+   otherwise the next FP64 residual pass decides.  grid (1, pulse slots). */
+__global__ void k_mixed_ctl(BPred bp)
+{
+    if (threadIdx.x != 0) return;
+    if (bp_select(bp) < 0) return;
+    DevScal *a = bp.a;
+    const DevScal *b = bp.b;
+    a->pending = 0;
+    a->inner_total += b->iter;
+    const double rin = b->rr, est = 1e-14 * b->r0_sqnorm;
+    const double tol2 = a->tol2rel * a->rhs_sqnorm;
+    if (isfinite(rin) && rin + est < 0.25 * tol2) {
+        a->rr = rin + est;
+        a->state = ST_DONE;
     }
 }
 
@@ -984,6 +1115,7 @@ struct gade_solver {
     double2 *xprev, *delta64;
     DevScal *d_sc2, *h_sc2;
     int have_prev;
+    int *d_hprev;               /* [pulse] x_prev exists (batched mixed precision) */
 };
 
 static void prof_begin(gade_solver *s, cudaStream_t st)
@@ -1451,6 +1583,7 @@ static int solver_create(const gade_problem *p, int npulse, const double *dts, c
         UP(s->xprev, (const double2 *)nullptr, NP * s->n);
         UP(s->delta64, (const double2 *)nullptr, NP * s->n);
         UP(s->d_sc2, (const DevScal *)nullptr, NP);
+        UP(s->d_hprev, (const int *)nullptr, NP);
         if (cudaMallocHost((void **)&s->h_sc2, sizeof(DevScal) * NP) != cudaSuccess) {
             gade_setup_release(su); gade_solver_free(s); return fail(GADE_ERR_CUDA, "pinned allocation failed");
         }
@@ -1491,11 +1624,12 @@ static OpP op_params(const gade_solver *s)
     return P;
 }
 
-static RedP make_red(const gade_solver *s, DevScal *sc, int kind, int pred)
+static RedP make_red(const gade_solver *s, DevScal *sc, int kind, int pred, DevScal *pa = nullptr,
+                     DevScal *pb = nullptr)
 {
     RedP r;
     r.part = s->d_part; r.ticket = s->d_ticket; r.sc = sc; r.kind = kind; r.out = nullptr;
-    r.pstride = s->pstride; r.pred = pred;
+    r.pstride = s->pstride; r.pred = pred; r.pa = pa; r.pb = pb;
     return r;
 }
 
@@ -1516,10 +1650,10 @@ static void apply_dims(const gade_solver *s, size_t elem, int *nt, size_t *smem)
 }
 
 static int launch_apply(gade_solver *s, const double2 *x, int mode, VecP V, int redkind, cudaStream_t st,
-                        int pred = PRED_NONE)
+                        int pred = PRED_NONE, DevScal *pb = nullptr)
 {
     OpP P = op_params(s);
-    RedP red = make_red(s, s->d_sc, redkind, pred);
+    RedP red = make_red(s, s->d_sc, redkind, pred, nullptr, pb);
     dim3 grid(s->nslot, s->nchunk, s->nblk);
     int nt;
     size_t smem;
@@ -1757,9 +1891,6 @@ static int sync_scal2(gade_solver *s)
     return GADE_OK;
 }
 
-#define MIXED_MAX_SWEEPS 8
-#define MIXED_INNER_TOL 1e-6
-
 /*
  * Mixed-precision CN step.  With delta = x_{n+1} - x_n the CN residual is
  *   r = (S x_n - H x_n) - (S + H)(x_n + delta) = q - A delta,  q = -2 H x_n,
@@ -1781,7 +1912,9 @@ static int mixed_step(gade_solver *s, const double *ft, int32_t maxit, double to
     const size_t rsm = sizeof(double) * NRED * blk;
     if ((rc = launch_tables(s, ft, 3))) return rc;
     prof_begin(s, s->stream);
-    k_mixed_prep<<<grid, blk, 0, s->stream>>>(n, s->x, s->xprev, s->have_prev, s->delta64, s->d32, s->tmp0);
+    const BPred none = {nullptr, s->d_sc, s->d_sc2, PRED_NONE};
+    k_mixed_prep<<<grid, blk, 0, s->stream>>>(n, s->x, s->xprev, s->have_prev, nullptr, s->delta64, s->d32, s->tmp0,
+                                              none);
     prof_end(s, s->stream, 2);
     CKL();
     const double eps2 = 1e-12 * 1e-12;
@@ -1818,7 +1951,8 @@ static int mixed_step(gade_solver *s, const double *ft, int32_t maxit, double to
         {
             RedP red = make_red(s, s->d_sc2, RED_RHS, PRED_NONE);
             prof_begin(s, s->stream);
-            k_inner_init<<<grid, blk, rsm, s->stream>>>(n, s->r, s->e32, s->ri32, s->r032, s->p32, s->v32, red);
+            k_inner_init<<<grid, blk, rsm, s->stream>>>(n, s->r, s->e32, s->ri32, s->r032, s->p32, s->v32, red,
+                                                        nullptr);
             prof_end(s, s->stream, 2);
             CKL();
         }
@@ -1850,7 +1984,7 @@ static int mixed_step(gade_solver *s, const double *ft, int32_t maxit, double to
             if (!(rin >= tol_in2)) break;
         }
         prof_begin(s, s->stream);
-        k_delta_add<<<grid, blk, 0, s->stream>>>(n, s->delta64, s->e32, s->d32, s->x, s->tmp0);
+        k_delta_add<<<grid, blk, 0, s->stream>>>(n, s->delta64, s->e32, s->d32, s->x, s->tmp0, none);
         prof_end(s, s->stream, 2);
         CKL();
         const double est_err2 = 1e-14 * r0in;
@@ -1860,7 +1994,7 @@ static int mixed_step(gade_solver *s, const double *ft, int32_t maxit, double to
         }
     }
     prof_begin(s, s->stream);
-    k_mixed_finish<<<grid, blk, 0, s->stream>>>(n, s->x, s->xprev, s->delta64);
+    k_mixed_finish<<<grid, blk, 0, s->stream>>>(n, s->x, s->xprev, s->delta64, nullptr, none);
     prof_end(s, s->stream, 2);
     CKL();
     s->have_prev = 1;
@@ -2193,10 +2327,58 @@ static int batch_seq_iters(gade_batch *b, int K, cudaStream_t st)
     return GADE_OK;
 }
 
+/* mixed precision: one refinement sweep of every listed pulse that needs
+   one (FP64 residual pass, inner-solve start), K inner complex64 iterations
+   of every pulse whose inner solve runs, then the delta update and the
+   certification test of every pulse whose inner solve has ended */
+static int batch_seq_sweep(gade_batch *b, int K, cudaStream_t st)
+{
+    gade_solver *s = b->s;
+    int rc;
+    const long long n = s->n;
+    const int blk = s->upd_block;
+    const dim3 grid(s->upd_grid, s->nslot);
+    const size_t rsm = sizeof(double) * NRED * blk;
+    VecP R = {};
+    R.out0 = s->r; R.in0 = s->x; R.in1 = s->delta64;
+    if ((rc = launch_apply(s, s->tmp0, AX_MIX, R, RED_MIX, st, PRED_MIX, s->d_sc2))) return rc;
+    {
+        RedP red = make_red(s, s->d_sc2, RED_RHS, PRED_MIX, s->d_sc, nullptr);
+        k_inner_init<<<grid, blk, rsm, st>>>(n, s->r, s->e32, s->ri32, s->r032, s->p32, s->v32, red, s->d_plist);
+        CKL();
+    }
+    for (int it = 0; it < K; it++) {
+        if ((rc = launch_precond32(s, PC_P, s->ri32, s->v32, s->p32, s->y32, s->d_sc2, PRED_RUN))) return rc;
+        VecP A1 = {}; A1.out0 = s->v32; A1.in0 = s->r032;
+        if ((rc = launch_apply32(s, s->y32, AX_R0V, A1, RED_R0V, s->d_sc2, PRED_RUN))) return rc;
+        if ((rc = launch_precond32(s, PC_S, s->ri32, s->v32, s->s32, s->z32, s->d_sc2, PRED_RUN))) return rc;
+        VecP A2 = {}; A2.out0 = s->t32; A2.in0 = s->s32;
+        if ((rc = launch_apply32(s, s->z32, AX_TS, A2, RED_TS, s->d_sc2, PRED_RUN))) return rc;
+        RedP red = make_red(s, s->d_sc2, RED_UPDATE, PRED_RUN);
+        k_update<float><<<grid, blk, rsm, st>>>(n, s->e32, s->y32, s->z32, s->ri32, s->s32, s->t32, s->r032,
+                                                red, s->d_plist);
+        CKL();
+    }
+    const BPred fin = {s->d_plist, s->d_sc, s->d_sc2, PRED_FIN};
+    k_delta_add<<<grid, blk, 0, st>>>(n, s->delta64, s->e32, s->d32, s->x, s->tmp0, fin);
+    CKL();
+    k_mixed_ctl<<<dim3(1, s->nslot), 32, 0, st>>>(fin);
+    CKL();
+    return GADE_OK;
+}
+
 static int batch_seq_first(gade_batch *b, cudaStream_t st)
 {
     gade_solver *s = b->s;
     int rc;
+    if (s->prec == GADE_PREC_MIXED) {
+        if ((rc = launch_table_kernels(s, 3, st))) return rc;
+        const BPred all = {s->d_plist, s->d_sc, s->d_sc2, PRED_NONE};
+        k_mixed_prep<<<dim3(s->upd_grid, s->nslot), s->upd_block, 0, st>>>(
+            s->n, s->x, s->xprev, 0, s->d_hprev, s->delta64, s->d32, s->tmp0, all);
+        CKL();
+        return batch_seq_sweep(b, b->kiter, st);
+    }
     if ((rc = launch_table_kernels(s, 1, st))) return rc;
     VecP V = {};
     V.out0 = s->rhs; V.out1 = s->r; V.out2 = s->r0;
@@ -2218,7 +2400,7 @@ static int batch_run_seq(gade_batch *b, int which)
     cudaStream_t st = b->s->stream;
     switch (which) {
     case 0: return batch_seq_first(b, st);
-    case 1: return batch_seq_iters(b, b->kiter, st);
+    case 1: return b->s->prec == GADE_PREC_MIXED ? batch_seq_sweep(b, b->kiter, st) : batch_seq_iters(b, b->kiter, st);
     default: return batch_seq_restart(b, st);
     }
 }
@@ -2280,8 +2462,14 @@ static int batch_autotune(gade_batch *b, const gade_problem *p)
         float ms = 0;
         for (int rep = 0; rep < 4; rep++) {
             if (rep == 1) CK(cudaEventRecord(e0, s->stream));
-            if (mixed) { V.out0 = s->v32; V.in0 = s->r032; rc = launch_apply32(s, s->y32, AX_R0V, V, RED_R0V, s->d_sc); }
-            else { V.out0 = s->tmp1; rc = launch_apply(s, s->y, AX_R0V, V, RED_R0V, s->stream); }
+            /* mixed precision: one FP64 residual pass and four complex64 applies,
+               about one step's mix */
+            V.out0 = s->tmp1; V.in0 = s->r0;
+            rc = launch_apply(s, s->y, AX_R0V, V, RED_R0V, s->stream);
+            for (int k = 0; mixed && !rc && k < 4; k++) {
+                VecP V32 = {}; V32.out0 = s->v32; V32.in0 = s->r032;
+                rc = launch_apply32(s, s->y32, AX_R0V, V32, RED_R0V, s->d_sc);
+            }
             if (rc) { gade_setup_release(su); cudaEventDestroy(e0); cudaEventDestroy(e1); return rc; }
         }
         CK(cudaEventRecord(e1, s->stream));
@@ -2308,8 +2496,8 @@ extern "C" int gade_batch_create(const gade_problem *p, int32_t npulse, const do
     if (!p || !dt || !out) return fail(GADE_ERR_ARG, "gade_batch_create: NULL argument");
     *out = nullptr;
     if (npulse < 1 || npulse > 65535) return fail(GADE_ERR_ARG, "gade_batch_create: npulse %d out of range", npulse);
-    if (precision != GADE_PREC_FP64)
-        return fail(GADE_ERR_ARG, "gade_batch_create: precision %d is not available for batches", precision);
+    if (precision != GADE_PREC_FP64 && precision != GADE_PREC_MIXED)
+        return fail(GADE_ERR_ARG, "gade_batch_create: unknown precision %d", precision);
     gade_batch_options o = {0, 0, 1};
     if (opt) o = *opt;
     if (o.chunk_splines < 0 || o.chunk_splines > 64 || o.iters_per_launch < 0 || o.iters_per_launch > 64)
@@ -2352,6 +2540,8 @@ extern "C" int gade_batch_set_x(gade_batch *b, int32_t pulse, const double *x, i
     if (n != s->n) return fail(GADE_ERR_ARG, "gade_batch_set_x: size %lld != %lld", (long long)n, s->n);
     CK(cudaSetDevice(s->device));
     CK(cudaMemcpyAsync(s->x + (size_t)pulse * s->n, x, sizeof(double2) * (size_t)n, cudaMemcpyHostToDevice, s->stream));
+    /* a new state has no extrapolation history */
+    if (s->d_hprev) CK(cudaMemsetAsync(s->d_hprev + pulse, 0, sizeof(int), s->stream));
     CK(cudaStreamSynchronize(s->stream));
     return GADE_OK;
 }
@@ -2365,6 +2555,107 @@ extern "C" int gade_batch_get_x(gade_batch *b, int32_t pulse, double *x, int64_t
     CK(cudaSetDevice(s->device));
     CK(cudaMemcpyAsync(x, s->x + (size_t)pulse * s->n, sizeof(double2) * (size_t)n, cudaMemcpyDeviceToHost, s->stream));
     CK(cudaStreamSynchronize(s->stream));
+    return GADE_OK;
+}
+
+/* iterations per captured launch: large enough that most steps need one
+   replay, shrunk only after 32 steps that all needed fewer */
+static void batch_adapt(gade_batch *b, int kmax)
+{
+    if (b->kfixed) return;
+    int want = kmax + 1 > 1 ? kmax + 1 : 1;
+    if (want > 64) want = 64;
+    if (want > b->kwin) b->kwin = want;
+    b->kwin_steps++;
+    if (want > b->kiter || (b->kwin_steps >= 32 && b->kwin < b->kiter)) {
+        b->kiter = want > b->kiter ? want : b->kwin;
+        b->kwin = 0; b->kwin_steps = 0;
+        batch_drop_graphs(b);
+    } else if (b->kwin_steps >= 32) {
+        b->kwin = 0; b->kwin_steps = 0;
+    }
+}
+
+/* Mixed-precision step of the listed pulses: the refinement of the
+   single-pulse mixed step, with its tests in the reduction epilogues. */
+static int batch_step_mixed(gade_batch *b, const std::vector<int> &list, int32_t maxit, double tol,
+                            gade_step_stats *stats)
+{
+    gade_solver *s = b->s;
+    int rc;
+    const int maxit_in = maxit < 50 ? maxit : 50;
+    if (tol != b->tol_c || maxit != b->maxit_c) {
+        for (int k = 0; k < s->npulse; k++) {
+            DevScal &a = s->h_sc[k], &in = s->h_sc2[k];
+            a = DevScal{};
+            a.ctl = 1; a.tol2rel = tol * tol; a.maxit = maxit; a.maxit_in = maxit_in;
+            in = DevScal{};
+            in.ctl = 2; in.maxit = maxit_in; in.state = ST_DONE;
+        }
+        CK(cudaMemcpyAsync(s->d_sc, s->h_sc, sizeof(DevScal) * s->npulse, cudaMemcpyHostToDevice, s->stream));
+        CK(cudaMemcpyAsync(s->d_sc2, s->h_sc2, sizeof(DevScal) * s->npulse, cudaMemcpyHostToDevice, s->stream));
+        b->tol_c = tol; b->maxit_c = maxit;
+    }
+    CK(cudaMemcpyAsync(s->d_coef, s->h_coef, sizeof(double2) * (size_t)s->npulse * s->lmax * 3,
+                       cudaMemcpyHostToDevice, s->stream));
+    if ((rc = batch_launch(b, 0))) return rc;
+    /* each replay advances every running pulse by a sweep or by inner
+       iterations, and both are bounded */
+    const long long guard_max = (long long)(MIXED_MAX_SWEEPS + 1) * (maxit_in + 2) + 2;
+    int kmax = 0;
+    for (long long guard = 0;; guard++) {
+        CK(cudaMemcpyAsync(s->h_sc, s->d_sc, sizeof(DevScal) * s->npulse, cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaMemcpyAsync(s->h_sc2, s->d_sc2, sizeof(DevScal) * s->npulse, cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+        int nrun = 0;
+        for (int k : list) {
+            const DevScal &a = s->h_sc[k], &in = s->h_sc2[k];
+            if (a.err | in.err) {
+                CK(cudaMemsetAsync(&s->d_sc[k].err, 0, sizeof(unsigned), s->stream));
+                CK(cudaMemsetAsync(&s->d_sc2[k].err, 0, sizeof(unsigned), s->stream));
+                return fail(GADE_ERR_CUDA, "pulse %d: device wait timed out (flags %u): TMA copy did not complete",
+                            k, a.err | in.err);
+            }
+            if (a.state == ST_BAD)
+                return fail(GADE_ERR_NUMERIC, "pulse %d: non-finite right-hand side or refinement residual", k);
+            if (a.state == ST_RUN) nrun++;
+            if (in.iter > kmax) kmax = in.iter;
+        }
+        if (!nrun) break;
+        if (guard > guard_max) return fail(GADE_ERR_STATE, "gade_batch_step: refinement control did not terminate");
+        if ((rc = batch_launch(b, 1))) return rc;
+    }
+    {
+        const BPred done = {s->d_plist, s->d_sc, s->d_sc2, PRED_DONE};
+        k_mixed_finish<<<dim3(s->upd_grid, s->nslot), s->upd_block, 0, s->stream>>>(s->n, s->x, s->xprev, s->delta64,
+                                                                                   s->d_hprev, done);
+        CKL();
+    }
+    int stalled = -1;
+    for (int k : list) {
+        const DevScal &a = s->h_sc[k];
+        gade_step_stats st = {};
+        if (a.state == ST_ZERO) {
+            CK(cudaMemsetAsync(s->x + (size_t)k * s->n, 0, sizeof(double2) * (size_t)s->n, s->stream));
+            CK(cudaMemsetAsync(s->d_hprev + k, 0, sizeof(int), s->stream));
+        } else {
+            st.iters = a.inner_total;
+            st.inner_iters = a.inner_total;
+            st.refinements = a.refinements;
+            st.true_residual = sqrt(a.rr / a.rhs_sqnorm);
+            st.tol_error = st.true_residual;
+            st.snorm = a.snorm;
+            if (a.stalled && stalled < 0) stalled = k;
+        }
+        if (stats) stats[k] = st;
+    }
+    b->steps++;
+    batch_adapt(b, kmax);
+    if (stalled >= 0) {
+        const DevScal &a = s->h_sc[stalled];
+        return fail(GADE_ERR_NUMERIC, "pulse %d: mixed-precision refinement stalled at |r|/|b| = %.3e > tol %.3e after %d sweeps",
+                    stalled, sqrt(a.rr / a.rhs_sqnorm), tol, a.sweeps);
+    }
     return GADE_OK;
 }
 
@@ -2390,6 +2681,7 @@ extern "C" int gade_batch_step(gade_batch *b, const int32_t *active, const doubl
             return fail(rc, "pulse %d: %s", k, msg);
         }
     if ((rc = batch_set_list(b, list))) return rc;
+    if (s->prec == GADE_PREC_MIXED) return batch_step_mixed(b, list, maxit, tol, stats);
     if (tol != b->tol_c || maxit != b->maxit_c) {
         /* control values of every pulse (the rest of each record is reset by
            the right-hand-side reduction of the step) */
@@ -2439,23 +2731,8 @@ extern "C" int gade_batch_step(gade_batch *b, const int32_t *active, const doubl
         }
         if (stats) stats[k] = st;
     }
-    CK(cudaStreamSynchronize(s->stream));
     b->steps++;
-    /* iterations per captured launch: large enough that most steps need one
-       replay, shrunk only after 32 steps with fewer iterations */
-    if (!b->kfixed) {
-        int want = kmax + 1 > 1 ? kmax + 1 : 1;
-        if (want > 64) want = 64;
-        if (want > b->kwin) b->kwin = want;
-        b->kwin_steps++;
-        if (want > b->kiter || (b->kwin_steps >= 32 && b->kwin < b->kiter)) {
-            b->kiter = want > b->kiter ? want : b->kwin;
-            b->kwin = 0; b->kwin_steps = 0;
-            batch_drop_graphs(b);
-        } else if (b->kwin_steps >= 32) {
-            b->kwin = 0; b->kwin_steps = 0;
-        }
-    }
+    batch_adapt(b, kmax);
     return GADE_OK;
 }
 

@@ -124,3 +124,48 @@ def test_batch_maxit_and_edge_cases(batch_case, native_lib):
     assert e.value.code == 4
     with pytest.raises(GadeError):
         b.set_x(5, np.zeros(prob.n, complex))
+
+
+def _s_err(p, x, xref):
+    S, _ = O.stationary(p, 0.0)
+    e = x - xref
+    return math.sqrt(abs(np.vdot(e, S @ e).real) / abs(np.vdot(xref, S @ xref).real))
+
+
+def test_mixed_batch_matches_fp64(batch_case, native_lib):
+    """complex64 inner solves in FP64 refinement, batched: every pulse
+    against the FP64 batch at tight tolerance (relative S-norm <= 1e-8)."""
+    d, params, info, prob, tables, dirs = batch_case
+    x64, r64, _ = run_batch(prob, PULSES, tables, tol=1e-12)
+    xm, rm, b = run_batch(prob, PULSES, tables, tol=1e-10, precision="mixed")
+    p = O.load_problem(d, info["lmax"])
+    for k in range(len(PULSES)):
+        assert _s_err(p, xm[k], x64[k]) <= 1e-8, k
+        assert all(r["true_residual"] <= 1e-10 for r in rm[k])
+        assert all(r["refinements"] >= 1 for r in rm[k])
+        sn = np.array([r["snorm"] for r in rm[k]])
+        assert np.all(np.abs(sn - sn[0]) < 1e-7)
+
+
+def test_mixed_batch_matches_single_pulse_mixed(batch_case, native_lib):
+    """A batched mixed pulse follows the single-pulse mixed solver's rules:
+    same refinement passes and inner iterations on the pulse's own inputs."""
+    d, params, info, prob, tables, dirs = batch_case
+    xm, rm, _ = run_batch(prob, PULSES, tables, tol=1e-10, precision="mixed")
+    for k, pk in enumerate(PULSES):
+        T = pk["cycles"] * 2 * math.pi / pk["omega"]
+        xs, rs, _ = run(dirs[k], T, info["lmax"], pk["E0"], pk["omega"], pk["cycles"], pk["ntime"], tol=1e-10,
+                        precision="mixed", write_outputs=False)
+        assert _rel(xm[k], xs) < 1e-8, k
+        assert sum(abs(a["refinements"] - r["refinements"]) for a, r in zip(rm[k], rs)) <= 2
+        assert sum(abs(a["inner_iters"] - r["inner_iters"]) for a, r in zip(rm[k], rs)) <= 4
+
+
+def test_mixed_batch_bit_identical_to_single_pulse_batches(batch_case, native_lib):
+    d, params, info, prob, tables, dirs = batch_case
+    xs, recs, _ = run_batch(prob, PULSES, tables, tol=1e-10, precision="mixed", chunk_splines=16)
+    for k in range(len(PULSES)):
+        x1, r1, _ = run_batch(prob, [PULSES[k]], tables[k:k + 1], tol=1e-10, precision="mixed", chunk_splines=16,
+                              iters_per_launch=3)
+        assert np.array_equal(xs[k], x1[0]), k
+        assert [r["inner_iters"] for r in recs[k]] == [r["inner_iters"] for r in r1[0]]
