@@ -67,6 +67,8 @@ def build(verbose: bool = False) -> str:
                         "-I", INCLUDE, "-c", os.path.join(CSRC, "gade_host.c")],
         "gade_cuda.o": [nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
                         "-I", INCLUDE, "-c", os.path.join(CSRC, "gade_cuda.cu")],
+        "gade_learned.o": [nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
+                           "-I", INCLUDE, "-c", os.path.join(CSRC, "gade_learned.cu")],
         "dirac_solver.o": ["gcc", "-O3", "-std=gnu11", "-Wall", "-I", INCLUDE, "-c",
                            os.path.join(CSRC, "dirac_solver.c")],
     }
@@ -74,7 +76,7 @@ def build(verbose: bool = False) -> str:
     _run_all(cmds)
     lib = library_path()
     _run_all([[nvcc, *ARCH, "-shared", "-o", lib, os.path.join(LIB, "gade_host.o"),
-               os.path.join(LIB, "gade_cuda.o"), "-lcudart", "-lm"]])
+               os.path.join(LIB, "gade_cuda.o"), os.path.join(LIB, "gade_learned.o"), "-lcudart", "-lm"]])
     _run_all([["gcc", "-o", solver_path(), os.path.join(LIB, "dirac_solver.o"), "-L", LIB,
                "-lgade_gb300", "-Wl,-rpath,$ORIGIN", "-L", cuda_lib, "-Wl,-rpath," + cuda_lib,
                "-lcudart", "-lm"]])

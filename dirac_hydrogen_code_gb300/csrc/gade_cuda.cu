@@ -59,6 +59,9 @@ static int fail(int code, const char *fmt, ...)
 
 extern "C" const char *gade_last_error(void) { return g_err; }
 
+/* error reporting of the other translation units of the library */
+extern "C" int gade_set_error(int code, const char *msg) { return fail(code, "%s", msg); }
+
 #define CK(call)                                                                     \
     do {                                                                             \
         cudaError_t e_ = (call);                                                     \
@@ -144,6 +147,7 @@ struct DevScal {
        summed over sweeps, inner iteration limit, stall flag */
     int pending, sweeps, refinements, inner_total, maxit_in, stalled;
     double tol2abs;        /* inner-solve record: absolute target for |r|^2 */
+    double rr_init;        /* refinement record: |r|^2 of the initial guess */
 };
 
 enum { ST_RUN = 0, ST_DONE, ST_ZERO, ST_RESTART, ST_BAD };
@@ -337,7 +341,7 @@ __device__ void reduce_finish(RedP red, double (&v)[NRED], double *sh, unsigned 
                 const int first = sc->refinements == 0;
                 sc->refinements++;
                 sc->rr = acc[1];
-                if (first) { sc->rhs_sqnorm = acc[0]; sc->snorm = acc[2]; }
+                if (first) { sc->rhs_sqnorm = acc[0]; sc->snorm = acc[2]; sc->rr_init = acc[1]; }
                 const double b2 = sc->rhs_sqnorm, tol2 = sc->tol2rel * b2;
                 if (first && !isfinite(b2)) sc->state = ST_BAD;
                 else if (first && b2 == 0.0) sc->state = ST_ZERO;
@@ -948,13 +952,15 @@ __device__ __forceinline__ int bp_select(BPred &bp)
    Under device control the first CTA also opens the step's records. */
 __global__ void k_mixed_prep(long long n, const double2 *__restrict__ x, const double2 *__restrict__ xprev,
                              int have_prev, const int *__restrict__ hprev, double2 *__restrict__ d64,
-                             float2 *__restrict__ d32, double2 *__restrict__ w, BPred bp)
+                             float2 *__restrict__ d32, double2 *__restrict__ w, BPred bp,
+                             const double2 *__restrict__ corr)
 {
     const int pulse = bp_select(bp);
     if (pulse < 0) return;
     {
         const long long vo = (long long)pulse * n;
         x += vo; xprev += vo; d64 += vo; d32 += vo; w += vo;
+        if (corr) corr += vo;
     }
     if (hprev) have_prev = hprev[pulse];
     if (blockIdx.x == 0 && threadIdx.x == 0 && bp.a && bp.a->ctl == 1) {
@@ -966,7 +972,11 @@ __global__ void k_mixed_prep(long long n, const double2 *__restrict__ x, const d
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const double2 xv = x[i];
         double2 d = make_double2(0, 0);
-        if (have_prev) { const double2 xp = xprev[i]; d = make_double2(xv.x - xp.x, xv.y - xp.y); }
+        if (have_prev) {
+            const double2 xp = xprev[i];
+            d = make_double2(xv.x - xp.x, xv.y - xp.y);
+            if (corr) { const double2 c = corr[i]; d.x += c.x; d.y += c.y; }
+        }
         d64[i] = d;
         d32[i] = make_float2((float)d.x, (float)d.y);
         w[i] = make_double2(2.0 * xv.x + d.x, 2.0 * xv.y + d.y);
@@ -1914,7 +1924,7 @@ static int mixed_step(gade_solver *s, const double *ft, int32_t maxit, double to
     prof_begin(s, s->stream);
     const BPred none = {nullptr, s->d_sc, s->d_sc2, PRED_NONE};
     k_mixed_prep<<<grid, blk, 0, s->stream>>>(n, s->x, s->xprev, s->have_prev, nullptr, s->delta64, s->d32, s->tmp0,
-                                              none);
+                                              none, nullptr);
     prof_end(s, s->stream, 2);
     CKL();
     const double eps2 = 1e-12 * 1e-12;
@@ -1935,6 +1945,7 @@ static int mixed_step(gade_solver *s, const double *ft, int32_t maxit, double to
         if (fp64_res == 1) {
             b2 = s->h_sc->rhs_sqnorm;
             st.snorm = s->h_sc->snorm;
+            st.init_residual = sqrt(rr / b2);
             tol2 = tol * tol * b2;
             if (!std::isfinite(b2)) return fail(GADE_ERR_NUMERIC, "non-finite right-hand side");
             if (b2 == 0) {
@@ -2296,6 +2307,8 @@ struct gade_batch {
     long long replays, steps;
     float tune_ms[4];
     int tune_cs[4], ntune;
+    double2 *d_corr;                /* [npulse][n] initial-guess corrections (mixed) */
+    int use_guess;
 };
 
 static void batch_drop_graphs(gade_batch *b)
@@ -2375,7 +2388,7 @@ static int batch_seq_first(gade_batch *b, cudaStream_t st)
         if ((rc = launch_table_kernels(s, 3, st))) return rc;
         const BPred all = {s->d_plist, s->d_sc, s->d_sc2, PRED_NONE};
         k_mixed_prep<<<dim3(s->upd_grid, s->nslot), s->upd_block, 0, st>>>(
-            s->n, s->x, s->xprev, 0, s->d_hprev, s->delta64, s->d32, s->tmp0, all);
+            s->n, s->x, s->xprev, 0, s->d_hprev, s->delta64, s->d32, s->tmp0, all, b->use_guess ? b->d_corr : nullptr);
         CKL();
         return batch_seq_sweep(b, b->kiter, st);
     }
@@ -2645,6 +2658,7 @@ static int batch_step_mixed(gade_batch *b, const std::vector<int> &list, int32_t
             st.true_residual = sqrt(a.rr / a.rhs_sqnorm);
             st.tol_error = st.true_residual;
             st.snorm = a.snorm;
+            st.init_residual = sqrt(a.rr_init / a.rhs_sqnorm);
             if (a.stalled && stalled < 0) stalled = k;
         }
         if (stats) stats[k] = st;
@@ -2754,3 +2768,35 @@ extern "C" int gade_batch_get_info(const gade_batch *b, gade_batch_info *info)
 }
 
 extern "C" void *gade_batch_stream(const gade_batch *b) { return b && b->s ? (void *)b->s->stream : nullptr; }
+
+extern "C" int gade_batch_state_device(gade_batch *b, void **x_dev, int64_t *ld)
+{
+    if (!b || !x_dev || !ld) return fail(GADE_ERR_ARG, "gade_batch_state_device: NULL argument");
+    *x_dev = b->s->x;
+    *ld = b->s->n;
+    return GADE_OK;
+}
+
+extern "C" int gade_batch_guess_buffer(gade_batch *b, void **corr_dev, int64_t *ld)
+{
+    if (!b || !corr_dev || !ld) return fail(GADE_ERR_ARG, "gade_batch_guess_buffer: NULL argument");
+    gade_solver *s = b->s;
+    if (s->prec != GADE_PREC_MIXED) return fail(GADE_ERR_STATE, "gade_batch_guess_buffer: only mixed-precision batches take a guess");
+    if (!b->d_corr) {
+        CK(cudaSetDevice(s->device));
+        int rc = dev_upload(s, &b->d_corr, (const double2 *)nullptr, (size_t)s->npulse * s->n);
+        if (rc) return rc;
+    }
+    *corr_dev = b->d_corr;
+    *ld = s->n;
+    return GADE_OK;
+}
+
+extern "C" int gade_batch_use_guess(gade_batch *b, int32_t enable)
+{
+    if (!b) return fail(GADE_ERR_ARG, "gade_batch_use_guess: NULL batch");
+    if (enable && !b->d_corr) return fail(GADE_ERR_STATE, "gade_batch_use_guess: no guess buffer (gade_batch_guess_buffer)");
+    if ((enable != 0) != (b->use_guess != 0)) batch_drop_graphs(b);
+    b->use_guess = enable != 0;
+    return GADE_OK;
+}

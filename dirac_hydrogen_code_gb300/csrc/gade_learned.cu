@@ -1,0 +1,468 @@
+/*
+ * Learned initial guess: the kernels of a small MLP (BF16 tensor-core GEMMs
+ * with FP32 accumulation, forward and backward, Adam) and of the POD
+ * subspace it predicts in (projection of states onto the basis, expansion of
+ * predicted coefficients into a correction vector).
+ *
+ * The network maps the POD projections of the last four states and the
+ * pulse factors f_a(t) to the POD coefficients of the part of the next state
+ * that linear extrapolation misses (x_{n+1} - 2 x_n + x_{n-1}); the mixed
+ * precision step then starts from x_n + (x_n - x_{n-1}) + U c.  Everything
+ * here works on device pointers handed in by the host; nothing allocates.
+ *
+ * Tensor-core path: mma.sync.aligned.m16n8k16 (BF16 in, FP32 accumulate)
+ * from shared-memory tiles.  The GEMMs of this network are a few MFLOP per
+ * step (M = pulses, N = 256), far from any roofline; the kernels favour
+ * exact, checkable arithmetic over peak throughput.
+ */
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <math.h>
+
+#include "gade.h"
+#include "gade_learned.h"
+
+extern "C" int gade_set_error(int code, const char *msg);
+
+static int lfail(int code, const char *what, cudaError_t e)
+{
+    char buf[512];
+    snprintf(buf, sizeof(buf), "%s: %s", what, cudaGetErrorString(e));
+    return gade_set_error(code, buf);
+}
+
+#define LCK(what)                                                                    \
+    do {                                                                             \
+        cudaError_t e_ = cudaGetLastError();                                         \
+        if (e_ != cudaSuccess) return lfail(GADE_ERR_CUDA, what, e_);                \
+    } while (0)
+
+typedef __nv_bfloat16 bf16;
+
+/* ------------------------------------------------------------------ */
+/* GEMM: C = epi(A B + bias)                                           */
+/* ------------------------------------------------------------------ */
+/* A(i,k) = A[i*sa0 + k*sa1], B(k,j) = B[k*sb0 + j*sb1] (any transposition),
+ * FP32 accumulation.  Epilogue: + bias[j]; times (mask(i,j) > 0) when a
+ * mask is given (ReLU backward); ReLU when act = 1; FP32 result to C and/or
+ * a BF16 copy to C16. */
+#define GBM 64
+#define GBN 64
+#define GBK 32
+#define GPAD 8
+
+__device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4], const uint32_t (&b)[2])
+{
+    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
+                 "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
+                 : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
+__global__ void __launch_bounds__(128) k_gemm_bf16(int M, int N, int K, const bf16 *__restrict__ A, long long sa0,
+                                                   long long sa1, const bf16 *__restrict__ B, long long sb0,
+                                                   long long sb1, const float *__restrict__ bias,
+                                                   const float *__restrict__ mask, long long ldm, int act,
+                                                   float *__restrict__ C, long long ldc, bf16 *__restrict__ C16,
+                                                   long long ldc16)
+{
+    __shared__ __align__(16) bf16 As[GBM][GBK + GPAD];   /* [i][k] */
+    __shared__ __align__(16) bf16 Bs[GBN][GBK + GPAD];   /* [j][k] */
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int wm = warp >> 1, wn = warp & 1;             /* 2 x 2 warps of 32 x 32 */
+    const int i0 = blockIdx.y * GBM, j0 = blockIdx.x * GBN;
+    float acc[2][4][4];
+#pragma unroll
+    for (int a = 0; a < 2; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++)
+#pragma unroll
+            for (int c = 0; c < 4; c++) acc[a][b][c] = 0.f;
+    const bf16 zero = __float2bfloat16(0.f);
+    for (int k0 = 0; k0 < K; k0 += GBK) {
+        for (int e = tid; e < GBM * GBK; e += 128) {
+            const int r = e / GBK, k = e % GBK;
+            const int gi = i0 + r, gk = k0 + k;
+            As[r][k] = (gi < M && gk < K) ? A[gi * sa0 + gk * sa1] : zero;
+        }
+        for (int e = tid; e < GBN * GBK; e += 128) {
+            const int c = e / GBK, k = e % GBK;
+            const int gj = j0 + c, gk = k0 + k;
+            Bs[c][k] = (gj < N && gk < K) ? B[gk * sb0 + gj * sb1] : zero;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < GBK; kk += 16) {
+            uint32_t af[2][4], bfr[4][2];
+            const int kc = kk + (lane & 3) * 2;
+#pragma unroll
+            for (int mt = 0; mt < 2; mt++) {
+                const int r = wm * 32 + mt * 16 + (lane >> 2);
+                af[mt][0] = *(const uint32_t *)&As[r][kc];
+                af[mt][1] = *(const uint32_t *)&As[r + 8][kc];
+                af[mt][2] = *(const uint32_t *)&As[r][kc + 8];
+                af[mt][3] = *(const uint32_t *)&As[r + 8][kc + 8];
+            }
+#pragma unroll
+            for (int nt = 0; nt < 4; nt++) {
+                const int c = wn * 32 + nt * 8 + (lane >> 2);
+                bfr[nt][0] = *(const uint32_t *)&Bs[c][kc];
+                bfr[nt][1] = *(const uint32_t *)&Bs[c][kc + 8];
+            }
+#pragma unroll
+            for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+                for (int nt = 0; nt < 4; nt++) mma_bf16(acc[mt][nt], af[mt], bfr[nt]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int mt = 0; mt < 2; mt++)
+#pragma unroll
+        for (int nt = 0; nt < 4; nt++)
+#pragma unroll
+            for (int h = 0; h < 4; h++) {
+                const int i = i0 + wm * 32 + mt * 16 + (lane >> 2) + (h >= 2 ? 8 : 0);
+                const int j = j0 + wn * 32 + nt * 8 + (lane & 3) * 2 + (h & 1);
+                if (i >= M || j >= N) continue;
+                float v = acc[mt][nt][h];
+                if (bias) v += bias[j];
+                if (mask && !(mask[i * ldm + j] > 0.f)) v = 0.f;
+                if (act == 1) v = v > 0.f ? v : 0.f;
+                if (C) C[i * ldc + j] = v;
+                if (C16) C16[i * ldc16 + j] = __float2bfloat16(v);
+            }
+}
+
+extern "C" int gade_gemm_bf16(int32_t M, int32_t N, int32_t K, const void *A, int64_t sa0, int64_t sa1,
+                              const void *B, int64_t sb0, int64_t sb1, const float *bias, const float *mask,
+                              int64_t ldm, int32_t act, float *C, int64_t ldc, void *C16, int64_t ldc16,
+                              void *stream)
+{
+    if (M < 0 || N < 0 || K < 0 || !A || !B || (!C && !C16) || (act != 0 && act != 1))
+        return gade_set_error(GADE_ERR_ARG, "gade_gemm_bf16: bad argument");
+    if (M == 0 || N == 0) return GADE_OK;
+    dim3 grid((N + GBN - 1) / GBN, (M + GBM - 1) / GBM);
+    k_gemm_bf16<<<grid, 128, 0, (cudaStream_t)stream>>>(M, N, K, (const bf16 *)A, sa0, sa1, (const bf16 *)B, sb0, sb1,
+                                                         bias, mask, ldm, act, C, ldc, (bf16 *)C16, ldc16);
+    LCK("gade_gemm_bf16");
+    return GADE_OK;
+}
+
+/* ------------------------------------------------------------------ */
+/* loss, bias gradient, Adam, conversions                              */
+/* ------------------------------------------------------------------ */
+/* mean squared error over M x N: grad = 2 (out - target) / (M N) (FP32 and
+ * BF16), per-row partial sums of the squared error into rowloss[M] */
+__global__ void k_mse(int M, int N, const float *__restrict__ out, const float *__restrict__ target,
+                      float *__restrict__ grad, bf16 *__restrict__ grad16, double *__restrict__ rowloss)
+{
+    const int i = blockIdx.x;
+    if (i >= M) return;
+    __shared__ double sh[256];
+    double s = 0;
+    const float scale = 2.0f / ((float)M * (float)N);
+    for (int j = threadIdx.x; j < N; j += blockDim.x) {
+        const float d = out[(size_t)i * N + j] - target[(size_t)i * N + j];
+        const float g = scale * d;
+        if (grad) grad[(size_t)i * N + j] = g;
+        grad16[(size_t)i * N + j] = __float2bfloat16(g);
+        s += (double)d * d;
+    }
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) rowloss[i] = sh[0];
+}
+
+extern "C" int gade_mse_grad(int32_t M, int32_t N, const float *out, const float *target, float *grad, void *grad16,
+                             double *rowloss, void *stream)
+{
+    if (M <= 0 || N <= 0 || !out || !target || !grad16 || !rowloss)
+        return gade_set_error(GADE_ERR_ARG, "gade_mse_grad: bad argument");
+    k_mse<<<M, 256, 0, (cudaStream_t)stream>>>(M, N, out, target, grad, (bf16 *)grad16, rowloss);
+    LCK("gade_mse_grad");
+    return GADE_OK;
+}
+
+/* db[j] = sum_i G(i, j) in fixed order */
+__global__ void k_colsum(int M, int N, const float *__restrict__ G, long long ldg, float *__restrict__ db)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= N) return;
+    float s = 0.f;
+    for (int i = 0; i < M; i++) s += G[(size_t)i * ldg + j];
+    db[j] = s;
+}
+
+extern "C" int gade_colsum(int32_t M, int32_t N, const float *G, int64_t ldg, float *db, void *stream)
+{
+    if (M < 0 || N <= 0 || !G || !db) return gade_set_error(GADE_ERR_ARG, "gade_colsum: bad argument");
+    k_colsum<<<(N + 255) / 256, 256, 0, (cudaStream_t)stream>>>(M, N, G, ldg, db);
+    LCK("gade_colsum");
+    return GADE_OK;
+}
+
+/* Adam on FP32 master weights (Kingma & Ba 2015); refreshes the BF16 copy */
+__global__ void k_adam(long long n, float *__restrict__ w, bf16 *__restrict__ w16, const float *__restrict__ g,
+                       float *__restrict__ m, float *__restrict__ v, float lr, float b1, float b2, float eps,
+                       float c1, float c2)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        const float mi = b1 * m[i] + (1.f - b1) * gi;
+        const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+        w[i] = wi;
+        if (w16) w16[i] = __float2bfloat16(wi);
+    }
+}
+
+extern "C" int gade_adam(int64_t n, float *w, void *w16, const float *g, float *m, float *v, float lr, float beta1,
+                         float beta2, float eps, int32_t step, void *stream)
+{
+    if (n <= 0 || !w || !g || !m || !v || step < 1) return gade_set_error(GADE_ERR_ARG, "gade_adam: bad argument");
+    const float c1 = 1.f - powf(beta1, (float)step), c2 = 1.f - powf(beta2, (float)step);
+    int grid = (int)((n + 255) / 256);
+    if (grid > 4096) grid = 4096;
+    k_adam<<<grid, 256, 0, (cudaStream_t)stream>>>(n, w, (bf16 *)w16, g, m, v, lr, beta1, beta2, eps, c1, c2);
+    LCK("gade_adam");
+    return GADE_OK;
+}
+
+__global__ void k_to_bf16(long long n, const float *__restrict__ x, bf16 *__restrict__ y)
+{
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        y[i] = __float2bfloat16(x[i]);
+}
+
+extern "C" int gade_to_bf16(int64_t n, const float *x, void *y, void *stream)
+{
+    if (n < 0 || !x || !y) return gade_set_error(GADE_ERR_ARG, "gade_to_bf16: bad argument");
+    if (n == 0) return GADE_OK;
+    int grid = (int)((n + 255) / 256);
+    if (grid > 4096) grid = 4096;
+    k_to_bf16<<<grid, 256, 0, (cudaStream_t)stream>>>(n, x, (bf16 *)y);
+    LCK("gade_to_bf16");
+    return GADE_OK;
+}
+
+/* ------------------------------------------------------------------ */
+/* POD subspace                                                        */
+/* ------------------------------------------------------------------ */
+/* coef[p][r] = sum_i conj(U[r][i]) x_p[i]: U complex64 [R][n], x complex128
+ * [npulse][n] (stride ldx), FP64 accumulation.  Stage 1: grid (pulse,
+ * chunk); every block stages its x slice in shared memory and 8 warps take
+ * the basis rows; partials [chunk][p][r].  Stage 2 sums chunks in order. */
+#define PJ_L 1024
+__global__ void __launch_bounds__(256) k_pod_partial(int n, int R, const float2 *__restrict__ U,
+                                                     const double2 *__restrict__ x, long long ldx,
+                                                     double2 *__restrict__ part, int npulse)
+{
+    __shared__ double2 xs[PJ_L];
+    const int p = blockIdx.x, ch = blockIdx.y;
+    const int i0 = ch * PJ_L;
+    const int len = n - i0 < PJ_L ? n - i0 : PJ_L;
+    const double2 *xp = x + (size_t)p * ldx + i0;
+    for (int e = threadIdx.x; e < len; e += 256) xs[e] = xp[e];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int r = warp; r < R; r += 8) {
+        const float2 *u = U + (size_t)r * n + i0;
+        double sr = 0, si = 0;
+        for (int e = lane; e < len; e += 32) {
+            const float2 uv = u[e];
+            const double2 xv = xs[e];
+            sr += (double)uv.x * xv.x + (double)uv.y * xv.y;
+            si += (double)uv.x * xv.y - (double)uv.y * xv.x;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            sr += __shfl_xor_sync(0xffffffffu, sr, o);
+            si += __shfl_xor_sync(0xffffffffu, si, o);
+        }
+        if (lane == 0) part[((size_t)ch * npulse + p) * R + r] = make_double2(sr, si);
+    }
+}
+
+__global__ void k_pod_sum(int nch, int npulse, int R, const double2 *__restrict__ part, double2 *__restrict__ coef)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= npulse * R) return;
+    double sr = 0, si = 0;
+    for (int c = 0; c < nch; c++) {
+        const double2 v = part[(size_t)c * npulse * R + t];
+        sr += v.x; si += v.y;
+    }
+    coef[t] = make_double2(sr, si);
+}
+
+extern "C" int gade_pod_project(int64_t n, int32_t R, const void *U, const void *x, int64_t ldx, int32_t npulse,
+                                void *coef, void *scratch, int64_t scratch_bytes, void *stream)
+{
+    if (n <= 0 || n > (1ll << 31) - 1 || R <= 0 || npulse <= 0 || !U || !x || !coef || !scratch)
+        return gade_set_error(GADE_ERR_ARG, "gade_pod_project: bad argument");
+    const int nch = (int)((n + PJ_L - 1) / PJ_L);
+    const int64_t need = (int64_t)nch * npulse * R * (int64_t)sizeof(double2);
+    if (scratch_bytes < need) return gade_set_error(GADE_ERR_ARG, "gade_pod_project: scratch too small");
+    cudaStream_t st = (cudaStream_t)stream;
+    k_pod_partial<<<dim3(npulse, nch), 256, 0, st>>>((int)n, R, (const float2 *)U, (const double2 *)x, ldx,
+                                                     (double2 *)scratch, npulse);
+    LCK("gade_pod_project");
+    k_pod_sum<<<(npulse * R + 255) / 256, 256, 0, st>>>(nch, npulse, R, (const double2 *)scratch, (double2 *)coef);
+    LCK("gade_pod_project");
+    return GADE_OK;
+}
+
+extern "C" int64_t gade_pod_project_scratch(int64_t n, int32_t R, int32_t npulse)
+{
+    return ((n + PJ_L - 1) / PJ_L) * (int64_t)npulse * R * (int64_t)sizeof(double2);
+}
+
+/* y_p[i] = sum_r U[r][i] c_p[r] for the pulses whose scale is nonzero;
+ * complex64 basis and coefficients, complex128 result (stride ldy).  One
+ * thread per i walks the basis rows, so U is read once per launch for all
+ * the pulses of the block's tile. */
+#define EX_PT 8
+__global__ void __launch_bounds__(256) k_pod_expand(int n, int R, const float2 *__restrict__ U,
+                                                    const float2 *__restrict__ c, const float *__restrict__ scale,
+                                                    int npulse, double2 *__restrict__ y, long long ldy)
+{
+    extern __shared__ float2 cs[];                   /* [EX_PT][R] */
+    const int p0 = blockIdx.y * EX_PT;
+    const int np = npulse - p0 < EX_PT ? npulse - p0 : EX_PT;
+    for (int e = threadIdx.x; e < np * R; e += blockDim.x) {
+        const int pp = e / R, r = e % R;
+        const float s = scale ? scale[p0 + pp] : 1.f;
+        const float2 v = c[(size_t)(p0 + pp) * R + r];
+        cs[pp * R + r] = make_float2(s * v.x, s * v.y);
+    }
+    __syncthreads();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float ar[EX_PT], ai[EX_PT];
+#pragma unroll
+        for (int pp = 0; pp < EX_PT; pp++) { ar[pp] = 0.f; ai[pp] = 0.f; }
+        for (int r = 0; r < R; r++) {
+            const float2 u = U[(size_t)r * n + i];
+#pragma unroll
+            for (int pp = 0; pp < EX_PT; pp++) {
+                if (pp < np) {
+                    const float2 cv = cs[pp * R + r];
+                    ar[pp] = fmaf(u.x, cv.x, fmaf(-u.y, cv.y, ar[pp]));
+                    ai[pp] = fmaf(u.x, cv.y, fmaf(u.y, cv.x, ai[pp]));
+                }
+            }
+        }
+#pragma unroll
+        for (int pp = 0; pp < EX_PT; pp++)
+            if (pp < np) y[(size_t)(p0 + pp) * ldy + i] = make_double2(ar[pp], ai[pp]);
+    }
+}
+
+extern "C" int gade_pod_expand(int64_t n, int32_t R, const void *U, const void *c, const float *scale,
+                               int32_t npulse, void *y, int64_t ldy, void *stream)
+{
+    if (n <= 0 || n > (1ll << 31) - 1 || R <= 0 || R > 1024 || npulse <= 0 || !U || !c || !y)
+        return gade_set_error(GADE_ERR_ARG, "gade_pod_expand: bad argument");
+    int gx = (int)((n + 255) / 256);
+    if (gx > 1216) gx = 1216;
+    const size_t smem = sizeof(float2) * EX_PT * (size_t)R;
+    k_pod_expand<<<dim3(gx, (npulse + EX_PT - 1) / EX_PT), 256, smem, (cudaStream_t)stream>>>(
+        (int)n, R, (const float2 *)U, (const float2 *)c, scale, npulse, (double2 *)y, ldy);
+    LCK("gade_pod_expand");
+    return GADE_OK;
+}
+
+/* ------------------------------------------------------------------ */
+/* network input / output                                              */
+/* ------------------------------------------------------------------ */
+/* Input row of pulse p: the projections of the last K states (newest
+ * first; hist is a ring [K][npulse][R] complex128 whose newest slot is
+ * `head`) as (re, im) pairs, then the 12 reals of f(t), all normalised
+ * ((v - mu) / sd) and rounded to BF16: row length K*2R + 12. */
+__global__ void k_features(int npulse, int R, int K, int head, const double2 *__restrict__ hist,
+                           const double *__restrict__ ft, const float *__restrict__ mu, const float *__restrict__ sd,
+                           bf16 *__restrict__ out, float *__restrict__ out32)
+{
+    const int p = blockIdx.x;
+    const int D = K * 2 * R + 12;
+    for (int e = threadIdx.x; e < D; e += blockDim.x) {
+        double v;
+        if (e < K * 2 * R) {
+            const int j = e / (2 * R), q = e % (2 * R);
+            const int slot = (head - j + K) % K;
+            const double2 h = hist[((size_t)slot * npulse + p) * R + q / 2];
+            v = (q & 1) ? h.y : h.x;
+        } else {
+            v = ft[(size_t)p * 12 + (e - K * 2 * R)];
+        }
+        const float z = (float)((v - (double)mu[e]) / (double)sd[e]);
+        out[(size_t)p * D + e] = __float2bfloat16(z);
+        if (out32) out32[(size_t)p * D + e] = z;
+    }
+}
+
+extern "C" int gade_learned_features(int32_t npulse, int32_t R, int32_t K, int32_t head, const void *hist,
+                                     const double *ft, const float *mu, const float *sd, void *out16, float *out32,
+                                     void *stream)
+{
+    if (npulse <= 0 || R <= 0 || K <= 0 || head < 0 || head >= K || !hist || !ft || !mu || !sd || !out16)
+        return gade_set_error(GADE_ERR_ARG, "gade_learned_features: bad argument");
+    k_features<<<npulse, 256, 0, (cudaStream_t)stream>>>(npulse, R, K, head, (const double2 *)hist, ft, mu, sd,
+                                                         (bf16 *)out16, out32);
+    LCK("gade_learned_features");
+    return GADE_OK;
+}
+
+/* Network output of pulse p (2R normalised reals) -> complex64 POD
+ * coefficients c = out * sd + mu.  The correction is kept (scale 1) only
+ * while |c| <= limit * |p_0 - p_1| (the projection of the last state
+ * change): a prediction larger than the step itself is implausible and the
+ * pulse falls back to plain extrapolation (scale 0).  One block per pulse. */
+__global__ void k_outputs(int npulse, int R, int K, int head, const float *__restrict__ out,
+                          const float *__restrict__ mu, const float *__restrict__ sd, const double2 *__restrict__ hist,
+                          float limit, float2 *__restrict__ c, float *__restrict__ scale)
+{
+    const int p = blockIdx.x;
+    __shared__ double sh[2][256];
+    double cn = 0, dn = 0;
+    const int s0 = head, s1 = (head - 1 + K) % K;
+    for (int r = threadIdx.x; r < R; r += blockDim.x) {
+        const float re = out[(size_t)p * 2 * R + 2 * r] * sd[2 * r] + mu[2 * r];
+        const float im = out[(size_t)p * 2 * R + 2 * r + 1] * sd[2 * r + 1] + mu[2 * r + 1];
+        c[(size_t)p * R + r] = make_float2(re, im);
+        cn += (double)re * re + (double)im * im;
+        const double2 a = hist[((size_t)s0 * npulse + p) * R + r], b = hist[((size_t)s1 * npulse + p) * R + r];
+        dn += (a.x - b.x) * (a.x - b.x) + (a.y - b.y) * (a.y - b.y);
+    }
+    sh[0][threadIdx.x] = cn;
+    sh[1][threadIdx.x] = dn;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) { sh[0][threadIdx.x] += sh[0][threadIdx.x + w]; sh[1][threadIdx.x] += sh[1][threadIdx.x + w]; }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const bool ok = isfinite(sh[0][0]) && sh[0][0] <= (double)limit * limit * sh[1][0];
+        scale[p] = ok ? 1.f : 0.f;
+    }
+}
+
+extern "C" int gade_learned_outputs(int32_t npulse, int32_t R, int32_t K, int32_t head, const float *out,
+                                    const float *mu, const float *sd, const void *hist, float limit, void *c,
+                                    float *scale, void *stream)
+{
+    if (npulse <= 0 || R <= 0 || K < 2 || head < 0 || head >= K || !out || !mu || !sd || !hist || !c || !scale)
+        return gade_set_error(GADE_ERR_ARG, "gade_learned_outputs: bad argument");
+    k_outputs<<<npulse, 256, 0, (cudaStream_t)stream>>>(npulse, R, K, head, out, mu, sd, (const double2 *)hist, limit,
+                                                        (float2 *)c, scale);
+    LCK("gade_learned_outputs");
+    return GADE_OK;
+}

@@ -32,7 +32,7 @@ class ProblemInfo(C.Structure):
 class StepStats(C.Structure):
     _fields_ = [("iters", C.c_int32), ("tol_error", C.c_double), ("restarts", C.c_int32),
                 ("refinements", C.c_int32), ("inner_iters", C.c_int32), ("true_residual", C.c_double),
-                ("snorm", C.c_double)]
+                ("snorm", C.c_double), ("init_residual", C.c_double)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -93,6 +93,27 @@ _SIGS = {
                                   C.POINTER(StepStats)]),
     "gade_batch_get_info": (C.c_int, [C.c_void_p, C.POINTER(BatchInfo)]),
     "gade_batch_stream": (C.c_void_p, [C.c_void_p]),
+    "gade_batch_state_device": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_int64)]),
+    "gade_batch_guess_buffer": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_int64)]),
+    "gade_batch_use_guess": (C.c_int, [C.c_void_p, C.c_int32]),
+}
+
+# include/gade_learned.h (device pointers as integers)
+_P = C.c_void_p
+_LEARNED_SIGS = {
+    "gade_gemm_bf16": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, _P, C.c_int64, C.c_int64, _P, C.c_int64,
+                                 C.c_int64, _P, _P, C.c_int64, C.c_int32, _P, C.c_int64, _P, C.c_int64, _P]),
+    "gade_mse_grad": (C.c_int, [C.c_int32, C.c_int32, _P, _P, _P, _P, _P, _P]),
+    "gade_colsum": (C.c_int, [C.c_int32, C.c_int32, _P, C.c_int64, _P, _P]),
+    "gade_adam": (C.c_int, [C.c_int64, _P, _P, _P, _P, _P, C.c_float, C.c_float, C.c_float, C.c_float,
+                            C.c_int32, _P]),
+    "gade_to_bf16": (C.c_int, [C.c_int64, _P, _P, _P]),
+    "gade_pod_project": (C.c_int, [C.c_int64, C.c_int32, _P, _P, C.c_int64, C.c_int32, _P, _P, C.c_int64, _P]),
+    "gade_pod_project_scratch": (C.c_int64, [C.c_int64, C.c_int32, C.c_int32]),
+    "gade_pod_expand": (C.c_int, [C.c_int64, C.c_int32, _P, _P, _P, C.c_int32, _P, C.c_int64, _P]),
+    "gade_learned_features": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, _P, _P, _P, _P, _P, _P, _P]),
+    "gade_learned_outputs": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, _P, _P, _P, _P, C.c_float,
+                                       _P, _P, _P]),
 }
 
 
@@ -110,7 +131,7 @@ def load_library() -> C.CDLL:
         raise GadeError(-1, f"{path} is missing: run dirac_hydrogen_code_gb300.build.build() "
                             "(or __graft_entry__.build()) first; there is no fallback path")
     lib = C.CDLL(path)
-    for name, (res, args) in _SIGS.items():
+    for name, (res, args) in list(_SIGS.items()) + list(_LEARNED_SIGS.items()):
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
@@ -344,6 +365,21 @@ class Batch:
     def stream(self) -> int:
         return int(load_library().gade_batch_stream(self._h) or 0)
 
+    def state_device(self) -> tuple[int, int]:
+        """(device address of the pulse states, per-pulse stride in complex elements)."""
+        p, ld = C.c_void_p(), C.c_int64()
+        _check(load_library().gade_batch_state_device(self._h, C.byref(p), C.byref(ld)))
+        return int(p.value), int(ld.value)
+
+    def guess_buffer(self) -> tuple[int, int]:
+        """(device address of the initial-guess corrections, per-pulse stride)."""
+        p, ld = C.c_void_p(), C.c_int64()
+        _check(load_library().gade_batch_guess_buffer(self._h, C.byref(p), C.byref(ld)))
+        return int(p.value), int(ld.value)
+
+    def use_guess(self, enable: bool = True):
+        _check(load_library().gade_batch_use_guess(self._h, 1 if enable else 0))
+
     def close(self):
         if getattr(self, "_h", None):
             load_library().gade_batch_free(self._h)
@@ -354,3 +390,13 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def call(name: str, *args):
+    """Call a device-pointer entry point of include/gade_learned.h; raise on
+    a nonzero status."""
+    fn = getattr(load_library(), name)
+    rc = fn(*args)
+    if fn.restype is C.c_int:
+        _check(rc)
+    return rc

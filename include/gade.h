@@ -51,6 +51,7 @@ typedef struct {
     int32_t inner_iters;  /* total inner complex64 iterations (mixed)          */
     double  true_residual;/* |b - A x|/|b| at exit (mixed precision only)      */
     double  snorm;        /* x^H S x before the step, FP64 (mixed precision)  */
+    double  init_residual;/* |b - A x0|/|b| of the initial guess, FP64 (mixed)  */
 } gade_step_stats;
 
 /* Message of the last failing call on this thread ("" if none). */
@@ -216,6 +217,20 @@ int gade_batch_get_x(gade_batch *b, int32_t pulse, double *x, int64_t n);
 int gade_batch_step(gade_batch *b, const int32_t *active, const double *ft, int32_t maxit, double tol,
                     gade_step_stats *stats);
 int gade_batch_get_info(const gade_batch *b, gade_batch_info *info);
+
+/* Device address of the pulse states (complex128, pulse k at x_dev + k*ld
+ * elements), for projections and copies on gade_batch_stream.  Valid until
+ * gade_batch_free. */
+int gade_batch_state_device(gade_batch *b, void **x_dev, int64_t *ld);
+
+/* Initial-guess correction of mixed-precision batches: a device buffer of
+ * npulse complex128 vectors (pulse k at corr_dev + k*ld elements), made on
+ * the first call.  While enabled, a step starts pulse k from
+ * x_n + (x_n - x_{n-1}) + corr_k (the learned guess, gade_learned.h) instead
+ * of the linear extrapolation alone; a pulse without an x_{n-1} starts from
+ * x_n.  The FP64 refinement still certifies every step. */
+int gade_batch_guess_buffer(gade_batch *b, void **corr_dev, int64_t *ld);
+int gade_batch_use_guess(gade_batch *b, int32_t enable);
 /* The cudaStream_t (as void*) on which the batch's work is ordered. */
 void *gade_batch_stream(const gade_batch *b);
 

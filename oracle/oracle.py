@@ -8,7 +8,7 @@ through this module.
 
 Parity pin: this restatement is checked against the reference C sources
 themselves, compiled in place with single-rank MPI/BLAS/SuperLU shims by
-``oracle/build_ref.sh`` (outputs in ``oracle/_ref/``), on generated inputs;
+``oracle/build_ref.py`` (outputs in ``oracle/_ref/``), on generated inputs;
 the comparison outputs are committed under ``tests/golden/``.
 
 Functions follow, line by line:

@@ -11,8 +11,8 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def _declared():
-    src = open(os.path.join(ROOT, "include", "gade.h")).read()
+def _declared(header="gade.h"):
+    src = open(os.path.join(ROOT, "include", header)).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
     return sorted(set(re.findall(r"\b(gade_[a-z0-9_]+)\s*\(", src)))
 
@@ -22,8 +22,11 @@ def test_library_exports_every_declared_symbol(native_lib):
     assert len(names) >= 20
     missing = [n for n in names if not hasattr(native_lib, n)]
     assert not missing, missing
-    from dirac_hydrogen_code_gb300.native import _SIGS
+    from dirac_hydrogen_code_gb300.native import _LEARNED_SIGS, _SIGS
     assert set(_SIGS) == set(names), set(names) ^ set(_SIGS)
+    learned = _declared("gade_learned.h")
+    assert not [n for n in learned if not hasattr(native_lib, n)]
+    assert set(_LEARNED_SIGS) == set(learned), set(learned) ^ set(_LEARNED_SIGS)
 
 
 def test_problem_load_on_host(workdirs, native_lib):

@@ -1,0 +1,126 @@
+"""GPU kernels of the learned initial guess against the numpy oracle
+(oracle/mlp.py) and numpy linear algebra:
+
+  * BF16 tensor-core GEMM (every transposition, ragged sizes, bias, ReLU,
+    mask): relative error <= 1e-5 against float64 products of the same
+    BF16-rounded operands (FP32 accumulation)
+  * MLP loss gradients: relative Frobenius error <= 2e-3 per parameter
+    against the oracle with the same BF16 rounding points
+  * Adam: <= 1e-5 relative against the float64 update
+  * POD projection / expansion: <= 1e-6 relative (complex64 basis)
+"""
+import numpy as np
+import pytest
+import torch
+
+import mlp as M
+from dirac_hydrogen_code_gb300 import native
+from dirac_hydrogen_code_gb300.learned import MLP
+
+pytestmark = pytest.mark.gpu
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def _bf(x):
+    return torch.from_numpy(np.asarray(x, np.float32)).cuda().to(torch.bfloat16)
+
+
+@pytest.mark.parametrize("M_,N_,K_", [(1, 8, 16), (37, 70, 45), (130, 256, 1036), (512, 256, 256)])
+@pytest.mark.parametrize("ta,tb", [(False, False), (True, False), (False, True)])
+def test_gemm_bf16(native_lib, M_, N_, K_, ta, tb):
+    rng = np.random.default_rng(M_ + N_ + K_)
+    A = M.bf16(rng.standard_normal((M_, K_)))
+    B = M.bf16(rng.standard_normal((K_, N_)))
+    bias = rng.standard_normal(N_).astype(np.float32)
+    mask = rng.standard_normal((M_, N_)).astype(np.float32)
+    Ad = _bf(A.T.copy() if ta else A)
+    Bd = _bf(B.T.copy() if tb else B)
+    sa = (1, M_) if ta else (K_, 1)
+    sb = (1, K_) if tb else (N_, 1)
+    C = torch.empty(M_, N_, device="cuda")
+    C16 = torch.empty(M_, N_, dtype=torch.bfloat16, device="cuda")
+    bd, md = torch.from_numpy(bias).cuda(), torch.from_numpy(mask).cuda()
+    for act, use_mask in [(0, False), (1, False), (0, True)]:
+        native.call("gade_gemm_bf16", M_, N_, K_, Ad.data_ptr(), *sa, Bd.data_ptr(), *sb, bd.data_ptr(),
+                    md.data_ptr() if use_mask else None, N_, act, C.data_ptr(), N_, C16.data_ptr(), N_, 0)
+        torch.cuda.synchronize()
+        ref = A @ B + bias
+        if use_mask:
+            ref = ref * (mask > 0)
+        if act:
+            ref = np.maximum(ref, 0)
+        got = C.cpu().numpy().astype(np.float64)
+        assert _rel(got, ref) <= 1e-5, (act, use_mask)
+        assert np.array_equal(C16.float().cpu().numpy(), M.bf16(got).astype(np.float32))
+
+
+def test_mlp_gradients_match_oracle(native_lib):
+    din, dh, dout, rows = 1036, 256, 256, 192
+    mlp = MLP(din, dh, dout, max_rows=rows, seed=3)
+    rng = np.random.default_rng(5)
+    X = rng.standard_normal((rows, din))
+    T = rng.standard_normal((rows, dout))
+    with torch.no_grad():
+        for i in range(3):
+            mlp.b[i].copy_(torch.from_numpy(rng.standard_normal(mlp.b[i].numel()) * 0.1))
+    mlp.sync_bf16(0)
+    X16 = _bf(X)
+    Td = torch.from_numpy(T.astype(np.float32)).cuda()
+    out = mlp.forward(X16, rows, 0)
+    mlp.backward(X16, Td, rows, 0)
+    torch.cuda.synchronize()
+    params = dict(W1=mlp.W[0].double().cpu().numpy(), b1=mlp.b[0].double().cpu().numpy(),
+                  W2=mlp.W[1].double().cpu().numpy(), b2=mlp.b[1].double().cpu().numpy(),
+                  W3=mlp.W[2].double().cpu().numpy(), b3=mlp.b[2].double().cpu().numpy())
+    f = M.forward(params, X)
+    assert _rel(out.double().cpu().numpy(), f["out"]) <= 1e-3
+    loss, g = M.loss_and_grads(params, X, T.astype(np.float32).astype(np.float64))
+    assert abs(float(mlp.rowloss[:rows].sum()) / (rows * dout) - loss) <= 1e-4 * loss
+    names = ["W1", "b1", "W2", "b2", "W3", "b3"]
+    for name, gd in zip(names, mlp.grads):
+        assert _rel(gd.double().cpu().numpy(), g[name]) <= 2e-3, name
+
+
+def test_adam_matches_oracle(native_lib):
+    rng = np.random.default_rng(7)
+    n = 5000
+    w, g = rng.standard_normal(n), rng.standard_normal(n)
+    m, v = rng.standard_normal(n) * 0.1, np.abs(rng.standard_normal(n)) * 0.1
+    wd, gd, md, vd = (torch.from_numpy(a.astype(np.float32)).cuda() for a in (w, g, m, v))
+    w16 = torch.empty(n, dtype=torch.bfloat16, device="cuda")
+    native.call("gade_adam", n, wd.data_ptr(), w16.data_ptr(), gd.data_ptr(), md.data_ptr(), vd.data_ptr(),
+                1e-3, 0.9, 0.999, 1e-8, 3, 0)
+    torch.cuda.synchronize()
+    f32 = lambda a: a.astype(np.float32).astype(np.float64)   # noqa: E731
+    wr, mr, vr = M.adam(f32(w), f32(g), f32(m), f32(v), 3)
+    assert _rel(wd.double().cpu().numpy(), wr) <= 1e-6
+    assert _rel(md.double().cpu().numpy(), mr) <= 1e-6 and _rel(vd.double().cpu().numpy(), vr) <= 1e-6
+    assert np.array_equal(w16.float().cpu().numpy(), M.bf16(wd.cpu().numpy()).astype(np.float32))
+
+
+def test_pod_project_and_expand(native_lib):
+    rng = np.random.default_rng(9)
+    n, R, P = 70001, 48, 5
+    U = (rng.standard_normal((R, n)) + 1j * rng.standard_normal((R, n))).astype(np.complex64)
+    X = rng.standard_normal((P, n)) + 1j * rng.standard_normal((P, n))
+    Ud, Xd = torch.from_numpy(U).cuda(), torch.from_numpy(X).cuda()
+    coef = torch.empty(P, R, dtype=torch.complex128, device="cuda")
+    sb = native.call("gade_pod_project_scratch", n, R, P)
+    scratch = torch.empty(sb, dtype=torch.uint8, device="cuda")
+    native.call("gade_pod_project", n, R, Ud.data_ptr(), Xd.data_ptr(), n, P, coef.data_ptr(), scratch.data_ptr(),
+                sb, 0)
+    torch.cuda.synchronize()
+    ref = X @ U.astype(np.complex128).conj().T
+    assert _rel(coef.cpu().numpy(), ref) <= 1e-12
+    c = (rng.standard_normal((P, R)) + 1j * rng.standard_normal((P, R))).astype(np.complex64)
+    scale = np.array([1, 0, 1, 1, 0.5], np.float32)
+    cd, sd = torch.from_numpy(c).cuda(), torch.from_numpy(scale).cuda()
+    y = torch.empty(P, n, dtype=torch.complex128, device="cuda")
+    native.call("gade_pod_expand", n, R, Ud.data_ptr(), cd.data_ptr(), sd.data_ptr(), P, y.data_ptr(), n, 0)
+    torch.cuda.synchronize()
+    yref = (scale[:, None] * c.astype(np.complex128)) @ U.astype(np.complex128)
+    assert _rel(y.cpu().numpy(), yref) <= 1e-6
+    assert np.all(y[1].cpu().numpy() == 0)
