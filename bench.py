@@ -14,6 +14,12 @@ Under torchrun (N>1) every rank runs an independent replica of the pulse on
 its own GPU (the single-pulse solve does not shard; no collectives on the
 data path): ``value`` is total steps/s over the ranks, timed as max over
 ranks between barriers.
+
+Variants (rank 0, in ``variants``): the single pulse in mixed precision
+against plain FP64 at the same residual; 64 seeded pulses of uneven length
+batched on one GPU (FP64 and mixed, pulse-steps/s); the learned initial
+guess at NKappa=16 against the plain and extrapolated guesses on held-out
+pulses (a bounded window of steps per pulse, ``--learned-steps``).
 """
 from __future__ import annotations
 
@@ -263,7 +269,12 @@ def run_ours(args):
 
     variants = None
     if rank == 0 and not args.no_variants:
-        variants = mixed_variant(prob, params, info, T, args, device, torch, native, psi, fts, l2_flush)
+        variants = {"single_pulse_precision": mixed_variant(prob, params, info, T, args, device, torch, native,
+                                                            psi, fts, l2_flush)}
+        if not args.no_batch:
+            variants["batch64"] = batch_variant(prob, params, args, torch)
+        if not args.no_learned:
+            variants["learned_nkappa16"] = learned_variant(args, torch)
 
     # CPU baseline on a bounded sample (rank 0, N=1)
     cpu = None
@@ -358,6 +369,106 @@ def mixed_variant(prob, params, info, T, args, device, torch, native, psi, fts, 
     return out
 
 
+BATCH_SEED = 2026
+
+
+def batch_variant(prob, params, args, torch):
+    """64 pulses on the nondipole medium matrices (Intensity log-uniform in
+    [1, 100], Omega uniform in [10, 100], Cycles in {1, 2, 3}, Ntime =
+    500 Cycles; seeded), each with its own radial tables, dt and LU factors,
+    advanced together: plain FP64 at tol 1e-12 and mixed precision at 1e-10.
+    Timed: batch steps after warm-up, CUDA events on the batch's stream.
+    Unit: pulse-steps/s (one CN step of one pulse)."""
+    import numpy as np
+    from dirac_hydrogen_code_gb300.cn import pulse, step_times
+    from dirac_hydrogen_code_gb300.gen.pulses import draw_pulses, pulse_tables_many
+    from dirac_hydrogen_code_gb300.native import Batch
+    pulses = draw_pulses(64, BATCH_SEED)
+    t0 = time.perf_counter()
+    tables = pulse_tables_many(params, pulses)
+    t_tables = time.perf_counter() - t0
+    grids = [step_times(p["maxtime"], p["ntime"]) for p in pulses]
+    ft = np.zeros((len(pulses), 6), complex)
+    out = {"pulses": len(pulses), "seed": BATCH_SEED, "tables_s": t_tables, "unit": "pulse-steps/s"}
+    for tag, prec, tol in (("fp64_tol1e-12", "fp64", 1e-12), ("mixed_tol1e-10", "mixed", 1e-10)):
+        b = Batch(prob, [g[0] for g in grids], tables, precision=prec)
+        stream = torch.cuda.ExternalStream(b.stream())
+
+        def steps(j0, j1):
+            st = []
+            for j in range(j0, j1):
+                for k, p in enumerate(pulses):
+                    ft[k] = pulse(p["E0"], p["omega"], p["cycles"], grids[k][1][j][1])
+                st.append(b.step(ft, maxit=MAXIT, tol=tol))
+            return st
+        steps(0, args.warmup)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        st = steps(args.warmup, args.warmup + args.batch_steps)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        inf = b.info()
+        out[tag] = {"pulse_steps_per_s": len(pulses) * args.batch_steps / (ms / 1e3),
+                    "ms_per_batch_step": ms / args.batch_steps,
+                    "iters_per_step": float(np.mean([[r["iters"] for r in row] for row in st])),
+                    "fp64_residual_passes_per_step": float(np.mean([[r["refinements"] for r in row] for row in st])),
+                    "graph_replays_per_step": inf["graph_replays"] / max(inf["steps"], 1),
+                    "chunk_splines": inf["chunk_splines"], "autotune_ms": dict(zip(inf["tune_cs"], inf["tune_ms"]))}
+        b.close()
+    out["speedup_mixed_vs_fp64"] = out["mixed_tol1e-10"]["pulse_steps_per_s"] / out["fp64_tol1e-12"]["pulse_steps_per_s"]
+    return out
+
+
+def learned_variant(args, torch):
+    """Learned initial guess at NKappa=16, NMu=8, NSplines=300, Nl=10, 5
+    cycles, Ntime=4000: POD basis (rank <= 128) from 200 seeded snapshots of
+    8 training pulses, MLP 2 x 256 trained on 32 training pulses, evaluated
+    on 8 held-out pulses; pulses differ in Intensity only (log-uniform in
+    [1, 100], seeded), so they share g, dt and the LU factors.  Bounded
+    sample: the first `learned_steps` steps of every pulse.  Compared at the
+    same FP64 residual 1e-10: plain FP64, mixed precision with the
+    extrapolated guess, mixed precision with the learned guess; errors
+    against an FP64 run at tol 1e-12."""
+    import numpy as np
+    from dirac_hydrogen_code_gb300 import learned as L
+    from dirac_hydrogen_code_gb300.gen import CONFIGS, generate
+    from dirac_hydrogen_code_gb300.native import Problem
+    params = CONFIGS["nondipole_large"]
+    W = args.learned_steps
+    out = {"workload": "nondipole_large (NKappa=16)", "steps_per_pulse": W, "unit": "steps/s"}
+    with tempfile.TemporaryDirectory() as d:
+        t0 = time.perf_counter()
+        info = generate(params, d)
+        out["generate_s"] = time.perf_counter() - t0
+        prob = Problem(d, info["lmax"])
+        mk = lambda n, seed: L.intensity_pulses(n, seed, params["Omega"], params["Cycles"], params["Ntime"])  # noqa
+        train, held = mk(32, 101), mk(8, 202)
+        t0 = time.perf_counter()
+        model = L.build_model(prob, train, W, rank=128, nsnap=200, pod_pulses=8, epochs=30, seed=1)
+        out["build_s"] = time.perf_counter() - t0
+        out["model"] = {k: model.history[k] for k in ("rows", "rank", "sv_ratio", "snapshots", "train_s")}
+        out["model"]["loss_first_last"] = [model.history["loss"][0], model.history["loss"][-1]]
+        xr, _, _ = L.run_held_out(prob, held, W, 1e-12, "fp64", None)
+        for tag, prec, mdl in (("fp64_tol1e-10", "fp64", None), ("mixed_tol1e-10", "mixed", None),
+                               ("learned_mixed_tol1e-10", "mixed", model)):
+            xs, st, ms = L.run_held_out(prob, held, W, 1e-10, prec, mdl)
+            err = np.linalg.norm(xs - xr, axis=1) / np.linalg.norm(xr, axis=1)
+            rec = {"steps_per_s": len(held) * W / (ms / 1e3),
+                   "iters_per_step": float(np.mean([[r["iters"] for r in row] for row in st])),
+                   "final_l2_err_vs_fp64_max": float(err.max())}
+            if prec == "mixed":
+                ini = np.array([[r["init_residual"] for r in row] for row in st])[L.K_HIST:]
+                rec["init_residual_mean"] = float(ini.mean())
+                rec["fp64_residual_passes_per_step"] = float(np.mean([[r["refinements"] for r in row] for row in st]))
+            out[tag] = rec
+        prob.close()
+    base = out["fp64_tol1e-10"]["steps_per_s"]
+    out["speedup_vs_fp64"] = {k: out[k]["steps_per_s"] / base for k in ("mixed_tol1e-10", "learned_mixed_tol1e-10")}
+    return out
+
+
 def _ncu_traffic():
     """DRAM bytes per k_apply launch (dram__bytes_read.sum + dram__bytes_write.sum)
     from the committed ncu summary of this workload."""
@@ -402,7 +513,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=4)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--no-variants", action="store_true", help="skip the mixed-precision comparison")
+    ap.add_argument("--no-variants", action="store_true", help="skip every variant (precision, batch, learned)")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 64-pulse batch variant")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-guess variant")
+    ap.add_argument("--batch-steps", type=int, default=10, help="timed batch steps of the batch variant")
+    ap.add_argument("--learned-steps", type=int, default=200, help="steps per pulse of the learned variant")
     ap.add_argument("--profile-precision", default=None, choices=["fp64", "mixed"],
                     help="only run this precision's steps (for profiler captures)")
     args = ap.parse_args()

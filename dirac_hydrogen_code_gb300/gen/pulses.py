@@ -12,6 +12,7 @@ products that ``dump_couplings`` writes, up to summation order.
 from __future__ import annotations
 
 import math
+import os
 
 import numpy as np
 from scipy.special import spherical_jn
@@ -112,3 +113,22 @@ def draw_pulses(n: int, seed: int) -> list[dict]:
     cycles = rng.integers(1, 4, n)
     return [dict(E0=float(E0[i]), omega=float(omega[i]), cycles=int(cycles[i]), ntime=500 * int(cycles[i]),
                  maxtime=int(cycles[i]) * 2 * math.pi / float(omega[i])) for i in range(n)]
+
+
+def _tables_job(args):
+    params, omega, cycles = args
+    return pulse_tables(params, omega, cycles)
+
+
+def pulse_tables_many(params: dict, pulses: list[dict], workers: int | None = None) -> np.ndarray:
+    """[npulse, 6, lmax, 4, blk_nnz] radial tables of many pulses, computed in
+    a pool of fresh (spawned) worker processes: safe after the parent has
+    initialised a GPU."""
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+    jobs = [(params, p["omega"], p["cycles"]) for p in pulses]
+    workers = workers or min(len(jobs), os.cpu_count() or 1)
+    if workers <= 1 or len(jobs) <= 1:
+        return np.stack([_tables_job(j) for j in jobs])
+    with ProcessPoolExecutor(max_workers=workers, mp_context=mp.get_context("spawn")) as ex:
+        return np.stack(list(ex.map(_tables_job, jobs, chunksize=max(1, len(jobs) // (4 * workers)))))
