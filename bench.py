@@ -156,6 +156,16 @@ def run_reference(args):
     return 0
 
 
+def max_over_ranks(t_local: float, dist, device: str) -> float:
+    """The job's time: the slowest rank's (every rank gets it)."""
+    if dist is None:
+        return t_local
+    import torch
+    tt = torch.tensor([t_local], dtype=torch.float64, device=device if dist.get_backend() == "nccl" else "cpu")
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return float(tt.item())
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -216,11 +226,7 @@ def run_ours(args):
     launches = sol.launch_count() - launches0
     clk = clocks.stop()
     ms = sum(a.elapsed_time(b) for a, b in ev)
-    t_local = ms / 1e3
-    if dist is not None:
-        tt = torch.tensor([t_local], device=f"cuda:{device}")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_local = float(tt.item())
+    t_local = max_over_ranks(ms / 1e3, dist, f"cuda:{device}")
     value = ws * args.steps / t_local
 
     # e2e through the C ABI with pinned host buffers
@@ -238,11 +244,7 @@ def run_ours(args):
         native._check(lib.gade_solver_get_x(h, ptr, n))
         idx += 1
     barrier()
-    te = time.perf_counter() - t0
-    if dist is not None:
-        tt = torch.tensor([te], device=f"cuda:{device}")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        te = float(tt.item())
+    te = max_over_ranks(time.perf_counter() - t0, dist, f"cuda:{device}")
     e2e = ws * args.steps / te
 
     # roofline of the dominant kernel (matrix-free operator)

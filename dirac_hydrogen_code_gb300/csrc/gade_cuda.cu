@@ -1217,6 +1217,16 @@ extern "C" int gade_problem_get_psi0(const gade_problem *p, double *psi, int32_t
     return GADE_OK;
 }
 
+extern "C" int gade_problem_get_blocks(const gade_problem *p, int32_t *kappa, int32_t *ang)
+{
+    if (!p) return fail(GADE_ERR_ARG, "gade_problem_get_blocks: NULL problem");
+    for (int r = 0; r < p->nblk; r++) {
+        if (kappa) kappa[r] = p->kappa[r];
+        if (ang) ang[r] = p->perm[r];
+    }
+    return GADE_OK;
+}
+
 extern "C" void gade_problem_free(gade_problem *p) { gade_problem_release(p); }
 
 extern "C" void gade_solver_free(gade_solver *s)

@@ -466,3 +466,60 @@ extern "C" int gade_learned_outputs(int32_t npulse, int32_t R, int32_t K, int32_
     LCK("gade_learned_outputs");
     return GADE_OK;
 }
+
+/* ------------------------------------------------------------------ */
+/* eigenstate projection (populations)                                 */
+/* ------------------------------------------------------------------ */
+/* grid (block row, pulse), 256 threads: the block's slice of x is staged in
+ * shared memory; thread t owns eigenvectors j = t, t+256, ... (consecutive
+ * threads read consecutive W entries); class sums reduce in fixed order. */
+__global__ void __launch_bounds__(256) k_eigproj(int nblk, int B, const int *__restrict__ kidx,
+                                                 const double *__restrict__ W, const double *__restrict__ ev,
+                                                 double e_lo, const double2 *__restrict__ x, long long ldx,
+                                                 double2 *__restrict__ coef, double *__restrict__ classes)
+{
+    extern __shared__ double2 xs[];                  /* [B] */
+    __shared__ double red[4][256];
+    const int r = blockIdx.x, p = blockIdx.y, tid = threadIdx.x;
+    const int k = kidx[r];
+    const double2 *xr = x + (size_t)p * ldx + (size_t)r * B;
+    for (int i = tid; i < B; i += 256) xs[i] = xr[i];
+    __syncthreads();
+    const double *Wk = W + (size_t)k * B * B;
+    const double *E = ev + (size_t)k * B;
+    double acc[4] = {0, 0, 0, 0};
+    for (int j = tid; j < B; j += 256) {
+        double cr = 0, ci = 0;
+        for (int i = 0; i < B; i++) {
+            const double w = Wk[(size_t)i * B + j];
+            cr = fma(w, xs[i].x, cr);
+            ci = fma(-w, xs[i].y, ci);          /* conj(x) */
+        }
+        if (coef) coef[((size_t)p * nblk + r) * B + j] = make_double2(cr, ci);
+        const double pj = cr * cr + ci * ci;
+        const double e = E[j];
+        acc[e < e_lo ? 0 : (e < 0.0 ? 1 : 2)] += pj;
+        acc[3] += pj;
+    }
+    for (int c = 0; c < 4; c++) red[c][tid] = acc[c];
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (tid < w)
+            for (int c = 0; c < 4; c++) red[c][tid] += red[c][tid + w];
+        __syncthreads();
+    }
+    if (tid < 4) classes[((size_t)p * nblk + r) * 4 + tid] = red[tid][0];
+}
+
+extern "C" int gade_eigproj(int32_t npulse, int32_t nblk, int32_t B, const int32_t *block_kidx, const double *W,
+                            const double *evals, double e_lo, const void *x, int64_t ldx, void *coef,
+                            double *classes, void *stream)
+{
+    if (npulse <= 0 || nblk <= 0 || B <= 0 || B > 2048 || npulse > 65535 || !block_kidx || !W || !evals || !x ||
+        !classes)
+        return gade_set_error(GADE_ERR_ARG, "gade_eigproj: bad argument");
+    k_eigproj<<<dim3(nblk, npulse), 256, sizeof(double2) * (size_t)B, (cudaStream_t)stream>>>(
+        nblk, B, block_kidx, W, evals, e_lo, (const double2 *)x, ldx, (double2 *)coef, classes);
+    LCK("gade_eigproj");
+    return GADE_OK;
+}

@@ -63,6 +63,7 @@ _SIGS = {
     "gade_problem_load": (C.c_int, [C.c_char_p, C.c_int32, C.POINTER(C.c_void_p)]),
     "gade_problem_get_info": (C.c_int, [C.c_void_p, C.POINTER(ProblemInfo)]),
     "gade_problem_get_psi0": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "gade_problem_get_blocks": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "gade_problem_free": (None, [C.c_void_p]),
     "gade_solver_create": (C.c_int, [C.c_void_p, C.c_double, C.c_double, C.c_int32, C.c_int32,
                                      C.POINTER(C.c_void_p)]),
@@ -114,6 +115,8 @@ _LEARNED_SIGS = {
     "gade_learned_features": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, _P, _P, _P, _P, _P, _P, _P]),
     "gade_learned_outputs": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, _P, _P, _P, _P, C.c_float,
                                        _P, _P, _P]),
+    "gade_eigproj": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, _P, _P, _P, C.c_double, _P, C.c_int64, _P, _P,
+                               _P]),
 }
 
 
@@ -161,6 +164,14 @@ class Problem:
         _check(lib.gade_problem_get_info(h, C.byref(info)))
         self.info = {k: getattr(info, k) for k, _ in ProblemInfo._fields_}
         self.n = int(info.n)
+
+    def blocks(self) -> tuple[np.ndarray, np.ndarray]:
+        """(kappa, original angular index) of every block row."""
+        nblk = int(self.info["nblk"])
+        kap = np.empty(nblk, np.int32)
+        ang = np.empty(nblk, np.int32)
+        _check(load_library().gade_problem_get_blocks(self._h, kap.ctypes.data, ang.ctypes.data))
+        return kap, ang
 
     def psi0(self) -> tuple[np.ndarray, np.ndarray]:
         psi = np.empty(self.n, np.complex128)

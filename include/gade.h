@@ -65,6 +65,11 @@ int gade_problem_get_info(const gade_problem *p, gade_problem_info *info);
 /* psi0.vec contents: psi (2n doubles) and perm (n int32), either may be NULL.
  * Replaces vec_read/vec_read_perm (tools/dirac_solver.c:68-108). */
 int gade_problem_get_psi0(const gade_problem *p, double *psi, int32_t *perm);
+/* kappa[r] and the original angular index ang[r] of every block row r
+ * (nblk entries each; either may be NULL): the rows of H.csr map to angular
+ * indices through its perm array, kappa = ik(index) (tools/dirac_solver.c:
+ * 396-431, tools/solver_common.c:87-94). */
+int gade_problem_get_blocks(const gade_problem *p, int32_t *kappa, int32_t *ang);
 void gade_problem_free(gade_problem *p);
 
 /* Builds the device solver for a fixed time step dt (and h, always 1 in the

@@ -1,7 +1,8 @@
 /*
  * gade_learned.h - kernels of the learned initial guess (no counterpart in
  * the reference, whose BiCGSTAB always starts from the previous solution,
- * tools/dirac_solver.c:533-551).
+ * tools/dirac_solver.c:533-551) and of the eigenstate projection that turns
+ * states into bound / ionised populations.
  *
  * A POD basis U (R complex64 rows of length n, orthonormal) spans the part
  * of the next state that linear extrapolation misses; an MLP with two hidden
@@ -75,6 +76,19 @@ int gade_learned_features(int32_t npulse, int32_t R, int32_t K, int32_t head, co
  * prediction falls back to plain extrapolation. */
 int gade_learned_outputs(int32_t npulse, int32_t R, int32_t K, int32_t head, const float *out, const float *mu,
                          const float *sd, const void *hist, float limit, void *c, float *scale, void *stream);
+
+/* Eigenstate projection of states (the populations of src/process_output.cpp
+ * with src/hamiltonian.h:1246-1330): for every pulse p < npulse and block
+ * row r, coef[p][r][j] = sum_i conj(x_p[r*B + i]) W[k_r][i][j] with
+ * W = S(k) V(k) (real, [nk][B][B], j fastest) from the per-kappa eigenpairs
+ * of (H0(k), S(k)), k_r = block_kidx[r] (device).  classes[p][r][0..2] =
+ * sum_j |coef|^2 over eigenvalues E < e_lo (negative-energy), e_lo <= E < 0
+ * (bound) and E >= 0 (continuum) of evals [nk][B]; classes[..][3] = total.
+ * x complex128 with pulse stride ldx; coef (may be NULL) complex128
+ * [npulse][nblk][B]; classes double [npulse][nblk][4]; B <= 2048. */
+int gade_eigproj(int32_t npulse, int32_t nblk, int32_t B, const int32_t *block_kidx, const double *W,
+                 const double *evals, double e_lo, const void *x, int64_t ldx, void *coef, double *classes,
+                 void *stream);
 
 #ifdef __cplusplus
 }
