@@ -358,6 +358,11 @@ def mixed_variant(prob, params, info, T, args, device, torch, native, psi, fts, 
                     "kernel_ms_per_step": {k: round(v / args.steps, 4) for k, v in kt.items() if k.endswith("_ms")}}
         sol.close()
     ref = finals["fp64"]
+    eb = _eigenbasis(prob)
+    pref = eb.populations(ref)
+    for tag in ("fp64_tol1e-10", "mixed_tol1e-10"):
+        out[tag]["population_err_vs_fp64"] = _pop_err(eb.populations(finals[tag]), pref)
+    out["fp64"]["populations"] = pref
     chk = native.Solver(prob, dt, 1.0, precision="fp64", device=device)
     chk.set_time(fts[0])
     _, sref, _ = chk.apply(ref, parts=True)
@@ -372,6 +377,18 @@ def mixed_variant(prob, params, info, T, args, device, torch, native, psi, fts, 
 
 
 BATCH_SEED = 2026
+
+
+def _eigenbasis(prob):
+    from dirac_hydrogen_code_gb300.populations import Eigenbasis
+    kap, _ = prob.blocks()
+    return Eigenbasis(prob.workdir, kap)
+
+
+def _pop_err(p, ref):
+    """absolute error of the bound and continuum populations"""
+    return {"bound_abs": abs(p["bound"] - ref["bound"]), "continuum_abs": abs(p["continuum"] - ref["continuum"]),
+            "continuum_rel": abs(p["continuum"] - ref["continuum"]) / max(ref["continuum"], 1e-300)}
 
 
 def batch_variant(prob, params, args, torch):
@@ -392,6 +409,7 @@ def batch_variant(prob, params, args, torch):
     grids = [step_times(p["maxtime"], p["ntime"]) for p in pulses]
     ft = np.zeros((len(pulses), 6), complex)
     out = {"pulses": len(pulses), "seed": BATCH_SEED, "tables_s": t_tables, "unit": "pulse-steps/s"}
+    finals = {}
     for tag, prec, tol in (("fp64_tol1e-12", "fp64", 1e-12), ("mixed_tol1e-10", "mixed", 1e-10)):
         b = Batch(prob, [g[0] for g in grids], tables, precision=prec)
         stream = torch.cuda.ExternalStream(b.stream())
@@ -418,8 +436,15 @@ def batch_variant(prob, params, args, torch):
                     "fp64_residual_passes_per_step": float(np.mean([[r["refinements"] for r in row] for row in st])),
                     "graph_replays_per_step": inf["graph_replays"] / max(inf["steps"], 1),
                     "chunk_splines": inf["chunk_splines"], "autotune_ms": dict(zip(inf["tune_cs"], inf["tune_ms"]))}
+        finals[tag] = np.stack([b.get_x(k) for k in range(len(pulses))])
         b.close()
     out["speedup_mixed_vs_fp64"] = out["mixed_tol1e-10"]["pulse_steps_per_s"] / out["fp64_tol1e-12"]["pulse_steps_per_s"]
+    ref, mx = finals["fp64_tol1e-12"], finals["mixed_tol1e-10"]
+    eb = _eigenbasis(prob)
+    perr = [_pop_err(eb.populations(mx[k]), eb.populations(ref[k])) for k in range(len(pulses))]
+    out["mixed_tol1e-10"]["err_vs_fp64_after_timed_steps"] = {
+        "l2_rel_max": float(np.max(np.linalg.norm(mx - ref, axis=1) / np.linalg.norm(ref, axis=1))),
+        "bound_abs_max": max(e["bound_abs"] for e in perr), "continuum_abs_max": max(e["continuum_abs"] for e in perr)}
     return out
 
 
@@ -453,6 +478,9 @@ def learned_variant(args, torch):
         out["model"] = {k: model.history[k] for k in ("rows", "rank", "sv_ratio", "snapshots", "train_s")}
         out["model"]["loss_first_last"] = [model.history["loss"][0], model.history["loss"][-1]]
         xr, _, _ = L.run_held_out(prob, held, W, 1e-12, "fp64", None)
+        eb = _eigenbasis(prob)
+        pref = [eb.populations(x) for x in xr]
+        out["fp64_tol1e-12_populations_mean"] = {k: float(np.mean([p[k] for p in pref])) for k in pref[0]}
         for tag, prec, mdl in (("fp64_tol1e-10", "fp64", None), ("mixed_tol1e-10", "mixed", None),
                                ("learned_mixed_tol1e-10", "mixed", model)):
             xs, st, ms = L.run_held_out(prob, held, W, 1e-10, prec, mdl)
@@ -460,6 +488,9 @@ def learned_variant(args, torch):
             rec = {"steps_per_s": len(held) * W / (ms / 1e3),
                    "iters_per_step": float(np.mean([[r["iters"] for r in row] for row in st])),
                    "final_l2_err_vs_fp64_max": float(err.max())}
+            perr = [_pop_err(eb.populations(xs[k]), pref[k]) for k in range(len(held))]
+            rec["population_err_vs_fp64_max"] = {"bound_abs": max(e["bound_abs"] for e in perr),
+                                                 "continuum_abs": max(e["continuum_abs"] for e in perr)}
             if prec == "mixed":
                 ini = np.array([[r["init_residual"] for r in row] for row in st])[L.K_HIST:]
                 rec["init_residual_mean"] = float(ini.mean())

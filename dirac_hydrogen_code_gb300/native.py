@@ -160,6 +160,7 @@ class Problem:
         h = C.c_void_p()
         _check(lib.gade_problem_load(os.fsencode(workdir), int(lmax), C.byref(h)))
         self._h = h
+        self.workdir = workdir
         info = ProblemInfo()
         _check(lib.gade_problem_get_info(h, C.byref(info)))
         self.info = {k: getattr(info, k) for k, _ in ProblemInfo._fields_}
