@@ -452,24 +452,58 @@ __global__ void k_tables(TabP T, const double2 *__restrict__ coef)
 /* ------------------------------------------------------------------ */
 /* matrix-free operator                                                */
 /* ------------------------------------------------------------------ */
-/* grid (nchunk, nblk); blockDim = RM (one thread per row of the chunk) */
-template <typename R, bool RC>
+/* Shared-memory carve-up of k_apply, computed the same way on the host
+   (launch size) and in the kernel: every piece starts on a 32-byte boundary. */
+struct ApplySmem {
+    unsigned xr, ub, xs, ds, lcs, angc, ang, shred, total;
+};
+
+__host__ __device__ __forceinline__ unsigned up32(unsigned o) { return (o + 31u) & ~31u; }
+
+__host__ __device__ __forceinline__ ApplySmem apply_smem(int CS, int W, int RM, int AM, int G, unsigned elem,
+                                                         unsigned ang4, int nt)
+{
+    ApplySmem s;
+    unsigned o = 0;
+    s.xr = o;    o = up32(o + elem * CS);
+    s.ub = o;    o = up32(o + 4u * elem * G * CS);
+    s.xs = o;    o = up32(o + elem * CS);
+    s.ds = o;    o = up32(o + elem * CS);
+    s.lcs = o;   o = up32(o + 4u * W * RM);
+    s.angc = o;  o = up32(o + 4u * AM);
+    s.ang = o;   o = up32(o + ang4 * AM);
+    s.shred = o; o = up32(o + 8u * NRED * nt);
+    s.total = o;
+    return s;
+}
+
+/*
+ * grid (pulse slot, row chunk, block row); two threads per output row (HJ
+ * ELL slots each: HJ = (W+1)/2).  Per thread the local columns of its HJ
+ * slots stay in registers for the whole kernel; empty slots point to a zero
+ * column, so the table loops carry no branch and unroll completely.  The four
+ * contracted vectors u, w, u', w' of a column are interleaved (one 32- or
+ * 64-byte record) and so are the four angular factors of a term.
+ */
+template <typename R, bool RC, int HJ>
 __global__ void __launch_bounds__(256) k_apply(OpP P, const typename Cx<R>::T *__restrict__ x, int mode,
                                                VecP V, RedP red)
 {
     typedef typename Cx<R>::T C;
-    extern __shared__ unsigned char smem_raw[];
-    /* G orders per gather phase: 2 (FP64) or 4 (FP32); u, w, u', w' of each */
+    typedef typename std::conditional<RC, typename R4<R>::T, C4<C>>::type A4;   /* a0, a0 k_c, a1, a1 k_c */
+    extern __shared__ __align__(32) unsigned char smem_raw[];
+    /* G orders per gather phase: 2 (FP64) or 4 (FP32) */
     constexpr int G = sizeof(R) == 8 ? 2 : 4;
-    C *xr = (C *)smem_raw;                    /* [CM] */
-    C *ub = xr + P.CM;                        /* [G][4][CM] */
-    C *xs = ub + 4 * G * P.CM;                /* [CM] AX_MIX: x_n slice   */
-    C *ds = xs + P.CM;                        /* [CM] AX_MIX: delta slice */
-    int *lcs = (int *)(ds + P.CM);            /* [W][RM] local column of each ELL slot */
-    int *angc = lcs + P.W * P.RM;             /* [AM] coupled block of each angular term of row r */
-    typedef typename std::conditional<RC, R, C>::type A;
-    A *ang = (A *)(angc + ((P.AM + 3) & ~3)); /* [4][AM] a0, a0 k_c, a1, a1 k_c (16-byte aligned) */
-    double *shred = (double *)(ang + 4 * P.AM); /* [NRED * blockDim] */
+    const int CS = (P.CM + 2) & ~1;           /* column stride: CM + the zero column, even */
+    const ApplySmem L = apply_smem(CS, P.W, P.RM, P.AM, G, sizeof(C), sizeof(A4), blockDim.x);
+    C *xr = (C *)(smem_raw + L.xr);           /* [CS] */
+    C4<C> *ub = (C4<C> *)(smem_raw + L.ub);   /* [G][CS] u, w, u', w' of a column */
+    C *xs = (C *)(smem_raw + L.xs);           /* [CS] AX_MIX: x_n slice   */
+    C *ds = (C *)(smem_raw + L.ds);           /* [CS] AX_MIX: delta slice */
+    int *lcs = (int *)(smem_raw + L.lcs);     /* [W][RM] local column of each ELL slot (CM: empty) */
+    int *angc = (int *)(smem_raw + L.angc);   /* [AM] coupled block of each angular term of row r */
+    A4 *ang = (A4 *)(smem_raw + L.ang);       /* [AM] */
+    double *shred = (double *)(smem_raw + L.shred); /* [NRED * blockDim] */
 
     /* grid (pulse slot, chunk, block row): the slots of one chunk run side by
        side, so the shared maps and angular tables come from L2 for all but one */
@@ -496,20 +530,37 @@ __global__ void __launch_bounds__(256) k_apply(OpP P, const typename Cx<R>::T *_
     const int half = tid / P.RM, trow = tid - half * P.RM;
     const int i = (half < 2 && trow < nrows) ? P.chunk_rows[q * P.RM + trow] : -1;
     const int jb = half == 0 ? 0 : (W + 1) / 2, je = half == 0 ? (W + 1) / 2 : W;
+    const int nj = je - jb;                   /* <= HJ */
     const int *cols = P.chunk_cols + (size_t)q * CM;
-    const int *lcol = lcs;
     const C *xb = x + (size_t)r * B;
     {
         const int *gl = P.chunk_lcol + (size_t)q * W * P.RM;
-        for (int e = tid; e < W * P.RM; e += nt) lcs[e] = gl[e];
+        for (int e = tid; e < W * P.RM; e += nt) { const int v = gl[e]; lcs[e] = v < 0 ? CM : v; }
+        if (tid == 0) {
+            const C z = mk<C>(0, 0);
+            xr[CM] = z; xs[CM] = z; ds[CM] = z;
+            C4<C> z4; z4.a = z; z4.b = z; z4.c = z; z4.d = z;
+            for (int g = 0; g < G; g++) ub[g * CS + CM] = z4;
+        }
     }
     const int ea = P.ang_ptr[r * P.lmax], eb = P.ang_ptr[r * P.lmax + P.lmax];
     for (int e = tid; e < eb - ea; e += nt) {
         angc[e] = P.ang_c[ea + e];
-        ang[e] = ((const A *)P.ang_a0)[ea + e];
-        ang[P.AM + e] = ((const A *)P.ang_a0k)[ea + e];
-        ang[2 * P.AM + e] = ((const A *)P.ang_a1)[ea + e];
-        ang[3 * P.AM + e] = ((const A *)P.ang_a1k)[ea + e];
+        if constexpr (RC) {
+            A4 a;
+            a.a = ((const R *)P.ang_a0)[ea + e];
+            a.b = ((const R *)P.ang_a0k)[ea + e];
+            a.c = ((const R *)P.ang_a1)[ea + e];
+            a.d = ((const R *)P.ang_a1k)[ea + e];
+            ang[e] = a;
+        } else {
+            A4 a;
+            a.a = ((const C *)P.ang_a0)[ea + e];
+            a.b = ((const C *)P.ang_a0k)[ea + e];
+            a.c = ((const C *)P.ang_a1)[ea + e];
+            a.d = ((const C *)P.ang_a1k)[ea + e];
+            ang[e] = a;
+        }
     }
     /* rhs/parts modes need S x and H x apart; A x modes use D = S + i h dt/2 h0 */
     const bool separate = (mode == AX_RHS || mode == AX_PARTS);
@@ -521,37 +572,45 @@ __global__ void __launch_bounds__(256) k_apply(OpP P, const typename Cx<R>::T *_
     }
     __syncthreads();
 
+    /* this thread's slots: local column (CM when empty or past the half);
+       table rows advance by B per slot and stay on the half's last slot
+       past its end (the product is zero there) */
+    int lco[HJ];
+#pragma unroll
+    for (int t = 0; t < HJ; t++) lco[t] = (t < nj && trow < P.RM) ? lcs[(jb + t) * P.RM + trow] : CM;
+    const int jB = jb * B;
+
     C accS = mk<C>(0, 0), accH = mk<C>(0, 0), accD = mk<C>(0, 0);
     if (i >= 0) {
         if (mode == AX_MIX) {
             /* x = w = 2 x_n + delta: S x_n, S delta and (i h dt/2 h0) w */
-            const C *Se = (const C *)P.S_ell + (size_t)kk * W * B;
-            const C *He = (const C *)P.Hst_ell + (size_t)kk * W * B;
-            for (int j = jb; j < je; j++) {
-                const int lc = lcol[j * P.RM + trow];
-                if (lc >= 0) {
-                    const C sv = Se[(size_t)j * B + i];
-                    cfma(accS, sv, xs[lc]);
-                    cfma(accD, sv, ds[lc]);
-                    cfma(accH, He[(size_t)j * B + i], xr[lc]);
-                }
+            const C *Se = (const C *)P.S_ell + (size_t)kk * W * B + i + jB;
+            const C *He = (const C *)P.Hst_ell + (size_t)kk * W * B + i + jB;
+#pragma unroll
+            for (int t = 0; t < HJ; t++) {
+                const int lc = lco[t];
+                const C sv = *Se;
+                cfma(accS, sv, xs[lc]);
+                cfma(accD, sv, ds[lc]);
+                cfma(accH, *He, xr[lc]);
+                if (t + 1 < nj) { Se += B; He += B; }
             }
         } else if (separate) {
-            const C *Se = (const C *)P.S_ell + (size_t)kk * W * B;
-            const C *He = (const C *)P.Hst_ell + (size_t)kk * W * B;
-            for (int j = jb; j < je; j++) {
-                const int lc = lcol[j * P.RM + trow];
-                if (lc >= 0) {
-                    const C xv = xr[lc];
-                    cfma(accS, Se[(size_t)j * B + i], xv);
-                    cfma(accH, He[(size_t)j * B + i], xv);
-                }
+            const C *Se = (const C *)P.S_ell + (size_t)kk * W * B + i + jB;
+            const C *He = (const C *)P.Hst_ell + (size_t)kk * W * B + i + jB;
+#pragma unroll
+            for (int t = 0; t < HJ; t++) {
+                const C xv = xr[lco[t]];
+                cfma(accS, *Se, xv);
+                cfma(accH, *He, xv);
+                if (t + 1 < nj) { Se += B; He += B; }
             }
         } else {
-            const C *De = (const C *)P.D_ell + (size_t)kk * W * B;
-            for (int j = jb; j < je; j++) {
-                const int lc = lcol[j * P.RM + trow];
-                if (lc >= 0) cfma(accS, De[(size_t)j * B + i], xr[lc]);
+            const C *De = (const C *)P.D_ell + (size_t)kk * W * B + i + jB;
+#pragma unroll
+            for (int t = 0; t < HJ; t++) {
+                cfma(accS, *De, xr[lco[t]]);
+                if (t + 1 < nj) De += B;
             }
         }
     }
@@ -565,49 +624,56 @@ __global__ void __launch_bounds__(256) k_apply(OpP P, const typename Cx<R>::T *_
             const int g = item / ncols, c = item - g * ncols;
             const int l = P.act_l[ag + g];
             const int e0 = P.ang_ptr[r * P.lmax + l] - ea, e1 = P.ang_ptr[r * P.lmax + l + 1] - ea;
-            const int gc = cols[c];
-            C U = mk<C>(0, 0), Wv = mk<C>(0, 0), U1 = mk<C>(0, 0), W1 = mk<C>(0, 0);
+            const C *xc = x + cols[c];
+            C4<C> u;
+            u.a = mk<C>(0, 0); u.b = u.a; u.c = u.a; u.d = u.a;
 #pragma unroll 4
             for (int e = e0; e < e1; e++) {
-                const C xv = x[(size_t)angc[e] * B + gc];
+                const C xv = xc[(size_t)angc[e] * B];
+                const A4 a = ang[e];
                 if constexpr (RC) {
-                    rfma(U, ang[e], xv);
-                    rfma(Wv, ang[P.AM + e], xv);
-                    rfma(U1, ang[2 * P.AM + e], xv);
-                    rfma(W1, ang[3 * P.AM + e], xv);
+                    rfma(u.a, a.a, xv);
+                    rfma(u.b, a.b, xv);
+                    rfma(u.c, a.c, xv);
+                    rfma(u.d, a.d, xv);
                 } else {
-                    cfma(U, ang[e], xv);
-                    cfma(Wv, ang[P.AM + e], xv);
-                    cfma(U1, ang[2 * P.AM + e], xv);
-                    cfma(W1, ang[3 * P.AM + e], xv);
+                    cfma(u.a, a.a, xv);
+                    cfma(u.b, a.b, xv);
+                    cfma(u.c, a.c, xv);
+                    cfma(u.d, a.d, xv);
                 }
             }
-            C *u = ub + g * 4 * CM;
-            u[c] = U; u[CM + c] = Wv; u[2 * CM + c] = U1; u[3 * CM + c] = W1;
+            ub[g * CS + c] = u;
         }
         __syncthreads();
         if (i >= 0) {
             for (int g = 0; g < ng; g++) {
                 const int l = P.act_l[ag + g];
-                const C *u0 = ub + g * 4 * CM, *u1 = u0 + CM, *u2 = u1 + CM, *u3 = u2 + CM;
-                const size_t base = ((size_t)l * P.nk + kk) * W * B;
-#pragma unroll 6
-                for (int j = jb; j < je; j++) {
-                    const int lc = lcol[j * P.RM + trow];
-                    if (lc < 0) continue;
-                    if constexpr (RC) {
-                        typedef typename R4<R>::T Q4;
-                        const Q4 m = ((const Q4 *)P.M)[base + (size_t)j * B + i];
-                        rfma(accH, m.a, u0[lc]);
-                        rfma(accH, m.b, u1[lc]);
-                        rfma(accH, m.c, u2[lc]);
-                        rfma(accH, m.d, u3[lc]);
-                    } else {
-                        const C4<C> m = ((const C4<C> *)P.M)[base + (size_t)j * B + i];
-                        cfma(accH, m.a, u0[lc]);
-                        cfma(accH, m.b, u1[lc]);
-                        cfma(accH, m.c, u2[lc]);
-                        cfma(accH, m.d, u3[lc]);
+                const C4<C> *ug = ub + g * CS;
+                if constexpr (RC) {
+                    typedef typename R4<R>::T Q4;
+                    const Q4 *Mt = (const Q4 *)P.M + ((size_t)l * P.nk + kk) * W * B + i + jB;
+#pragma unroll
+                    for (int t = 0; t < HJ; t++) {
+                        const Q4 m = *Mt;
+                        const C4<C> u = ug[lco[t]];
+                        rfma(accH, m.a, u.a);
+                        rfma(accH, m.b, u.b);
+                        rfma(accH, m.c, u.c);
+                        rfma(accH, m.d, u.d);
+                        if (t + 1 < nj) Mt += B;
+                    }
+                } else {
+                    const C4<C> *Mt = (const C4<C> *)P.M + ((size_t)l * P.nk + kk) * W * B + i + jB;
+#pragma unroll
+                    for (int t = 0; t < HJ; t++) {
+                        const C4<C> m = *Mt;
+                        const C4<C> u = ug[lco[t]];
+                        cfma(accH, m.a, u.a);
+                        cfma(accH, m.b, u.b);
+                        cfma(accH, m.c, u.c);
+                        cfma(accH, m.d, u.d);
+                        if (t + 1 < nj) Mt += B;
                     }
                 }
             }
@@ -1376,13 +1442,23 @@ static int solver_create(const gade_problem *p, int npulse, const double *dts, c
     int cs = cs_req > 0 ? cs_req : choose_chunk_splines(p->nblk, p->blkdim, prop.multiProcessorCount);
     int rcode = gade_setup_build(p, dts[0], h, cs, &su, err, sizeof(err));
     if (rcode) return fail(rcode, "%s", err);
+    if (su->W < 29 || su->W > 32) {
+        /* two threads per row with 15 or 16 slots each: degree-7 radial bases give W = 30 */
+        int w = su->W;
+        gade_setup_release(su);
+        return fail(GADE_ERR_ARG, "base pattern rows hold up to %d entries; the operator kernel takes 29 to 32", w);
+    }
     {
         /* operator kernels may use more than the default 48 KB of dynamic shared memory */
         const int lim = 160 * 1024;
-        cudaFuncSetAttribute(k_apply<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-        cudaFuncSetAttribute(k_apply<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-        cudaFuncSetAttribute(k_apply<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-        cudaFuncSetAttribute(k_apply<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<double, true, 15>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<double, false, 15>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<float, true, 15>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<float, false, 15>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<double, true, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<double, false, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<float, true, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<float, false, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
     }
 
     gade_solver *s = new gade_solver();
@@ -1659,14 +1735,25 @@ static void apply_dims(const gade_solver *s, size_t elem, int *nt, size_t *smem)
     int t = 2 * s->RM > s->CM ? 2 * s->RM : s->CM;   /* two threads per row */
     t = (t + 31) / 32 * 32;
     *nt = t;
-    const size_t G = elem == sizeof(double2) ? 2 : 4;
-    const size_t areal = s->rc ? elem / 2 : elem;   /* one angular factor */
-    size_t b = elem * (3 + 4 * G) * (size_t)s->CM            /* xr, u-groups, xs, ds */
-             + sizeof(int) * (size_t)s->W * s->RM           /* ELL local columns */
-             + sizeof(int) * (size_t)((s->AM + 3) & ~3)     /* angular blocks */
-             + areal * 4 * (size_t)s->AM                    /* angular factors */
-             + sizeof(double) * NRED * t;                   /* reduction */
-    *smem = (b + 15) / 16 * 16;
+    const int G = elem == sizeof(double2) ? 2 : 4;
+    const unsigned ang4 = s->rc ? (unsigned)(2 * elem) : (unsigned)(4 * elem);   /* four angular factors */
+    const int CS = (s->CM + 2) & ~1;                 /* columns + the zero column, even */
+    *smem = apply_smem(CS, s->W, s->RM, s->AM, G, (unsigned)elem, ang4, t).total;
+}
+
+/* the operator kernel instance for a precision, coupling class and ELL half width */
+template <typename R>
+static void k_apply_launch(const gade_solver *s, dim3 grid, int nt, size_t smem, cudaStream_t st, OpP P,
+                           const typename Cx<R>::T *x, int mode, VecP V, RedP red)
+{
+    const int hj = (s->W + 1) / 2;
+    if (s->rc) {
+        if (hj == 15) k_apply<R, true, 15><<<grid, nt, smem, st>>>(P, x, mode, V, red);
+        else k_apply<R, true, 16><<<grid, nt, smem, st>>>(P, x, mode, V, red);
+    } else {
+        if (hj == 15) k_apply<R, false, 15><<<grid, nt, smem, st>>>(P, x, mode, V, red);
+        else k_apply<R, false, 16><<<grid, nt, smem, st>>>(P, x, mode, V, red);
+    }
 }
 
 static int launch_apply(gade_solver *s, const double2 *x, int mode, VecP V, int redkind, cudaStream_t st,
@@ -1679,8 +1766,7 @@ static int launch_apply(gade_solver *s, const double2 *x, int mode, VecP V, int 
     size_t smem;
     apply_dims(s, sizeof(double2), &nt, &smem);
     prof_begin(s, st);
-    if (s->rc) k_apply<double, true><<<grid, nt, smem, st>>>(P, x, mode, V, red);
-    else k_apply<double, false><<<grid, nt, smem, st>>>(P, x, mode, V, red);
+    k_apply_launch<double>(s, grid, nt, smem, st, P, x, mode, V, red);
     prof_end(s, st, 0);
     CKL();
     return GADE_OK;
@@ -1877,8 +1963,7 @@ static int launch_apply32(gade_solver *s, const float2 *x, int mode, VecP V, int
     size_t smem;
     apply_dims(s, sizeof(float2), &nt, &smem);
     prof_begin(s, s->stream);
-    if (s->rc) k_apply<float, true><<<grid, nt, smem, s->stream>>>(P, x, mode, V, red);
-    else k_apply<float, false><<<grid, nt, smem, s->stream>>>(P, x, mode, V, red);
+    k_apply_launch<float>(s, grid, nt, smem, s->stream, P, x, mode, V, red);
     prof_end(s, s->stream, 0);
     CKL();
     return GADE_OK;
@@ -2283,8 +2368,7 @@ extern "C" int gade_solver_apply_dot_noalloc(gade_solver *s, const void *x_dev, 
     int nt;
     size_t smem;
     apply_dims(s, sizeof(double2), &nt, &smem);
-    if (s->rc) k_apply<double, true><<<grid, nt, smem, st>>>(P, (const double2 *)x_dev, AX_R0V, V, red);
-    else k_apply<double, false><<<grid, nt, smem, st>>>(P, (const double2 *)x_dev, AX_R0V, V, red);
+    k_apply_launch<double>(s, grid, nt, smem, st, P, (const double2 *)x_dev, AX_R0V, V, red);
     CKL();
     return GADE_OK;
 }
