@@ -198,6 +198,12 @@ struct OpP {
     const int *plist;          /* grid x -> pulse (NULL: pulse 0) */
     long long vstride;         /* complex elements per pulse of every vector */
     size_t mstride, dstride;   /* elements per pulse of M and of Hst / D */
+    /* order split (one pulse only): nsplit CTAs share a (chunk, block row);
+       partial row sums go to split_acc [nsplit][3][nblk*B] and the last CTA
+       to arrive (split_tick [nchunk][nblk]) combines them in split order */
+    int nsplit;
+    void *split_acc;
+    unsigned int *split_tick;
 };
 
 struct VecP {
@@ -485,10 +491,14 @@ __host__ __device__ __forceinline__ ApplySmem apply_smem(int CS, int W, int RM, 
  * contracted vectors u, w, u', w' of a column are interleaved (one 32- or
  * 64-byte record) and so are the four angular factors of a term.
  */
-template <typename R, bool RC, int HJ>
-__global__ void __launch_bounds__(256) k_apply(OpP P, const typename Cx<R>::T *__restrict__ x, int mode,
-                                               VecP V, RedP red)
+template <typename R, bool RC, bool SEP>
+__global__ void __launch_bounds__(256, (sizeof(R) == 8 && SEP) ? 2 : 3)
+    k_apply(OpP P, const typename Cx<R>::T *__restrict__ x, int mode, VecP V, RedP red)
 {
+    /* SEP: modes that need S x and H x apart (AX_RHS, AX_PARTS, AX_MIX, three
+       accumulators); the BiCGSTAB modes use D = S + i h dt/2 h0 and one
+       accumulator, which lets the FP64 instance fit three CTAs per SM */
+    constexpr int HJ = 15;                    /* slots per thread: W in {29, 30} */
     typedef typename Cx<R>::T C;
     typedef typename std::conditional<RC, typename R4<R>::T, C4<C>>::type A4;   /* a0, a0 k_c, a1, a1 k_c */
     extern __shared__ __align__(32) unsigned char smem_raw[];
@@ -522,7 +532,8 @@ __global__ void __launch_bounds__(256) k_apply(OpP P, const typename Cx<R>::T *_
         P.Hst_ell = (const C *)P.Hst_ell + (size_t)pulse * P.dstride;
         P.D_ell = (const C *)P.D_ell + (size_t)pulse * P.dstride;
     }
-    const int q = blockIdx.y, r = blockIdx.z, tid = threadIdx.x, nt = blockDim.x;
+    const int q = blockIdx.y, r = blockIdx.z / P.nsplit, sp = blockIdx.z - r * P.nsplit;
+    const int tid = threadIdx.x, nt = blockDim.x;
     const int B = P.B, W = P.W, CM = P.CM;
     const int kk = P.row_kidx[r];
     const int nrows = P.chunk_nrows[q], ncols = P.chunk_ncols[q];
@@ -562,8 +573,6 @@ __global__ void __launch_bounds__(256) k_apply(OpP P, const typename Cx<R>::T *_
             ang[e] = a;
         }
     }
-    /* rhs/parts modes need S x and H x apart; A x modes use D = S + i h dt/2 h0 */
-    const bool separate = (mode == AX_RHS || mode == AX_PARTS);
 
     for (int c = tid; c < ncols; c += nt) xr[c] = xb[cols[c]];
     if (mode == AX_MIX) {
@@ -581,8 +590,8 @@ __global__ void __launch_bounds__(256) k_apply(OpP P, const typename Cx<R>::T *_
     const int jB = jb * B;
 
     C accS = mk<C>(0, 0), accH = mk<C>(0, 0), accD = mk<C>(0, 0);
-    if (i >= 0) {
-        if (mode == AX_MIX) {
+    if (i >= 0 && sp == 0) {                  /* diagonal blocks: the first split */
+        if (SEP && mode == AX_MIX) {
             /* x = w = 2 x_n + delta: S x_n, S delta and (i h dt/2 h0) w */
             const C *Se = (const C *)P.S_ell + (size_t)kk * W * B + i + jB;
             const C *He = (const C *)P.Hst_ell + (size_t)kk * W * B + i + jB;
@@ -595,7 +604,7 @@ __global__ void __launch_bounds__(256) k_apply(OpP P, const typename Cx<R>::T *_
                 cfma(accH, *He, xr[lc]);
                 if (t + 1 < nj) { Se += B; He += B; }
             }
-        } else if (separate) {
+        } else if (SEP) {
             const C *Se = (const C *)P.S_ell + (size_t)kk * W * B + i + jB;
             const C *He = (const C *)P.Hst_ell + (size_t)kk * W * B + i + jB;
 #pragma unroll
@@ -609,13 +618,20 @@ __global__ void __launch_bounds__(256) k_apply(OpP P, const typename Cx<R>::T *_
             const C *De = (const C *)P.D_ell + (size_t)kk * W * B + i + jB;
 #pragma unroll
             for (int t = 0; t < HJ; t++) {
-                cfma(accS, *De, xr[lco[t]]);
+                cfma(accH, *De, xr[lco[t]]);
                 if (t + 1 < nj) De += B;
             }
         }
     }
 
-    const int a_beg = P.act_ptr[r], a_end = P.act_ptr[r + 1];
+    int a_beg = P.act_ptr[r], a_end = P.act_ptr[r + 1];
+    if (P.nsplit > 1) {                       /* this CTA's share of the orders, whole gather groups */
+        const int na = a_end - a_beg;
+        const int per = ((na + P.nsplit - 1) / P.nsplit + G - 1) / G * G;
+        const int b0 = a_beg + sp * per < a_end ? a_beg + sp * per : a_end;
+        a_end = b0 + per < a_end ? b0 + per : a_end;
+        a_beg = b0;
+    }
     for (int ag = a_beg; ag < a_end; ag += G) {
         const int ng = a_end - ag < G ? a_end - ag : G;
         __syncthreads();     /* staging done / previous group's apply done */
@@ -684,20 +700,58 @@ __global__ void __launch_bounds__(256) k_apply(OpP P, const typename Cx<R>::T *_
     __syncthreads();
     {
         C *xch = (C *)shred;                  /* 3 per row; fits in the reduction buffer */
-        if (half == 1 && i >= 0) { xch[3 * trow] = accS; xch[3 * trow + 1] = accH; xch[3 * trow + 2] = accD; }
-        __syncthreads();
-        if (half == 0 && i >= 0) {
-            accS = cadd(accS, xch[3 * trow]);
-            accH = cadd(accH, xch[3 * trow + 1]);
-            accD = cadd(accD, xch[3 * trow + 2]);
+        if (SEP) {
+            if (half == 1 && i >= 0) { xch[3 * trow] = accS; xch[3 * trow + 1] = accH; xch[3 * trow + 2] = accD; }
+            __syncthreads();
+            if (half == 0 && i >= 0) {
+                accS = cadd(accS, xch[3 * trow]);
+                accH = cadd(accH, xch[3 * trow + 1]);
+                accD = cadd(accD, xch[3 * trow + 2]);
+            }
+        } else {
+            if (half == 1 && i >= 0) xch[trow] = accH;
+            __syncthreads();
+            if (half == 0 && i >= 0) accH = cadd(accH, xch[trow]);
         }
         __syncthreads();
+    }
+    if (P.nsplit > 1) {
+        /* partial row sums of this split; the last split of the (chunk, row)
+           sums all of them in split order and runs the epilogue */
+        __shared__ int split_last;
+        const size_t n = (size_t)P.nblk * B;
+        C *acc = (C *)P.split_acc;
+        const size_t gi = (size_t)r * B + i;
+        if (half == 0 && i >= 0) {
+            acc[((size_t)sp * 3 + 1) * n + gi] = accH;
+            if (SEP) { acc[((size_t)sp * 3) * n + gi] = accS; acc[((size_t)sp * 3 + 2) * n + gi] = accD; }
+        }
+        __threadfence();
+        __syncthreads();
+        if (tid == 0) {
+            const unsigned t = atomicAdd(&P.split_tick[(size_t)q * P.nblk + r], 1u);
+            split_last = (t == (unsigned)P.nsplit - 1u);
+        }
+        __syncthreads();
+        if (!split_last) return;
+        __threadfence();
+        if (half == 0 && i >= 0) {
+            accS = mk<C>(0, 0); accH = accS; accD = accS;
+            for (int k = 0; k < P.nsplit; k++) {
+                accH = cadd(accH, __ldcg(&acc[((size_t)k * 3 + 1) * n + gi]));
+                if (SEP) {
+                    accS = cadd(accS, __ldcg(&acc[((size_t)k * 3) * n + gi]));
+                    accD = cadd(accD, __ldcg(&acc[((size_t)k * 3 + 2) * n + gi]));
+                }
+            }
+        }
+        if (tid == 0) P.split_tick[(size_t)q * P.nblk + r] = 0u;
     }
     /* epilogue */
     double v[NRED] = {0, 0, 0, 0};
     if (half == 0 && i >= 0) {
         const size_t gi = (size_t)r * B + i;
-        const C ax = cadd(accH, accS);
+        const C ax = SEP ? cadd(accH, accS) : accH;
         switch (mode) {
         case AX_PLAIN:
             ((C *)V.out0)[gi] = ax;
@@ -751,7 +805,7 @@ __global__ void __launch_bounds__(256) k_apply(OpP P, const typename Cx<R>::T *_
         }
         }
     }
-    if (red.kind != RED_NONE) reduce_finish(red, v, shred, gridDim.y * gridDim.z, blockIdx.z * gridDim.y + blockIdx.y);
+    if (red.kind != RED_NONE) reduce_finish(red, v, shred, gridDim.y * (gridDim.z / P.nsplit), r * gridDim.y + q);
 }
 
 /* ------------------------------------------------------------------ */
@@ -1192,6 +1246,12 @@ struct gade_solver {
     DevScal *d_sc2, *h_sc2;
     int have_prev;
     int *d_hprev;               /* [pulse] x_prev exists (batched mixed precision) */
+    /* order split of the operator kernel (single-pulse solvers) */
+    int nsplit;
+    void *d_split_acc;
+    unsigned int *d_split_tick;
+    int nsm;
+    float split_ms[5];          /* autotuner: FP64 (+ complex64) apply time per split count */
 };
 
 static void prof_begin(gade_solver *s, cudaStream_t st)
@@ -1442,23 +1502,23 @@ static int solver_create(const gade_problem *p, int npulse, const double *dts, c
     int cs = cs_req > 0 ? cs_req : choose_chunk_splines(p->nblk, p->blkdim, prop.multiProcessorCount);
     int rcode = gade_setup_build(p, dts[0], h, cs, &su, err, sizeof(err));
     if (rcode) return fail(rcode, "%s", err);
-    if (su->W < 29 || su->W > 32) {
-        /* two threads per row with 15 or 16 slots each: degree-7 radial bases give W = 30 */
+    if (su->W < 29 || su->W > 30) {
+        /* two threads per row with 15 slots each: degree-7 radial bases give W = 30 */
         int w = su->W;
         gade_setup_release(su);
-        return fail(GADE_ERR_ARG, "base pattern rows hold up to %d entries; the operator kernel takes 29 to 32", w);
+        return fail(GADE_ERR_ARG, "base pattern rows hold up to %d entries; the operator kernel takes 29 or 30", w);
     }
     {
         /* operator kernels may use more than the default 48 KB of dynamic shared memory */
         const int lim = 160 * 1024;
-        cudaFuncSetAttribute(k_apply<double, true, 15>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-        cudaFuncSetAttribute(k_apply<double, false, 15>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-        cudaFuncSetAttribute(k_apply<float, true, 15>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-        cudaFuncSetAttribute(k_apply<float, false, 15>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-        cudaFuncSetAttribute(k_apply<double, true, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-        cudaFuncSetAttribute(k_apply<double, false, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-        cudaFuncSetAttribute(k_apply<float, true, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-        cudaFuncSetAttribute(k_apply<float, false, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<double, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<double, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<float, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<float, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<double, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<double, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<float, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<float, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
     }
 
     gade_solver *s = new gade_solver();
@@ -1476,6 +1536,8 @@ static int solver_create(const gade_problem *p, int npulse, const double *dts, c
     }
     s->bw = su->bw; s->Bp = su->Bp; s->nch = su->nch;
     s->dt = dts[0]; s->h = h; s->blk_nnz = p->blk_nnz;
+    s->nsm = prop.multiProcessorCount;
+    s->nsplit = 1;
     s->upd_block = 256;
     {
         /* vector kernels: at most two CTAs per SM, no more than one thread per element */
@@ -1694,16 +1756,7 @@ static int solver_create(const gade_problem *p, int npulse, const double *dts, c
     return GADE_OK;
 }
 
-extern "C" int gade_solver_create(const gade_problem *p, double dt, double h, int32_t precision,
-                                  int32_t device, gade_solver **out)
-{
-    if (!p || !out) return fail(GADE_ERR_ARG, "gade_solver_create: NULL argument");
-    *out = nullptr;
-    if (precision != GADE_PREC_FP64 && precision != GADE_PREC_MIXED)
-        return fail(GADE_ERR_ARG, "gade_solver_create: unknown precision %d", precision);
-    if (!(dt > 0) || !std::isfinite(dt)) return fail(GADE_ERR_ARG, "gade_solver_create: dt must be finite and > 0");
-    return solver_create(p, 1, &dt, nullptr, h, precision, device, 0, out);
-}
+
 
 static OpP op_params(const gade_solver *s)
 {
@@ -1717,6 +1770,8 @@ static OpP op_params(const gade_solver *s)
     P.chunk_cols = s->d_chunk_cols; P.chunk_lcol = s->d_chunk_lcol;
     P.M = s->d_M; P.S_ell = s->d_S_ell; P.Hst_ell = s->d_Hst_ell; P.D_ell = s->d_D_ell;
     P.plist = s->d_plist; P.vstride = s->n; P.mstride = s->mstride; P.dstride = s->dstride;
+    P.nsplit = s->nsplit > 1 ? s->nsplit : 1;
+    P.split_acc = s->d_split_acc; P.split_tick = s->d_split_tick;
     return P;
 }
 
@@ -1741,18 +1796,18 @@ static void apply_dims(const gade_solver *s, size_t elem, int *nt, size_t *smem)
     *smem = apply_smem(CS, s->W, s->RM, s->AM, G, (unsigned)elem, ang4, t).total;
 }
 
-/* the operator kernel instance for a precision, coupling class and ELL half width */
+/* the operator kernel instance for a precision, coupling class and mode class */
 template <typename R>
 static void k_apply_launch(const gade_solver *s, dim3 grid, int nt, size_t smem, cudaStream_t st, OpP P,
                            const typename Cx<R>::T *x, int mode, VecP V, RedP red)
 {
-    const int hj = (s->W + 1) / 2;
+    const bool sep = mode == AX_RHS || mode == AX_PARTS || mode == AX_MIX;
     if (s->rc) {
-        if (hj == 15) k_apply<R, true, 15><<<grid, nt, smem, st>>>(P, x, mode, V, red);
-        else k_apply<R, true, 16><<<grid, nt, smem, st>>>(P, x, mode, V, red);
+        if (sep) k_apply<R, true, true><<<grid, nt, smem, st>>>(P, x, mode, V, red);
+        else k_apply<R, true, false><<<grid, nt, smem, st>>>(P, x, mode, V, red);
     } else {
-        if (hj == 15) k_apply<R, false, 15><<<grid, nt, smem, st>>>(P, x, mode, V, red);
-        else k_apply<R, false, 16><<<grid, nt, smem, st>>>(P, x, mode, V, red);
+        if (sep) k_apply<R, false, true><<<grid, nt, smem, st>>>(P, x, mode, V, red);
+        else k_apply<R, false, false><<<grid, nt, smem, st>>>(P, x, mode, V, red);
     }
 }
 
@@ -1761,7 +1816,7 @@ static int launch_apply(gade_solver *s, const double2 *x, int mode, VecP V, int 
 {
     OpP P = op_params(s);
     RedP red = make_red(s, s->d_sc, redkind, pred, nullptr, pb);
-    dim3 grid(s->nslot, s->nchunk, s->nblk);
+    dim3 grid(s->nslot, s->nchunk, s->nblk * P.nsplit);
     int nt;
     size_t smem;
     apply_dims(s, sizeof(double2), &nt, &smem);
@@ -1958,7 +2013,7 @@ static int launch_apply32(gade_solver *s, const float2 *x, int mode, VecP V, int
 {
     OpP P = op_params32(s);
     RedP red = make_red(s, sc, redkind, pred);
-    dim3 grid(s->nslot, s->nchunk, s->nblk);
+    dim3 grid(s->nslot, s->nchunk, s->nblk * P.nsplit);
     int nt;
     size_t smem;
     apply_dims(s, sizeof(float2), &nt, &smem);
@@ -1981,6 +2036,65 @@ static int launch_precond32(gade_solver *s, int mode, const float2 *in0, const f
     else k_precond_tma<float, 32><<<grid, 128, smem, s->stream>>>(Q, mode, in0, in1, io, out, sc);
     prof_end(s, s->stream, 1);
     CKL();
+    return GADE_OK;
+}
+
+/*
+ * Order split of a single pulse: when one pulse's (chunk, block row) CTAs
+ * are too few to balance the SMs, 2-4 CTAs share each (chunk, block row),
+ * each with a part of the Bessel orders.  The count is chosen by timing the
+ * operator (FP64, plus two complex64 applies in mixed precision) for every
+ * candidate on the zeroed tables, once at creation.
+ */
+static int choose_split(gade_solver *s)
+{
+    const long long ctas = (long long)s->nchunk * s->nblk;
+    int maxs = (int)((8LL * s->nsm + ctas - 1) / ctas);
+    if (maxs > 4) maxs = 4;
+    for (int k = 0; k < 5; k++) s->split_ms[k] = 0.f;
+    if (maxs <= 1) return GADE_OK;
+    int rc;
+    if ((rc = dev_upload(s, (double2 **)&s->d_split_acc, (const double2 *)nullptr, (size_t)maxs * 3 * s->n))) return rc;
+    if ((rc = dev_upload(s, &s->d_split_tick, (const unsigned *)nullptr, (size_t)ctas))) return rc;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int best_ns = 1;
+    for (int ns = 1; ns <= maxs; ns++) {
+        s->nsplit = ns;
+        for (int rep = 0; rep < 4; rep++) {
+            if (rep == 1) CK(cudaEventRecord(e0, s->stream));
+            VecP V = {}; V.out0 = s->tmp1; V.in0 = s->r0;
+            rc = launch_apply(s, s->x, AX_R0V, V, RED_R0V, s->stream);
+            for (int k = 0; !rc && s->prec == GADE_PREC_MIXED && k < 2; k++) {
+                VecP V32 = {}; V32.out0 = s->v32; V32.in0 = s->r032;
+                rc = launch_apply32(s, s->y32, AX_R0V, V32, RED_R0V, s->d_sc, PRED_NONE);
+            }
+            if (rc) { cudaEventDestroy(e0); cudaEventDestroy(e1); return rc; }
+        }
+        CK(cudaEventRecord(e1, s->stream));
+        CK(cudaEventSynchronize(e1));
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        s->split_ms[ns] = ms / 3;
+        if (ms < best * 0.98f) { best = ms; best_ns = ns; }    /* more splits only for a clear gain */
+    }
+    cudaEventDestroy(e0); cudaEventDestroy(e1);
+    s->nsplit = best_ns;
+    return GADE_OK;
+}
+
+extern "C" int gade_solver_create(const gade_problem *p, double dt, double h, int32_t precision,
+                                  int32_t device, gade_solver **out)
+{
+    if (!p || !out) return fail(GADE_ERR_ARG, "gade_solver_create: NULL argument");
+    *out = nullptr;
+    if (precision != GADE_PREC_FP64 && precision != GADE_PREC_MIXED)
+        return fail(GADE_ERR_ARG, "gade_solver_create: unknown precision %d", precision);
+    if (!(dt > 0) || !std::isfinite(dt)) return fail(GADE_ERR_ARG, "gade_solver_create: dt must be finite and > 0");
+    int rc = solver_create(p, 1, &dt, nullptr, h, precision, device, 0, out);
+    if (rc) return rc;
+    if ((rc = choose_split(*out))) { gade_solver_free(*out); *out = nullptr; return rc; }
     return GADE_OK;
 }
 
@@ -2303,6 +2417,14 @@ extern "C" int gade_probe_fp64_peak(int32_t device, double *tflops)
     return GADE_OK;
 }
 
+extern "C" int gade_solver_split(const gade_solver *s, int32_t *nsplit, float *split_ms)
+{
+    if (!s) return fail(GADE_ERR_ARG, "gade_solver_split: NULL solver");
+    if (nsplit) *nsplit = s->nsplit;
+    if (split_ms) for (int k = 0; k < 4; k++) split_ms[k] = s->split_ms[k + 1];
+    return GADE_OK;
+}
+
 extern "C" int gade_solver_flops(const gade_solver *s, double *apply_flops, double *precond_flops)
 {
     if (!s) return fail(GADE_ERR_ARG, "gade_solver_flops: NULL solver");
@@ -2359,6 +2481,7 @@ extern "C" int gade_solver_apply_dot_noalloc(gade_solver *s, const void *x_dev, 
     /* the arrival ticket must start at zero */
     CK(cudaMemsetAsync(ticket, 0, sizeof(unsigned int), st));
     OpP P = op_params(s);
+    P.nsplit = 1;                /* the split's partial sums would need scratch */
     RedP red = make_red(s, s->d_sc, RED_DOT_OUT, PRED_NONE);
     red.part = base; red.ticket = ticket; red.out = (double *)dot_dev;
     VecP V = {};

@@ -83,6 +83,7 @@ _SIGS = {
     "gade_solver_kernel_times": (C.c_int, [C.c_void_p, C.POINTER(KernelTimes)]),
     "gade_probe_fp64_peak": (C.c_int, [C.c_int32, C.POINTER(C.c_double)]),
     "gade_solver_flops": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "gade_solver_split": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.c_void_p]),
     "gade_solver_apply_dot_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                                 C.c_void_p]),
     "gade_batch_create": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_double, C.c_int32,
@@ -284,6 +285,13 @@ class Solver:
         kt = KernelTimes()
         _check(load_library().gade_solver_kernel_times(self._h, C.byref(kt)))
         return {k: getattr(kt, k) for k, _ in KernelTimes._fields_}
+
+    def split(self) -> tuple[int, list[float]]:
+        """(order split of the operator kernel, timed apply ms for 1-4 splits)."""
+        ns = C.c_int32()
+        ms = (C.c_float * 4)()
+        _check(load_library().gade_solver_split(self._h, C.byref(ns), ms))
+        return int(ns.value), [float(v) for v in ms]
 
     def flops(self) -> tuple[float, float]:
         """(FP64 flops of one operator apply, of one preconditioner solve)."""

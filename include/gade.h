@@ -148,6 +148,14 @@ int gade_solver_profile(gade_solver *s, int32_t enable);
 /* Synchronises, returns the accumulated times and resets them. */
 int gade_solver_kernel_times(gade_solver *s, gade_kernel_times *out);
 
+/* Order split of the operator kernel chosen at creation (no reference
+ * counterpart): when one pulse has too few (row chunk, block row) work units
+ * to balance the SMs, nsplit CTAs share each unit, each with a part of the
+ * Bessel orders, and the last one combines their partial sums in a fixed
+ * order.  split_ms (4 floats, may be NULL) receives the timed apply for 1-4
+ * splits (0 where not timed). */
+int gade_solver_split(const gade_solver *s, int32_t *nsplit, float *split_ms);
+
 /* FP64 flops (2 per FMA) executed by one operator apply and one
  * preconditioner solve, counted exactly from the set-up structure. */
 int gade_solver_flops(const gade_solver *s, double *apply_flops, double *precond_flops);
