@@ -156,7 +156,6 @@ enum { ST_RUN = 0, ST_DONE, ST_ZERO, ST_RESTART, ST_BAD };
 enum { PRED_NONE = 0, PRED_RUN, PRED_RESTART, PRED_MIX, PRED_FIN, PRED_DONE };
 
 #define MIXED_MAX_SWEEPS 8
-#define MIXED_INNER_TOL 1e-6
 
 __device__ __forceinline__ bool pred_ok(int pred, const DevScal *a, const DevScal *b)
 {
@@ -1068,10 +1067,10 @@ __device__ __forceinline__ int bp_select(BPred &bp)
 }
 
 /* delta = x - x_prev (linear extrapolation of the state) or 0; FP32 copies.
-   hprev[pulse] (or have_prev when hprev is NULL) says whether x_prev exists.
+   hprev[pulse] says whether x_prev exists.
    Under device control the first CTA also opens the step's records. */
 __global__ void k_mixed_prep(long long n, const double2 *__restrict__ x, const double2 *__restrict__ xprev,
-                             int have_prev, const int *__restrict__ hprev, double2 *__restrict__ d64,
+                             const int *__restrict__ hprev, double2 *__restrict__ d64,
                              float2 *__restrict__ d32, double2 *__restrict__ w, BPred bp,
                              const double2 *__restrict__ corr)
 {
@@ -1082,7 +1081,7 @@ __global__ void k_mixed_prep(long long n, const double2 *__restrict__ x, const d
         x += vo; xprev += vo; d64 += vo; d32 += vo; w += vo;
         if (corr) corr += vo;
     }
-    if (hprev) have_prev = hprev[pulse];
+    const int have_prev = hprev[pulse];
     if (blockIdx.x == 0 && threadIdx.x == 0 && bp.a && bp.a->ctl == 1) {
         DevScal *a = bp.a;
         a->state = ST_RUN; a->pending = 0; a->sweeps = 0; a->refinements = 0; a->inner_total = 0;
@@ -1244,7 +1243,6 @@ struct gade_solver {
     float2 *x32, *d32, *q32, *r32, *e32, *ri32, *r032, *p32, *v32, *y32, *z32, *s32, *t32;
     double2 *xprev, *delta64;
     DevScal *d_sc2, *h_sc2;
-    int have_prev;
     int *d_hprev;               /* [pulse] x_prev exists (batched mixed precision) */
     /* order split of the operator kernel (single-pulse solvers) */
     int nsplit;
@@ -1252,7 +1250,11 @@ struct gade_solver {
     unsigned int *d_split_tick;
     int nsm;
     float split_ms[5];          /* autotuner: FP64 (+ complex64) apply time per split count */
+    gade_batch *engine;         /* step engine of a single-pulse solver (device control, graphs) */
 };
+
+static int solver_engine_step(gade_solver *s, const double *ft, int32_t maxit, double tol, gade_step_stats *stats);
+static void solver_engine_free(gade_solver *s);
 
 static void prof_begin(gade_solver *s, cudaStream_t st)
 {
@@ -1362,6 +1364,7 @@ extern "C" void gade_solver_free(gade_solver *s)
     cudaGetDevice(&cur);
     cudaSetDevice(s->device);
     if (s->stream) cudaStreamSynchronize(s->stream);
+    solver_engine_free(s);
     for (void *p : s->allocs) cudaFree(p);
     for (cudaEvent_t e : s->ev_pool) cudaEventDestroy(e);
     if (s->h_sc) cudaFreeHost(s->h_sc);
@@ -1936,8 +1939,9 @@ extern "C" int gade_solver_set_x(gade_solver *s, const double *x, int64_t n)
     if (n != s->n) return fail(GADE_ERR_ARG, "gade_solver_set_x: size %lld != %lld", (long long)n, s->n);
     CK(cudaSetDevice(s->device));
     CK(cudaMemcpyAsync(s->x, x, sizeof(double2) * (size_t)n, cudaMemcpyHostToDevice, s->stream));
+    /* a new state has no extrapolation history */
+    if (s->d_hprev) CK(cudaMemsetAsync(s->d_hprev, 0, sizeof(int), s->stream));
     CK(cudaStreamSynchronize(s->stream));
-    s->have_prev = 0;            /* a new state has no extrapolation history */
     return GADE_OK;
 }
 
@@ -2098,214 +2102,15 @@ extern "C" int gade_solver_create(const gade_problem *p, double dt, double h, in
     return GADE_OK;
 }
 
-static int sync_scal2(gade_solver *s)
-{
-    CK(cudaMemcpyAsync(s->h_sc2, s->d_sc2, sizeof(DevScal), cudaMemcpyDeviceToHost, s->stream));
-    CK(cudaStreamSynchronize(s->stream));
-    if (s->h_sc2->err) {
-        unsigned e = s->h_sc2->err;
-        CK(cudaMemsetAsync(&s->d_sc2->err, 0, sizeof(unsigned), s->stream));
-        return fail(GADE_ERR_CUDA, "device wait timed out (flags %u): TMA copy did not complete", e);
-    }
-    return GADE_OK;
-}
-
-/*
- * Mixed-precision CN step.  With delta = x_{n+1} - x_n the CN residual is
- *   r = (S x_n - H x_n) - (S + H)(x_n + delta) = q - A delta,  q = -2 H x_n,
- * so the refinement never cancels against S x_n.  FP64 is kept for q, for
- * every refinement residual q - A delta, for |b|, |r| and for the S-norm
- * x^H S x; the correction comes from complex64 BiCGSTAB on A e = r with the
- * FP32-rounded block-LU factors (FP64 LU on the host).  The inner recursive
- * residual of e is accurate to ~1e-7 |r|, so once the FP64 residual r is
- * small the inner estimate certifies |q - A (delta + e)| without another FP64
- * operator pass; otherwise the FP64 residual is recomputed and refinement
- * continues.  delta starts from the linear extrapolation x_n - x_{n-1}.
- */
-static int mixed_step(gade_solver *s, const double *ft, int32_t maxit, double tol, gade_step_stats *stats)
-{
-    int rc;
-    gade_step_stats st = {};
-    const long long n = s->n;
-    const int grid = s->upd_grid, blk = s->upd_block;
-    const size_t rsm = sizeof(double) * NRED * blk;
-    if ((rc = launch_tables(s, ft, 3))) return rc;
-    prof_begin(s, s->stream);
-    const BPred none = {nullptr, s->d_sc, s->d_sc2, PRED_NONE};
-    k_mixed_prep<<<grid, blk, 0, s->stream>>>(n, s->x, s->xprev, s->have_prev, nullptr, s->delta64, s->d32, s->tmp0,
-                                              none, nullptr);
-    prof_end(s, s->stream, 2);
-    CKL();
-    const double eps2 = 1e-12 * 1e-12;
-    const int maxit_in = maxit < 50 ? maxit : 50;
-    int sweep = 0, inner = 0, fp64_res = 0;
-    double rr = 0, b2 = 0, tol2 = 0;
-    bool done = false;
-    while (!done) {
-        /* one FP64 pass: r = q - A delta = -S delta - H (2 x_n + delta); the
-           first pass also gives |b|^2 (b = S x_n - H w/2 differs from the CN
-           right-hand side by H delta/2, ~1e-8 relative) and x_n^H S x_n */
-        VecP R = {};
-        R.out0 = s->r; R.in0 = s->x; R.in1 = s->delta64;
-        if ((rc = launch_apply(s, s->tmp0, AX_MIX, R, RED_MIX, s->stream))) return rc;
-        if ((rc = sync_scal(s))) return rc;
-        fp64_res++;
-        rr = s->h_sc->rr;
-        if (fp64_res == 1) {
-            b2 = s->h_sc->rhs_sqnorm;
-            st.snorm = s->h_sc->snorm;
-            st.init_residual = sqrt(rr / b2);
-            tol2 = tol * tol * b2;
-            if (!std::isfinite(b2)) return fail(GADE_ERR_NUMERIC, "non-finite right-hand side");
-            if (b2 == 0) {
-                CK(cudaMemsetAsync(s->x, 0, sizeof(double2) * (size_t)n, s->stream));
-                CK(cudaStreamSynchronize(s->stream));
-                s->have_prev = 0;
-                if (stats) *stats = st;
-                return GADE_OK;
-            }
-        }
-        if (!std::isfinite(rr)) return fail(GADE_ERR_NUMERIC, "non-finite refinement residual");
-        if (rr < tol2 || sweep >= MIXED_MAX_SWEEPS || maxit_in <= 0) break;
-        sweep++;
-        {
-            RedP red = make_red(s, s->d_sc2, RED_RHS, PRED_NONE);
-            prof_begin(s, s->stream);
-            k_inner_init<<<grid, blk, rsm, s->stream>>>(n, s->r, s->e32, s->ri32, s->r032, s->p32, s->v32, red,
-                                                        nullptr);
-            prof_end(s, s->stream, 2);
-            CKL();
-        }
-        if ((rc = sync_scal2(s))) return rc;
-        const double r0in = s->h_sc2->r0_sqnorm;
-        /* run the cheap inner solve until its estimate of the outer residual
-           certifies the tolerance (the estimate is good to ~1e-7 |r|) */
-        const double tol_in2 = 0.25 * tol2;
-        double rin = r0in;
-        for (int it = 0; it < maxit_in; it++) {
-            if (fabs(s->h_sc2->rho.x) < eps2 * r0in) break;     /* breakdown: refine again */
-            if ((rc = launch_precond32(s, PC_P, s->ri32, s->v32, s->p32, s->y32, s->d_sc2))) return rc;
-            VecP A1 = {}; A1.out0 = s->v32; A1.in0 = s->r032;
-            if ((rc = launch_apply32(s, s->y32, AX_R0V, A1, RED_R0V, s->d_sc2))) return rc;
-            if ((rc = launch_precond32(s, PC_S, s->ri32, s->v32, s->s32, s->z32, s->d_sc2))) return rc;
-            VecP A2 = {}; A2.out0 = s->t32; A2.in0 = s->s32;
-            if ((rc = launch_apply32(s, s->z32, AX_TS, A2, RED_TS, s->d_sc2))) return rc;
-            {
-                RedP red = make_red(s, s->d_sc2, RED_UPDATE, PRED_NONE);
-                prof_begin(s, s->stream);
-                k_update<float><<<grid, blk, rsm, s->stream>>>(n, s->e32, s->y32, s->z32, s->ri32, s->s32,
-                                                               s->t32, s->r032, red, nullptr);
-                prof_end(s, s->stream, 2);
-                CKL();
-            }
-            if ((rc = sync_scal2(s))) return rc;
-            inner++;
-            rin = s->h_sc2->rr;
-            if (!(rin >= tol_in2)) break;
-        }
-        prof_begin(s, s->stream);
-        k_delta_add<<<grid, blk, 0, s->stream>>>(n, s->delta64, s->e32, s->d32, s->x, s->tmp0, none);
-        prof_end(s, s->stream, 2);
-        CKL();
-        const double est_err2 = 1e-14 * r0in;
-        if (std::isfinite(rin) && rin + est_err2 < 0.25 * tol2) {
-            rr = rin + est_err2;
-            done = true;
-        }
-    }
-    prof_begin(s, s->stream);
-    k_mixed_finish<<<grid, blk, 0, s->stream>>>(n, s->x, s->xprev, s->delta64, nullptr, none);
-    prof_end(s, s->stream, 2);
-    CKL();
-    s->have_prev = 1;
-    st.iters = inner;
-    st.inner_iters = inner;
-    st.refinements = fp64_res;
-    st.true_residual = sqrt(rr / b2);
-    st.tol_error = st.true_residual;
-    if (stats) *stats = st;
-    if (!(rr < tol2) && maxit_in > 0)
-        return fail(GADE_ERR_NUMERIC, "mixed-precision refinement stalled at |r|/|b| = %.3e > tol %.3e after %d sweeps",
-                    sqrt(rr / b2), tol, sweep);
-    return GADE_OK;
-}
 
 extern "C" int gade_solver_step(gade_solver *s, const double *ft, int32_t maxit, double tol,
                                 gade_step_stats *stats)
 {
     if (!s || !ft) return fail(GADE_ERR_ARG, "gade_solver_step: NULL argument");
     if (maxit < 0) return fail(GADE_ERR_ARG, "gade_solver_step: maxit < 0");
+    if (!(tol >= 0) || !std::isfinite(tol)) return fail(GADE_ERR_ARG, "gade_solver_step: tol must be finite and >= 0");
     CK(cudaSetDevice(s->device));
-    if (s->prec == GADE_PREC_MIXED) return mixed_step(s, ft, maxit, tol, stats);
-    int rc;
-    gade_step_stats st = {};
-    if ((rc = launch_tables(s, ft))) return rc;
-    /* rhs = S x - H x, r = rhs - A x, r0 = r (tools/dirac_solver.c:533-536,
-       tools/gpu_bicgstab.c:169-181) */
-    VecP V = {};
-    V.out0 = s->rhs; V.out1 = s->r; V.out2 = s->r0;
-    if ((rc = launch_apply(s, s->x, AX_RHS, V, RED_RHS, s->stream))) return rc;
-    if ((rc = sync_scal(s))) return rc;
-    const double rhs_sqnorm = s->h_sc->rhs_sqnorm;
-    double r0_sqnorm = s->h_sc->r0_sqnorm;
-    if (!std::isfinite(rhs_sqnorm) || !std::isfinite(r0_sqnorm))
-        return fail(GADE_ERR_NUMERIC, "non-finite right-hand side or residual");
-    if (rhs_sqnorm == 0) {
-        CK(cudaMemsetAsync(s->x, 0, sizeof(double2) * (size_t)s->n, s->stream));
-        CK(cudaStreamSynchronize(s->stream));
-        st.iters = 0; st.tol_error = 0;
-        if (stats) *stats = st;
-        return GADE_OK;
-    }
-    const double tol2 = tol * tol * rhs_sqnorm;
-    const double eps2 = 1e-12 * 1e-12;
-    if (r0_sqnorm < tol2) {
-        st.iters = 0; st.tol_error = sqrt(r0_sqnorm / rhs_sqnorm);
-        if (stats) *stats = st;
-        return GADE_OK;
-    }
-    int i = 0;
-    double rr = r0_sqnorm;
-    while (i < maxit) {
-        /* restart when r has become orthogonal to r0; the CPU build tests
-           the real part of rho (fabs of a C complex), tools/bicgstab.c:208 */
-        if (fabs(s->h_sc->rho.x) < eps2 * r0_sqnorm) {
-            VecP R = {};
-            R.in0 = s->rhs; R.out1 = s->r; R.out2 = s->r0;
-            if ((rc = launch_apply(s, s->x, AX_RESTART, R, RED_RESTART, s->stream))) return rc;
-            if ((rc = sync_scal(s))) return rc;
-            r0_sqnorm = s->h_sc->r0_sqnorm;
-            st.restarts++;
-        }
-        /* p = r + beta (p - w v); y = M^-1 p */
-        if ((rc = launch_precond(s, PC_P, s->r, s->v, s->p, s->y, s->stream))) return rc;
-        /* v = A y; alpha = rho / <r0, v> */
-        VecP A1 = {}; A1.out0 = s->v; A1.in0 = s->r0;
-        if ((rc = launch_apply(s, s->y, AX_R0V, A1, RED_R0V, s->stream))) return rc;
-        /* s = r - alpha v; z = M^-1 s */
-        if ((rc = launch_precond(s, PC_S, s->r, s->v, s->s, s->z, s->stream))) return rc;
-        /* t = A z; w = <t,s>/<t,t> */
-        VecP A2 = {}; A2.out0 = s->t; A2.in0 = s->s;
-        if ((rc = launch_apply(s, s->z, AX_TS, A2, RED_TS, s->stream))) return rc;
-        /* x += alpha y + w z; r = s - w t; |r|^2; rho = <r0, r> */
-        {
-            RedP red = make_red(s, s->d_sc, RED_UPDATE, PRED_NONE);
-            prof_begin(s, s->stream);
-            k_update<double><<<s->upd_grid, s->upd_block, sizeof(double) * NRED * s->upd_block, s->stream>>>(
-                s->n, s->x, s->y, s->z, s->r, s->s, s->t, s->r0, red, nullptr);
-            prof_end(s, s->stream, 2);
-            CKL();
-        }
-        if ((rc = sync_scal(s))) return rc;
-        rr = s->h_sc->rr;
-        if (!std::isfinite(rr)) return fail(GADE_ERR_NUMERIC, "BiCGSTAB residual became non-finite at iteration %d", i);
-        if (rr < tol2) break;
-        ++i;
-    }
-    st.iters = i;
-    st.tol_error = sqrt(rr / rhs_sqnorm);
-    if (stats) *stats = st;
-    return GADE_OK;
+    return solver_engine_step(s, ft, maxit, tol, stats);
 }
 
 extern "C" int gade_solver_time_apply(gade_solver *s, int32_t reps, double *ms)
@@ -2526,6 +2331,8 @@ struct gade_batch {
     int tune_cs[4], ntune;
     double2 *d_corr;                /* [npulse][n] initial-guess corrections (mixed) */
     int use_guess;
+    int internal;                   /* the step engine of a gade_solver (one pulse, no launch list) */
+    long long nodes[3];             /* kernels of each captured graph */
 };
 
 static void batch_drop_graphs(gade_batch *b)
@@ -2605,7 +2412,7 @@ static int batch_seq_first(gade_batch *b, cudaStream_t st)
         if ((rc = launch_table_kernels(s, 3, st))) return rc;
         const BPred all = {s->d_plist, s->d_sc, s->d_sc2, PRED_NONE};
         k_mixed_prep<<<dim3(s->upd_grid, s->nslot), s->upd_block, 0, st>>>(
-            s->n, s->x, s->xprev, 0, s->d_hprev, s->delta64, s->d32, s->tmp0, all, b->use_guess ? b->d_corr : nullptr);
+            s->n, s->x, s->xprev, s->d_hprev, s->delta64, s->d32, s->tmp0, all, b->use_guess ? b->d_corr : nullptr);
         CKL();
         return batch_seq_sweep(b, b->kiter, st);
     }
@@ -2643,9 +2450,13 @@ static int batch_launch(gade_batch *b, int which)
     cudaGraphExec_t *slot = which == 0 ? &b->g_first : which == 1 ? &b->g_iter : &b->g_restart;
     if (!*slot) {
         cudaGraph_t g = nullptr;
+        const long long before = s->launches;
         CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
         int rc = batch_run_seq(b, which);
         cudaError_t ce = cudaStreamEndCapture(s->stream, &g);
+        /* capturing launches nothing: count the kernels at every replay */
+        b->nodes[which] = s->launches - before;
+        s->launches = before;
         if (rc) { if (g) cudaGraphDestroy(g); return rc; }
         if (ce != cudaSuccess) return fail(GADE_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(ce));
         ce = cudaGraphInstantiate(slot, g, 0);
@@ -2653,13 +2464,14 @@ static int batch_launch(gade_batch *b, int which)
         if (ce != cudaSuccess) { *slot = nullptr; return fail(GADE_ERR_CUDA, "graph instantiation failed: %s", cudaGetErrorString(ce)); }
     }
     CK(cudaGraphLaunch(*slot, s->stream));
+    s->launches += b->nodes[which];
     return GADE_OK;
 }
 
 static int batch_set_list(gade_batch *b, const std::vector<int> &list)
 {
     gade_solver *s = b->s;
-    if (list == b->list) return GADE_OK;
+    if (list == b->list || b->internal) return GADE_OK;
     CK(cudaMemcpyAsync(s->d_plist, list.data(), sizeof(int) * list.size(), cudaMemcpyHostToDevice, s->stream));
     CK(cudaStreamSynchronize(s->stream));
     b->list = list;
@@ -2743,7 +2555,7 @@ extern "C" int gade_batch_create(const gade_problem *p, int32_t npulse, const do
     gade_batch *b = new gade_batch();
     b->s = s;
     b->kfixed = o.iters_per_launch;
-    b->kiter = o.iters_per_launch > 0 ? o.iters_per_launch : 4;
+    b->kiter = o.iters_per_launch > 0 ? o.iters_per_launch : 2;
     b->use_graphs = o.use_graphs != 0;
     b->tol_c = -1; b->maxit_c = -1;
     for (int k = 0; k < npulse; k++) b->list.push_back(k);
@@ -2789,7 +2601,9 @@ extern "C" int gade_batch_get_x(gade_batch *b, int32_t pulse, double *x, int64_t
 }
 
 /* iterations per captured launch: large enough that most steps need one
-   replay, shrunk only after 32 steps that all needed fewer */
+   replay (grown at once), shrunk after 8 steps that all needed fewer (every
+   predicated-off iteration still launches its kernels) */
+#define BATCH_SHRINK_STEPS 8
 static void batch_adapt(gade_batch *b, int kmax)
 {
     if (b->kfixed) return;
@@ -2797,11 +2611,11 @@ static void batch_adapt(gade_batch *b, int kmax)
     if (want > 64) want = 64;
     if (want > b->kwin) b->kwin = want;
     b->kwin_steps++;
-    if (want > b->kiter || (b->kwin_steps >= 32 && b->kwin < b->kiter)) {
+    if (want > b->kiter || (b->kwin_steps >= BATCH_SHRINK_STEPS && b->kwin < b->kiter)) {
         b->kiter = want > b->kiter ? want : b->kwin;
         b->kwin = 0; b->kwin_steps = 0;
         batch_drop_graphs(b);
-    } else if (b->kwin_steps >= 32) {
+    } else if (b->kwin_steps >= BATCH_SHRINK_STEPS) {
         b->kwin = 0; b->kwin_steps = 0;
     }
 }
@@ -2890,6 +2704,9 @@ static int batch_step_mixed(gade_batch *b, const std::vector<int> &list, int32_t
     return GADE_OK;
 }
 
+static int batch_step_fp64(gade_batch *b, const std::vector<int> &list, int32_t maxit, double tol,
+                           gade_step_stats *stats);
+
 extern "C" int gade_batch_step(gade_batch *b, const int32_t *active, const double *ft, int32_t maxit, double tol,
                                gade_step_stats *stats)
 {
@@ -2913,6 +2730,15 @@ extern "C" int gade_batch_step(gade_batch *b, const int32_t *active, const doubl
         }
     if ((rc = batch_set_list(b, list))) return rc;
     if (s->prec == GADE_PREC_MIXED) return batch_step_mixed(b, list, maxit, tol, stats);
+    return batch_step_fp64(b, list, maxit, tol, stats);
+}
+
+/* FP64 step of the listed pulses with device-side BiCGSTAB control */
+static int batch_step_fp64(gade_batch *b, const std::vector<int> &list, int32_t maxit, double tol,
+                           gade_step_stats *stats)
+{
+    gade_solver *s = b->s;
+    int rc;
     if (tol != b->tol_c || maxit != b->maxit_c) {
         /* control values of every pulse (the rest of each record is reset by
            the right-hand-side reduction of the step) */
@@ -3016,4 +2842,44 @@ extern "C" int gade_batch_use_guess(gade_batch *b, int32_t enable)
     if ((enable != 0) != (b->use_guess != 0)) batch_drop_graphs(b);
     b->use_guess = enable != 0;
     return GADE_OK;
+}
+
+/*
+ * gade_solver_step runs on the batch engine with one pulse: the same kernels
+ * in the same order, BiCGSTAB's control (or the mixed-precision refinement's)
+ * in the reduction epilogues and the step replayed from captured CUDA graphs,
+ * so the host waits once per replay instead of once per iteration.  While
+ * event profiling is on the kernels are launched directly (the events of a
+ * replayed graph could not be told apart).
+ */
+static int solver_engine_step(gade_solver *s, const double *ft, int32_t maxit, double tol, gade_step_stats *stats)
+{
+    if (!s->engine) {
+        gade_batch *b = new gade_batch();
+        b->s = s;
+        b->internal = 1;
+        b->kiter = 2;
+        b->use_graphs = 1;
+        b->tol_c = -1; b->maxit_c = -1;
+        b->list.push_back(0);
+        s->engine = b;
+    }
+    gade_batch *b = s->engine;
+    const int want_graphs = s->profile ? 0 : 1;
+    if (want_graphs != b->use_graphs) { batch_drop_graphs(b); b->use_graphs = want_graphs; }
+    int rc = fill_coef(s, 0, ft);
+    if (rc) return rc;
+    gade_step_stats st = {};
+    rc = s->prec == GADE_PREC_MIXED ? batch_step_mixed(b, b->list, maxit, tol, &st)
+                                    : batch_step_fp64(b, b->list, maxit, tol, &st);
+    if (stats) *stats = st;
+    return rc;
+}
+
+static void solver_engine_free(gade_solver *s)
+{
+    if (!s || !s->engine) return;
+    batch_drop_graphs(s->engine);
+    delete s->engine;
+    s->engine = nullptr;
 }
