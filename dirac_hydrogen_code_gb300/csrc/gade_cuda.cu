@@ -1251,10 +1251,12 @@ struct gade_solver {
     int nsm;
     float split_ms[5];          /* autotuner: FP64 (+ complex64) apply time per split count */
     gade_batch *engine;         /* step engine of a single-pulse solver (device control, graphs) */
+    int split_cap;              /* splits the scratch holds */
 };
 
 static int solver_engine_step(gade_solver *s, const double *ft, int32_t maxit, double tol, gade_step_stats *stats);
 static void solver_engine_free(gade_solver *s);
+static void batch_drop_graphs(gade_batch *b);
 
 static void prof_begin(gade_solver *s, cudaStream_t st)
 {
@@ -2060,6 +2062,7 @@ static int choose_split(gade_solver *s)
     int rc;
     if ((rc = dev_upload(s, (double2 **)&s->d_split_acc, (const double2 *)nullptr, (size_t)maxs * 3 * s->n))) return rc;
     if ((rc = dev_upload(s, &s->d_split_tick, (const unsigned *)nullptr, (size_t)ctas))) return rc;
+    s->split_cap = maxs;
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1));
     float best = 1e30f;
@@ -2219,6 +2222,27 @@ extern "C" int gade_probe_fp64_peak(int32_t device, double *tflops)
     cudaFree(out);
     const double flops = 2.0 * 8.0 * iters * (double)blocks * threads;
     *tflops = flops / (best * 1e-3) / 1e12;
+    return GADE_OK;
+}
+
+extern "C" int gade_solver_set_split(gade_solver *s, int32_t nsplit)
+{
+    if (!s) return fail(GADE_ERR_ARG, "gade_solver_set_split: NULL solver");
+    if (nsplit < 1 || nsplit > 4) return fail(GADE_ERR_ARG, "gade_solver_set_split: nsplit %d not in 1..4", nsplit);
+    if (nsplit > 1 && !s->d_split_acc) {
+        /* the scratch of the largest split */
+        CK(cudaSetDevice(s->device));
+        const long long ctas = (long long)s->nchunk * s->nblk;
+        int rc;
+        if ((rc = dev_upload(s, (double2 **)&s->d_split_acc, (const double2 *)nullptr, (size_t)4 * 3 * s->n))) return rc;
+        if ((rc = dev_upload(s, &s->d_split_tick, (const unsigned *)nullptr, (size_t)ctas))) return rc;
+        s->split_cap = 4;
+    }
+    if (nsplit > s->split_cap && nsplit > 1)
+        return fail(GADE_ERR_ARG, "gade_solver_set_split: scratch holds %d splits", s->split_cap);
+    CK(cudaStreamSynchronize(s->stream));
+    if (s->engine) batch_drop_graphs(s->engine);
+    s->nsplit = nsplit;
     return GADE_OK;
 }
 

@@ -21,6 +21,7 @@ last state change is dropped on the device (plain extrapolation).
 from __future__ import annotations
 
 import math
+import os
 import time
 
 import numpy as np
@@ -401,3 +402,98 @@ def intensity_pulses(n: int, seed: int, omega: float, cycles: int, ntime: int) -
     E0 = np.exp(rng.uniform(0.0, math.log(100.0), n))
     T = cycles * 2 * math.pi / omega
     return [dict(E0=float(e), omega=omega, cycles=cycles, ntime=ntime, maxtime=T) for e in E0]
+
+
+def experiment(params: dict, nsteps: int, ntrain: int = 32, nheld: int = 8, rank: int = 128, nsnap: int = 200,
+               pod_pulses: int = 8, epochs: int = 30, seed: int = 1, tol: float = 1e-10, workdir: str | None = None,
+               log=None) -> dict:
+    """The learned-guess protocol: POD + network from `ntrain` seeded training
+    pulses (plain FP64 trajectories), then `nheld` seeded held-out pulses run
+    four ways for `nsteps` steps: FP64 at tol 1e-12 (reference), plain FP64 at
+    `tol`, mixed precision with the extrapolated guess and with the learned
+    guess (both at `tol`).  Pulses differ in Intensity only (log-uniform in
+    [1, 100]).  Returns steps/s, iterations, initial residuals and final-state
+    errors (relative L2, bound and continuum populations) of each run."""
+    import tempfile
+    from .gen import generate
+    from .populations import Eigenbasis
+    say = log or (lambda *a: None)
+    own = workdir is None
+    tmp = tempfile.TemporaryDirectory() if own else None
+    d = tmp.name if own else workdir
+    if not os.path.exists(os.path.join(d, "H.csr")):
+        generate(params, d)
+    lmax = params["Nl"] if params["Nl"] else 2 * params["Nkappa"] + 1
+    prob = Problem(d, lmax)
+    mk = lambda n, s: intensity_pulses(n, s, params["Omega"], params["Cycles"], params["Ntime"])  # noqa: E731
+    train, held = mk(ntrain, 100 + seed), mk(nheld, 200 + seed)
+    out = {"params": params, "steps_per_pulse": nsteps, "train_pulses": ntrain, "held_out_pulses": nheld,
+           "seeds": {"train": 100 + seed, "held_out": 200 + seed, "pod_and_network": seed}, "tol": tol}
+    t0 = time.perf_counter()
+    model = build_model(prob, train, nsteps, rank=rank, nsnap=nsnap, pod_pulses=pod_pulses, seed=seed,
+                        epochs=epochs, tol=tol, log=say)
+    out["build_s"] = time.perf_counter() - t0
+    out["model"] = {k: model.history[k] for k in ("rows", "rank", "sv_ratio", "snapshots", "train_s")}
+    out["model"]["loss_per_epoch"] = model.history["loss"]
+    kap, _ = prob.blocks()
+    eb = Eigenbasis(d, kap)
+    xr, _, ms_ref = run_held_out(prob, held, nsteps, 1e-12, "fp64", None)
+    pref = [eb.populations(x) for x in xr]
+    out["reference_fp64_tol1e-12"] = {"steps_per_s": nheld * nsteps / (ms_ref / 1e3),
+                                      "populations_mean": {k: float(np.mean([p[k] for p in pref])) for k in pref[0]}}
+    say("reference done", out["reference_fp64_tol1e-12"])
+    for tag, prec, mdl in (("fp64", "fp64", None), ("mixed", "mixed", None), ("learned_mixed", "mixed", model)):
+        xs, st, ms = run_held_out(prob, held, nsteps, tol, prec, mdl)
+        err = np.linalg.norm(xs - xr, axis=1) / np.linalg.norm(xr, axis=1)
+        pops = [eb.populations(x) for x in xs]
+        rec = {"steps_per_s": nheld * nsteps / (ms / 1e3),
+               "iters_per_step": float(np.mean([[r["iters"] for r in row] for row in st])),
+               "final_l2_err_max": float(err.max()), "final_l2_err_mean": float(err.mean()),
+               "bound_abs_err_max": max(abs(p["bound"] - q["bound"]) for p, q in zip(pops, pref)),
+               "continuum_abs_err_max": max(abs(p["continuum"] - q["continuum"]) for p, q in zip(pops, pref))}
+        if prec == "mixed":
+            ini = np.array([[r["init_residual"] for r in row] for row in st])[K_HIST:]
+            rec["init_residual_mean"] = float(ini.mean())
+            rec["init_residual_median"] = float(np.median(ini))
+            rec["fp64_residual_passes_per_step"] = float(np.mean([[r["refinements"] for r in row] for row in st]))
+        out[tag] = rec
+        say(tag, rec)
+    base = out["fp64"]["steps_per_s"]
+    out["speedup_vs_fp64"] = {k: out[k]["steps_per_s"] / base for k in ("mixed", "learned_mixed")}
+    prob.close()
+    if tmp is not None:
+        tmp.cleanup()
+    return out
+
+
+def main(argv=None) -> int:
+    import argparse
+    import json
+    import sys
+    from .gen import CONFIGS
+    ap = argparse.ArgumentParser(prog="python -m dirac_hydrogen_code_gb300.learned")
+    ap.add_argument("--workload", default="nondipole_large", choices=sorted(CONFIGS))
+    ap.add_argument("--steps", type=int, default=0, help="steps per pulse (0: the whole pulse, Ntime+1)")
+    ap.add_argument("--train", type=int, default=32)
+    ap.add_argument("--held", type=int, default=8)
+    ap.add_argument("--rank", type=int, default=128)
+    ap.add_argument("--epochs", type=int, default=30)
+    ap.add_argument("--out", default=None, help="write the result JSON here")
+    args = ap.parse_args(argv)
+    params = CONFIGS[args.workload]
+    T = params["Cycles"] * 2 * math.pi / params["Omega"]
+    nsteps = args.steps or len(step_times(T, params["Ntime"])[1])
+    res = experiment(params, nsteps, args.train, args.held, rank=args.rank, epochs=args.epochs,
+                     log=lambda *a: print(*a, file=sys.stderr, flush=True))
+    res["workload"] = args.workload
+    txt = json.dumps(res)
+    if args.out:
+        with open(args.out, "w") as f:
+            f.write(txt)
+    print(txt)
+    return 0
+
+
+if __name__ == "__main__":
+    import sys as _sys
+    _sys.exit(main())

@@ -84,6 +84,7 @@ _SIGS = {
     "gade_probe_fp64_peak": (C.c_int, [C.c_int32, C.POINTER(C.c_double)]),
     "gade_solver_flops": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "gade_solver_split": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.c_void_p]),
+    "gade_solver_set_split": (C.c_int, [C.c_void_p, C.c_int32]),
     "gade_solver_apply_dot_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                                 C.c_void_p]),
     "gade_batch_create": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_double, C.c_int32,
@@ -292,6 +293,9 @@ class Solver:
         ms = (C.c_float * 4)()
         _check(load_library().gade_solver_split(self._h, C.byref(ns), ms))
         return int(ns.value), [float(v) for v in ms]
+
+    def set_split(self, nsplit: int):
+        _check(load_library().gade_solver_set_split(self._h, int(nsplit)))
 
     def flops(self) -> tuple[float, float]:
         """(FP64 flops of one operator apply, of one preconditioner solve)."""

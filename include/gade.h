@@ -155,6 +155,9 @@ int gade_solver_kernel_times(gade_solver *s, gade_kernel_times *out);
  * order.  split_ms (4 floats, may be NULL) receives the timed apply for 1-4
  * splits (0 where not timed). */
 int gade_solver_split(const gade_solver *s, int32_t *nsplit, float *split_ms);
+/* Forces the order split (1-4) instead of the timed choice; results differ
+ * from the unsplit operator only by the order of summation. */
+int gade_solver_set_split(gade_solver *s, int32_t nsplit);
 
 /* FP64 flops (2 per FMA) executed by one operator apply and one
  * preconditioner solve, counted exactly from the set-up structure. */

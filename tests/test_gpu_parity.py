@@ -212,3 +212,26 @@ def test_drop_in_executable(workdirs, native_lib, tmp_path):
     os.remove(os.path.join(d2, "h02.csr"))
     res = subprocess.run(cmd, cwd=d2, capture_output=True, text=True, timeout=60)
     assert res.returncode == 1 and "h02.csr" in res.stderr
+
+
+def test_order_split_matches_unsplit(workdirs, native_lib):
+    """The operator with 1-4 order splits (partial sums combined by the last
+    CTA) gives the same steps up to the order of summation."""
+    d, params, info, T, dt = _setup(workdirs, "tiny_nondipole")
+    prob = Problem(d, info["lmax"])
+    psi, _ = prob.psi0()
+    fts = [pulse(params["Intensity"], params["Omega"], params["Cycles"], t) for _, t in step_times(T, params["Ntime"])[1][:6]]
+    ref = None
+    for ns in (1, 2, 3, 4):
+        sol = Solver(prob, dt)
+        sol.set_split(ns)
+        assert sol.split()[0] == ns
+        sol.set_x(psi)
+        its = [sol.step(ft, maxit=500, tol=1e-12)["iters"] for ft in fts]
+        x = sol.get_x()
+        if ref is None:
+            ref = (x, its)
+        else:
+            assert its == ref[1]
+            assert _rel(x, ref[0]) < 1e-13, ns
+        sol.close()
