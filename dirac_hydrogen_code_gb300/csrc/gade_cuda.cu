@@ -490,10 +490,14 @@ __host__ __device__ __forceinline__ ApplySmem apply_smem(int CS, int W, int RM, 
  * contracted vectors u, w, u', w' of a column are interleaved (one 32- or
  * 64-byte record) and so are the four angular factors of a term.
  */
-template <typename R, bool RC, bool SEP>
+template <typename R, bool RC, bool SEP, bool Z>
 __global__ void __launch_bounds__(256, (sizeof(R) == 8 && SEP) ? 2 : 3)
     k_apply(OpP P, const typename Cx<R>::T *__restrict__ x, int mode, VecP V, RedP red)
 {
+    /* Z: the DKB zero blocks hold (slots laid out by column half): the
+       first-half columns (this row's slots 0..14, thread half 0) have M3 = 0
+       and need no w', the second-half columns (slots 15..29, half 1) have
+       M1 = 0 and need no w */
     /* SEP: modes that need S x and H x apart (AX_RHS, AX_PARTS, AX_MIX, three
        accumulators); the BiCGSTAB modes use D = S + i h dt/2 h0 and one
        accumulator, which lets the FP64 instance fit three CTAs per SM */
@@ -639,7 +643,12 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 8 && SEP) ? 2 : 3)
             const int g = item / ncols, c = item - g * ncols;
             const int l = P.act_l[ag + g];
             const int e0 = P.ang_ptr[r * P.lmax + l] - ea, e1 = P.ang_ptr[r * P.lmax + l + 1] - ea;
-            const C *xc = x + cols[c];
+            const int gc = cols[c];
+            const C *xc = x + gc;
+            /* with the DKB zero blocks a first-half column needs no w' and a
+               second-half column no w */
+            const bool qcol = gc >= (B >> 1);
+            const bool need_b = !Z || !qcol, need_d = !Z || qcol;
             C4<C> u;
             u.a = mk<C>(0, 0); u.b = u.a; u.c = u.a; u.d = u.a;
 #pragma unroll 4
@@ -648,14 +657,14 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 8 && SEP) ? 2 : 3)
                 const A4 a = ang[e];
                 if constexpr (RC) {
                     rfma(u.a, a.a, xv);
-                    rfma(u.b, a.b, xv);
+                    if (need_b) rfma(u.b, a.b, xv);
                     rfma(u.c, a.c, xv);
-                    rfma(u.d, a.d, xv);
+                    if (need_d) rfma(u.d, a.d, xv);
                 } else {
                     cfma(u.a, a.a, xv);
-                    cfma(u.b, a.b, xv);
+                    if (need_b) cfma(u.b, a.b, xv);
                     cfma(u.c, a.c, xv);
-                    cfma(u.d, a.d, xv);
+                    if (need_d) cfma(u.d, a.d, xv);
                 }
             }
             ub[g * CS + c] = u;
@@ -668,26 +677,36 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 8 && SEP) ? 2 : 3)
                 if constexpr (RC) {
                     typedef typename R4<R>::T Q4;
                     const Q4 *Mt = (const Q4 *)P.M + ((size_t)l * P.nk + kk) * W * B + i + jB;
+                    const bool second = half == 1;
 #pragma unroll
                     for (int t = 0; t < HJ; t++) {
                         const Q4 m = *Mt;
                         const C4<C> u = ug[lco[t]];
                         rfma(accH, m.a, u.a);
-                        rfma(accH, m.b, u.b);
                         rfma(accH, m.c, u.c);
-                        rfma(accH, m.d, u.d);
+                        if (Z) {
+                            rfma(accH, second ? m.d : m.b, second ? u.d : u.b);
+                        } else {
+                            rfma(accH, m.b, u.b);
+                            rfma(accH, m.d, u.d);
+                        }
                         if (t + 1 < nj) Mt += B;
                     }
                 } else {
                     const C4<C> *Mt = (const C4<C> *)P.M + ((size_t)l * P.nk + kk) * W * B + i + jB;
+                    const bool second = half == 1;
 #pragma unroll
                     for (int t = 0; t < HJ; t++) {
                         const C4<C> m = *Mt;
                         const C4<C> u = ug[lco[t]];
                         cfma(accH, m.a, u.a);
-                        cfma(accH, m.b, u.b);
                         cfma(accH, m.c, u.c);
-                        cfma(accH, m.d, u.d);
+                        if (Z) {
+                            cfma(accH, second ? m.d : m.b, second ? u.d : u.b);
+                        } else {
+                            cfma(accH, m.b, u.b);
+                            cfma(accH, m.d, u.d);
+                        }
                         if (t + 1 < nj) Mt += B;
                     }
                 }
@@ -1252,6 +1271,7 @@ struct gade_solver {
     float split_ms[5];          /* autotuner: FP64 (+ complex64) apply time per split count */
     gade_batch *engine;         /* step engine of a single-pulse solver (device control, graphs) */
     int split_cap;              /* splits the scratch holds */
+    int zskip;                  /* the DKB zero blocks hold for every pulse's tables */
 };
 
 static int solver_engine_step(gade_solver *s, const double *ft, int32_t maxit, double tol, gade_step_stats *stats);
@@ -1426,8 +1446,11 @@ static int set_chunking(gade_solver *s, const gade_setup *su)
         for (int a = su->act_ptr[r]; a < su->act_ptr[r + 1]; a++) {
             int l = su->act_l[a];
             double ne = su->ang_ptr[r * s->lmax + l + 1] - su->ang_ptr[r * s->lmax + l];
-            fmas += 4.0 * fma_c * ne * cols;                       /* gather u, w, u', w' */
-            fmas += 4.0 * fma_c * (double)s->blk_nnz;              /* radial tables */
+            /* u, w, u', w' and their four tables; three of them per column
+               and per entry with the DKB zero blocks */
+            const double terms = s->zskip ? 3.0 : 4.0;
+            fmas += terms * fma_c * ne * cols;                     /* gather */
+            fmas += terms * fma_c * (double)s->blk_nnz;            /* radial tables */
         }
     s->apply_flops = 2.0 * fmas;
     return GADE_OK;
@@ -1516,14 +1539,22 @@ static int solver_create(const gade_problem *p, int npulse, const double *dts, c
     {
         /* operator kernels may use more than the default 48 KB of dynamic shared memory */
         const int lim = 160 * 1024;
-        cudaFuncSetAttribute(k_apply<double, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-        cudaFuncSetAttribute(k_apply<double, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-        cudaFuncSetAttribute(k_apply<float, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-        cudaFuncSetAttribute(k_apply<float, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-        cudaFuncSetAttribute(k_apply<double, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-        cudaFuncSetAttribute(k_apply<double, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-        cudaFuncSetAttribute(k_apply<float, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
-        cudaFuncSetAttribute(k_apply<float, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<double, true, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<double, true, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<double, false, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<double, false, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<float, true, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<float, true, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<float, false, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<float, false, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<double, true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<double, true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<double, false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<double, false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<float, true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<float, true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<float, false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<float, false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
     }
 
     gade_solver *s = new gade_solver();
@@ -1541,6 +1572,12 @@ static int solver_create(const gade_problem *p, int npulse, const double *dts, c
     }
     s->bw = su->bw; s->Bp = su->Bp; s->nch = su->nch;
     s->dt = dts[0]; s->h = h; s->blk_nnz = p->blk_nnz;
+    s->zskip = su->ell_halves && p->dkb_zero;
+    if (s->zskip && gext) {
+        const size_t per = (size_t)6 * p->lmax * 4 * bn;
+        for (int k = 0; k < npulse && s->zskip; k++)
+            if (!gade_dkb_zero(p, (const gc64 *)(gext + 2 * per * k))) s->zskip = 0;
+    }
     s->nsm = prop.multiProcessorCount;
     s->nsplit = 1;
     s->upd_block = 256;
@@ -1807,13 +1844,15 @@ static void k_apply_launch(const gade_solver *s, dim3 grid, int nt, size_t smem,
                            const typename Cx<R>::T *x, int mode, VecP V, RedP red)
 {
     const bool sep = mode == AX_RHS || mode == AX_PARTS || mode == AX_MIX;
-    if (s->rc) {
-        if (sep) k_apply<R, true, true><<<grid, nt, smem, st>>>(P, x, mode, V, red);
-        else k_apply<R, true, false><<<grid, nt, smem, st>>>(P, x, mode, V, red);
+#define KA(RC_, SEP_, Z_) k_apply<R, RC_, SEP_, Z_><<<grid, nt, smem, st>>>(P, x, mode, V, red)
+    if (s->zskip) {
+        if (s->rc) { if (sep) KA(true, true, true); else KA(true, false, true); }
+        else { if (sep) KA(false, true, true); else KA(false, false, true); }
     } else {
-        if (sep) k_apply<R, false, true><<<grid, nt, smem, st>>>(P, x, mode, V, red);
-        else k_apply<R, false, false><<<grid, nt, smem, st>>>(P, x, mode, V, red);
+        if (s->rc) { if (sep) KA(true, true, false); else KA(true, false, false); }
+        else { if (sep) KA(false, true, false); else KA(false, false, false); }
     }
+#undef KA
 }
 
 static int launch_apply(gade_solver *s, const double2 *x, int mode, VecP V, int redkind, cudaStream_t st,

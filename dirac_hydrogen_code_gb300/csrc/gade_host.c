@@ -260,6 +260,7 @@ int gade_problem_read(const char *dir, int lmax, gade_problem **out, char *err, 
         for (size_t i = 0; i < (size_t)hnnz * lmax && rcpl; i++)
             if (p->H0[i].re != 0.0 || p->H1[i].re != 0.0) rcpl = 0;
         p->real_coupling = rcpl;
+        p->dkb_zero = gade_dkb_zero(p, p->g);
     }
 
     for (int l = 0; l < 2 * lmax; l++) csr_free_(&H[l]);
@@ -331,6 +332,32 @@ static int band_lu(gc64 *band, int B, int bw)
     return 0;
 }
 
+/* 1 when the radial tables g ([a][l][q][blk_nnz], the loader's layout)
+   vanish where the DKB basis makes them vanish: with P0/Q0 the large and
+   Pk/Qk the kinetically balanced parts (Pk zero on the first radial half,
+   Qk on the second), g1 = <Pk|Q0> is zero on first-half rows, g2 = <P0|Qk>
+   on second-half columns and g3 = <Pk|Qk> outside (second-half rows,
+   first-half columns).  The per-step table M1 is then zero on second-half
+   columns and M3 on first-half columns, which the operator kernel skips. */
+int gade_dkb_zero(const gade_problem *p, const gc64 *g)
+{
+    const int B = p->blkdim, ns = B / 2;
+    if (B % 2) return 0;
+    const size_t bn = (size_t)p->blk_nnz;
+    for (int a = 0; a < 6; a++)
+        for (int l = 0; l < p->lmax; l++)
+            for (int q = 1; q < 4; q++) {
+                const gc64 *m = g + (((size_t)a * p->lmax + l) * 4 + q) * bn;
+                for (int32_t r = 0; r < B; r++)
+                    for (int32_t k = p->g_Ap[r]; k < p->g_Ap[r + 1]; k++) {
+                        const int c = p->g_Ai[k];
+                        const int zero = q == 1 ? r < ns : q == 2 ? c >= ns : !(r >= ns && c < ns);
+                        if (zero && (m[k].re != 0.0 || m[k].im != 0.0)) return 0;
+                    }
+            }
+    return 1;
+}
+
 int gade_problem_transpose_map(const gade_problem *p, int32_t *tpos)
 {
     for (int32_t r = 0; r < p->blkdim; r++)
@@ -361,18 +388,32 @@ int gade_setup_build(const gade_problem *p, double dt, double h, int chunk_splin
         s->row_kidx[r] = found;
     }
 
-    /* ELL view of the base pattern */
+    /* ELL view of the base pattern.  The DKB basis pairs spline s (first
+       radial half) with spline s of the second half; every entry couples
+       splines at most 7 apart.  When that holds the slots are laid out by
+       column half and spline offset (15 + 15), so slot t of a row always
+       means the same relative column and the first 15 slots hold exactly the
+       first-half columns.  Otherwise the slots follow CSR order. */
     int W = 0;
     for (int i = 0; i < B; i++) if (GAp[i + 1] - GAp[i] > W) W = GAp[i + 1] - GAp[i];
+    int halves = (B % 2 == 0);
+    const int ns = B / 2;
+    for (int i = 0; i < B && halves; i++)
+        for (int32_t k = GAp[i]; k < GAp[i + 1]; k++) {
+            const int d = GAi[k] % ns - i % ns;
+            if (d < -7 || d > 7) { halves = 0; break; }
+        }
+    if (halves) W = 30;
     s->W = W;
+    s->ell_halves = halves;
     s->ell_pos = malloc(sizeof(int32_t) * (size_t)W * B);
     s->ell_col = malloc(sizeof(int32_t) * (size_t)W * B);
-    for (int j = 0; j < W; j++)
-        for (int i = 0; i < B; i++) {
-            int32_t k = GAp[i] + j;
-            int ok = k < GAp[i + 1];
-            s->ell_pos[(size_t)j * B + i] = ok ? k : -1;
-            s->ell_col[(size_t)j * B + i] = ok ? GAi[k] : -1;
+    for (size_t e = 0; e < (size_t)W * B; e++) { s->ell_pos[e] = -1; s->ell_col[e] = -1; }
+    for (int i = 0; i < B; i++)
+        for (int32_t k = GAp[i]; k < GAp[i + 1]; k++) {
+            const int j = halves ? (GAi[k] >= ns ? 15 : 0) + (GAi[k] % ns - i % ns) + 7 : k - GAp[i];
+            s->ell_pos[(size_t)j * B + i] = k;
+            s->ell_col[(size_t)j * B + i] = GAi[k];
         }
 
     /* row chunks: spline s together with its partner s+B/2 when B is even */

@@ -36,6 +36,8 @@ typedef struct gade_problem {
     gc64 *psi0;                   /* psi0.vec values (n)               */
     int32_t *xperm;               /* psi0.vec permutation (n)          */
     int real_coupling;            /* g, gt real and H0l, H1l imaginary */
+    int dkb_zero;                 /* the radial tables vanish where the kinetically balanced
+                                     halves of the basis are zero (gade_dkb_zero) */
 } gade_problem;
 
 /* device-ready set-up arrays derived from a problem and a time step */
@@ -44,6 +46,8 @@ typedef struct gade_setup {
     int nk;                       /* number of distinct kappa values      */
     int *kvals;                   /* [nk]                                 */
     int *row_kidx;                /* [nblk] index into kvals              */
+    int ell_halves;               /* slots 0..14: columns of the first radial half, 15..29 the second,
+                                     slot = half*15 + (column spline - row spline + 7) */
     int32_t *ell_pos;             /* [W][B] CSR position or -1            */
     int32_t *ell_col;             /* [W][B] column or -1                  */
     /* row chunks: every block row is split into the same nchunk row sets */
@@ -82,6 +86,8 @@ void gade_setup_release(gade_setup *s);
 /* tpos[k]: CSR position of the transpose of base-pattern entry k; nonzero
    when the pattern is not structurally symmetric */
 int gade_problem_transpose_map(const gade_problem *p, int32_t *tpos);
+/* 1 when the radial tables g (loader layout) have the DKB zero blocks */
+int gade_dkb_zero(const gade_problem *p, const gc64 *g);
 
 /* kappa of an angular index, tools/solver_common.c:87-94 */
 int gade_ik(int i);
