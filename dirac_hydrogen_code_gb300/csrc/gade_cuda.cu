@@ -1356,6 +1356,7 @@ extern "C" int gade_problem_get_info(const gade_problem *p, gade_problem_info *i
     info->hall_nnz = p->hall_Ap[p->nblk];
     info->nnz_full = (int64_t)info->hall_nnz * p->blk_nnz;
     info->real_coupling = p->real_coupling;
+    info->dkb_zero = p->dkb_zero;
     return GADE_OK;
 }
 

@@ -26,7 +26,7 @@ class GadeError(RuntimeError):
 class ProblemInfo(C.Structure):
     _fields_ = [("lmax", C.c_int32), ("nblk", C.c_int32), ("blkdim", C.c_int32), ("blk_nnz", C.c_int32),
                 ("n", C.c_int64), ("hall_nnz", C.c_int64), ("nnz_full", C.c_int64),
-                ("real_coupling", C.c_int32)]
+                ("real_coupling", C.c_int32), ("dkb_zero", C.c_int32)]
 
 
 class StepStats(C.Structure):

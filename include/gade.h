@@ -41,6 +41,7 @@ typedef struct {
     int64_t hall_nnz;     /* non-zero blocks of H.csr                          */
     int64_t nnz_full;     /* non-zeros of the assembled operator (reference)   */
     int32_t real_coupling;/* 1: g real, H0l/H1l imaginary (fast path)          */
+    int32_t dkb_zero;     /* 1: g has the DKB zero blocks (the operator skips them) */
 } gade_problem_info;
 
 typedef struct {

@@ -36,6 +36,7 @@ def test_problem_load_on_host(workdirs, native_lib):
     p = Problem(d, info["lmax"])
     assert p.info["nblk"] == info["nblk"] and p.info["blkdim"] == info["blkdim"]
     assert p.info["nnz_full"] == info["nnz_full"] and p.info["real_coupling"] == 1
+    assert p.info["dkb_zero"] == 1          # the generated radial tables have the DKB zero blocks
     psi, perm = p.psi0()
     ref, rperm = formats.vec_read(os.path.join(d, "psi0.vec"))
     assert np.array_equal(psi, ref) and np.array_equal(perm, rperm)

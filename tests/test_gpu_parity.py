@@ -153,6 +153,33 @@ def test_general_complex_coupling(workdirs, native_lib, tmp_path):
     assert _rel(xg, xo) < 1e-12
 
 
+def test_without_dkb_zero_blocks(workdirs, native_lib, tmp_path):
+    """Radial tables that lack the DKB zero blocks take the four-term kernel
+    and still match the oracle."""
+    d, params, info, T, dt = _setup(workdirs, "tiny_nondipole")
+    d2 = str(tmp_path / "full")
+    shutil.copytree(d, d2)
+    rng = np.random.default_rng(12)
+    for l in range(info["lmax"]):
+        f = os.path.join(d2, f"g3a1l{l}.csr")          # fill g3's zero quadrants
+        m = formats.csr_read(f)
+        m.Ax = m.Ax + 1e-4 * rng.standard_normal(m.nnz) * np.max(np.abs(m.Ax))
+        formats.csr_write(f, m)
+    prob = Problem(d2, info["lmax"])
+    assert prob.info["dkb_zero"] == 0 and prob.info["real_coupling"] == 1
+    args = (d2, T, info["lmax"], params["Intensity"], params["Omega"], params["Cycles"], params["Ntime"])
+    sol = Solver(prob, dt)
+    p = O.load_problem(d2, info["lmax"])
+    ft = pulse(params["Intensity"], params["Omega"], params["Cycles"], 0.4 * T)
+    sol.set_time(ft)
+    x = rng.standard_normal(p.n) + 1j * rng.standard_normal(p.n)
+    _, _, hx = sol.apply(x, parts=True)
+    assert _rel(hx, O.timedep(p, dt, ft) @ x) < 1e-13
+    xo, ro, _ = O.run(*args, tol=1e-12, precond="blocklu", max_steps=5)
+    xg, rg, _ = run(*args, tol=1e-12, max_steps=5, write_outputs=False, problem=prob)
+    assert _rel(xg, xo) < 1e-12
+
+
 def test_edge_cases(workdirs, native_lib):
     d, params, info, T, dt = _setup(workdirs, "tiny_dipole")
     prob = Problem(d, info["lmax"])
