@@ -370,9 +370,10 @@ __device__ void reduce_finish(RedP red, double (&v)[NRED], double *sh, unsigned 
 /* per-step radial tables                                              */
 /* ------------------------------------------------------------------ */
 struct TabP {
-    int lmax, nk, W, B, blk_nnz;
-    const int *kvals, *ell_pos;
-    const void *g, *gt;           /* [pulse][lmax][3][4][blk_nnz] (a in the l-parity set) */
+    int lmax, nk, W, B;
+    const int *kvals;
+    const void *g, *gt;           /* [pulse][lmax][3][4][W][B]: ELL slot layout, zero on empty slots
+                                     (a in the l-parity set) */
     void *M;                      /* [pulse][lmax][nk][W][B] */
     const int *plist;             /* grid y -> pulse (NULL: pulse 0) */
     size_t gstride, mstride;      /* elements per pulse of g / gt and of M */
@@ -401,17 +402,16 @@ __global__ void k_tables(TabP T, const double2 *__restrict__ coef)
         }
     }
     const int l = (int)(tid / per_l);
-    const int slot = (int)(tid % per_l);      /* j*B + i */
-    const int k = T.ell_pos[slot];
+    const int slot = (int)(tid % per_l);      /* j*B + i: consecutive threads stream g, gt and M */
     if (RC) {
         typedef typename R4<R>::T Q4;
         double pg[4] = {0, 0, 0, 0}, pgt[4] = {0, 0, 0, 0};
-        if (k >= 0) {
+        {
             const double *g = (const double *)T.g, *gt = (const double *)T.gt;
             for (int ia = 0; ia < 3; ia++) {
                 const double c = coef[l * 3 + ia].y;
                 for (int q = 0; q < 4; q++) {
-                    size_t off = (((size_t)l * 3 + ia) * 4 + q) * T.blk_nnz + k;
+                    const size_t off = (((size_t)l * 3 + ia) * 4 + q) * per_l + slot;
                     pg[q] = fma(c, g[off], pg[q]);
                     pgt[q] = fma(c, gt[off], pgt[q]);
                 }
@@ -430,12 +430,12 @@ __global__ void k_tables(TabP T, const double2 *__restrict__ coef)
     } else {
         double2 pg[4], pgt[4];
         for (int q = 0; q < 4; q++) { pg[q] = make_double2(0, 0); pgt[q] = make_double2(0, 0); }
-        if (k >= 0) {
+        {
             const double2 *g = (const double2 *)T.g, *gt = (const double2 *)T.gt;
             for (int ia = 0; ia < 3; ia++) {
                 const double2 c = coef[l * 3 + ia];
                 for (int q = 0; q < 4; q++) {
-                    size_t off = (((size_t)l * 3 + ia) * 4 + q) * T.blk_nnz + k;
+                    const size_t off = (((size_t)l * 3 + ia) * 4 + q) * per_l + slot;
                     cfma(pg[q], c, g[off]);
                     cfma(pgt[q], c, gt[off]);
                 }
@@ -883,7 +883,9 @@ __device__ __forceinline__ void tma_bulk_load(void *dst, const void *src, unsign
 
 /* 4 warps per block row, one per SM sub-partition (each has its own FP64
  * unit): in every 32-row step warp w applies band terms d = 4w+1..4w+4 and
- * the inverse-block columns j = 8w..8w+7; partial sums meet in shared memory. */
+ * the inverse-block columns j = 8w..8w+7.  Partial sums meet in shared
+ * memory and warp 0 (its lanes are the chunk's rows) combines them once per
+ * row; the other warps read the combined values as broadcasts. */
 template <typename R, int BWP>
 __global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const typename Cx<R>::T *__restrict__ in0,
                                                      const typename Cx<R>::T *__restrict__ in1,
@@ -896,7 +898,7 @@ __global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const type
     extern __shared__ __align__(128) unsigned char smem_tma[];
     C *fac = (C *)smem_tma;          /* [2][CH]  */
     C *buf = fac + 2 * CH;                 /* [Bp]     */
-    C *pt = buf + Q.Bp;                    /* [4][32] partial t */
+    C *pt = buf + Q.Bp;                    /* [4][32] partial t, then t in pt[0..31] */
     C *py = pt + 128;                      /* [4][32] partial y */
     __shared__ __align__(8) uint64_t bar[2];
     __shared__ int all_ok;
@@ -997,17 +999,17 @@ __global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const type
         }
         pt[wid * 32 + lane] = t;
         __syncthreads();
+        if (wid == 0)                      /* the row's t from the four partials, once */
+            pt[lane] = mk<C>((t.x + pt[32 + lane].x) + (pt[64 + lane].x + pt[96 + lane].x),
+                             (t.y + pt[32 + lane].y) + (pt[64 + lane].y + pt[96 + lane].y));
+        __syncthreads();
         /* this warp's 8 columns of the inverse block */
         C a0 = mk<C>(0, 0), a1 = a0;
 #pragma unroll
         for (int q = 0; q < 8; q += 2) {
             const int j0 = wid * 8 + q, j1 = j0 + 1;
-            const C t0 = mk<C>((pt[j0].x + pt[32 + j0].x) + (pt[64 + j0].x + pt[96 + j0].x),
-                                            (pt[j0].y + pt[32 + j0].y) + (pt[64 + j0].y + pt[96 + j0].y));
-            const C t1 = mk<C>((pt[j1].x + pt[32 + j1].x) + (pt[64 + j1].x + pt[96 + j1].x),
-                                            (pt[j1].y + pt[32 + j1].y) + (pt[64 + j1].y + pt[96 + j1].y));
-            cfma(a0, F[j0 * 32 + lane], t0);
-            cfma(a1, F[j1 * 32 + lane], t1);
+            cfma(a0, F[j0 * 32 + lane], pt[j0]);
+            cfma(a1, F[j1 * 32 + lane], pt[j1]);
         }
         py[wid * 32 + lane] = mk<C>(a0.x + a1.x, a0.y + a1.y);
         __syncthreads();
@@ -1228,7 +1230,7 @@ struct gade_solver {
     void *d_ang_a0, *d_ang_a0k, *d_ang_a1, *d_ang_a1k;
     int *d_chunk_nrows, *d_chunk_ncols, *d_chunk_rows, *d_chunk_cols, *d_chunk_lcol;
     void *d_M, *d_S_ell, *d_Hst_ell, *d_D_ell;
-    int *d_kvals, *d_ell_pos;
+    int *d_kvals;
     void *d_g, *d_gt;
     int blk_nnz;
     /* preconditioner */
@@ -1597,7 +1599,7 @@ static int solver_create(const gade_problem *p, int npulse, const double *dts, c
     const size_t NP = (size_t)npulse;
     s->mstride = (size_t)s->lmax * s->nk * WB;
     s->dstride = (size_t)s->nk * WB;
-    s->gstride = (size_t)s->lmax * 3 * 4 * bn;
+    s->gstride = (size_t)s->lmax * 3 * 4 * WB;     /* radial tables in the ELL slot layout */
     s->bwp = s->bw <= 16 ? 16 : 32;
     if (s->bw > 32) { gade_setup_release(su); gade_solver_free(s); return fail(GADE_ERR_ARG, "preconditioner band %d wider than 32 is not supported", s->bw); }
     const int CH = 1024 + 32 * s->bwp;
@@ -1632,7 +1634,6 @@ static int solver_create(const gade_problem *p, int npulse, const double *dts, c
         if (rc) { gade_setup_release(su); gade_solver_free(s); return rc; }
     }
     UP(s->d_kvals, su->kvals, s->nk);
-    UP(s->d_ell_pos, su->ell_pos, WB);
     UP(s->d_ord, su->ord, s->B);
     {
         double2 *d;
@@ -1741,9 +1742,16 @@ static int solver_create(const gade_problem *p, int npulse, const double *dts, c
                 for (int ia = 0; ia < 3; ia++) {
                     int a = (l % 2 + 1) % 2 + 2 * ia;
                     for (int q = 0; q < 4; q++)
-                        for (size_t e = 0; e < bn; e++) {
-                            size_t src = (((size_t)a * s->lmax + l) * 4 + q) * bn + e;
-                            size_t dst = (((size_t)l * 3 + ia) * 4 + q) * bn + e;
+                        for (size_t slot = 0; slot < WB; slot++) {
+                            /* ELL slot layout: the table kernel streams them */
+                            const int e = su->ell_pos[slot];
+                            const size_t dst = (((size_t)l * 3 + ia) * 4 + q) * WB + slot;
+                            if (e < 0) {
+                                if (s->rc) { gr[dst] = 0.0; gtr[dst] = 0.0; }
+                                else { gc[dst] = make_double2(0, 0); gtc[dst] = make_double2(0, 0); }
+                                continue;
+                            }
+                            const size_t src = (((size_t)a * s->lmax + l) * 4 + q) * bn + e;
                             if (s->rc) { gr[dst] = g[src].re; gtr[dst] = gt[src].re; }
                             else { gc[dst] = make_double2(g[src].re, g[src].im); gtc[dst] = make_double2(gt[src].re, gt[src].im); }
                         }
@@ -1920,8 +1928,8 @@ static int fill_coef(gade_solver *s, int k, const double *ft)
 static int launch_table_kernels(gade_solver *s, int which, cudaStream_t st)
 {
     TabP T;
-    T.lmax = s->lmax; T.nk = s->nk; T.W = s->W; T.B = s->B; T.blk_nnz = s->blk_nnz;
-    T.kvals = s->d_kvals; T.ell_pos = s->d_ell_pos; T.g = s->d_g; T.gt = s->d_gt; T.M = s->d_M;
+    T.lmax = s->lmax; T.nk = s->nk; T.W = s->W; T.B = s->B;
+    T.kvals = s->d_kvals; T.g = s->d_g; T.gt = s->d_gt; T.M = s->d_M;
     T.plist = s->d_plist; T.gstride = s->gstride; T.mstride = s->mstride;
     long long total = (long long)s->lmax * s->W * s->B;
     int nt = 256;
