@@ -185,6 +185,12 @@ def run_ours(args):
     prob = native.Problem(tmp.name, info["lmax"])
     dt, steps = step_times(T, params["Ntime"])
     sol = native.Solver(prob, dt, 1.0, precision="fp64", device=device)
+    ns, split_ms = sol.split()
+    bal = sol.balanced()
+    partition = {"chosen": "balanced" if ns == 0 else f"order split {ns}",
+                 "apply_ms_timed_at_creation": {"balanced": bal["ms"],
+                                                **{f"split{k + 1}": v for k, v in enumerate(split_ms) if v > 0}},
+                 "balanced_ctas": bal["segments"], "balanced_pieces": bal["pieces"]}
     psi, _ = prob.psi0()
     sol.set_x(psi)
     stream = torch.cuda.ExternalStream(sol.stream(), device=device)
@@ -302,7 +308,9 @@ def run_ours(args):
             "data": "synthetic (generated dumpCouplings inputs)",
             "config": {"workload": WORKLOAD, "N": N, "nnz_equiv": nnz, "lmax": info["lmax"], "tol": TOL,
                        "l2": "flushed (256 MB write) between timed steps", "parallelism": f"replicas x{ws}",
-                       "iters_per_step": sorted(set(iters))},
+                       "iters_per_step": sorted(set(iters)),
+                       "iters_counting": "tools/bicgstab.c: the iteration that meets the tolerance is not counted",
+                       "operator_partition": partition},
             "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": 16 * N, "d2h_bytes_per_step": 16 * N},
             "gpu_launches": launches,
             "roofline": roof,

@@ -197,12 +197,17 @@ struct OpP {
     const int *plist;          /* grid x -> pulse (NULL: pulse 0) */
     long long vstride;         /* complex elements per pulse of every vector */
     size_t mstride, dstride;   /* elements per pulse of M and of Hst / D */
-    /* order split (one pulse only): nsplit CTAs share a (chunk, block row);
-       partial row sums go to split_acc [nsplit][3][nblk*B] and the last CTA
-       to arrive (split_tick [nchunk][nblk]) combines them in split order */
-    int nsplit;
-    void *split_acc;
-    unsigned int *split_tick;
+    /* partition of the work: unit u = (block row u / nchunk, chunk u % nchunk);
+       CTA y runs pieces seg_ptr[y] .. seg_ptr[y+1]-1 in order, a piece being
+       {unit, first active order, end, index within the unit | pieces of the
+       unit << 16}.  A unit cut into pieces leaves partial row sums in
+       piece_acc [piece][3][RM]; the last piece to arrive (unit_tick [unit])
+       sums them in piece order and runs the epilogue */
+    int nchunk;
+    const int *seg_ptr;
+    const int4 *pieces;
+    void *piece_acc;
+    unsigned int *unit_tick;
 };
 
 struct VecP {
@@ -250,24 +255,30 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double *sh)
     __syncthreads();
 }
 
-/* Per-CTA partials + last-CTA finalisation (fixed summation order).
-   ncta / cta: the CTAs of one pulse and this CTA's index among them. */
-__device__ void reduce_finish(RedP red, double (&v)[NRED], double *sh, unsigned ncta, unsigned cta)
+/* The CTA's block sum of v into partial slot idx (written by thread 0). */
+__device__ __forceinline__ void reduce_part(RedP red, double (&v)[NRED], double *sh, unsigned idx)
+{
+    block_sum<NRED>(v, sh);
+    if (threadIdx.x == 0)
+        for (int k = 0; k < NRED; k++) red.part[(size_t)idx * NRED + k] = v[k];
+}
+
+/* Arrival of one CTA (narrive CTAs per pulse); the last to arrive sums the
+   npart partial slots in index order and finalises the reduction. */
+__device__ void reduce_tail(RedP red, double *sh, unsigned narrive, unsigned npart)
 {
     __shared__ bool am_last;
     const int tid = threadIdx.x, nt = blockDim.x;
-    block_sum<NRED>(v, sh);
     if (tid == 0) {
-        for (int k = 0; k < NRED; k++) red.part[(size_t)cta * NRED + k] = v[k];
         __threadfence();
         unsigned t = atomicAdd(red.ticket, 1u);
-        am_last = (t == ncta - 1);
+        am_last = (t == narrive - 1);
     }
     __syncthreads();
     if (!am_last) return;
     __threadfence();
     double acc[NRED] = {0, 0, 0, 0};
-    for (unsigned j = tid; j < ncta; j += nt)
+    for (unsigned j = tid; j < npart; j += nt)
         for (int k = 0; k < NRED; k++) acc[k] += __ldcg(&red.part[(size_t)j * NRED + k]);
     block_sum<NRED>(acc, sh);
     if (tid == 0) {
@@ -364,6 +375,14 @@ __device__ void reduce_finish(RedP red, double (&v)[NRED], double *sh, unsigned 
         }
         *red.ticket = 0u;
     }
+}
+
+/* Per-CTA partials + last-CTA finalisation (fixed summation order).
+   ncta / cta: the CTAs of one pulse and this CTA's index among them. */
+__device__ void reduce_finish(RedP red, double (&v)[NRED], double *sh, unsigned ncta, unsigned cta)
+{
+    reduce_part(red, v, sh, cta);
+    reduce_tail(red, sh, ncta, ncta);
 }
 
 /* ------------------------------------------------------------------ */
@@ -483,9 +502,11 @@ __host__ __device__ __forceinline__ ApplySmem apply_smem(int CS, int W, int RM, 
 }
 
 /*
- * grid (pulse slot, row chunk, block row); two threads per output row (HJ
- * ELL slots each: HJ = (W+1)/2).  Per thread the local columns of its HJ
- * slots stay in registers for the whole kernel; empty slots point to a zero
+ * grid (pulse slot, segment): a unit is (block row, row chunk) and a segment
+ * a run of pieces of units (see OpP); one piece per unit and one unit per
+ * segment is the plain layout.  Two threads per output row (HJ ELL slots
+ * each: HJ = (W+1)/2).  Per thread the local columns of its HJ slots stay in
+ * registers for a piece; empty slots point to a zero
  * column, so the table loops carry no branch and unroll completely.  The four
  * contracted vectors u, w, u', w' of a column are interleaved (one 32- or
  * 64-byte record) and so are the four angular factors of a term.
@@ -518,26 +539,29 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 8 && SEP) ? 2 : 3)
     A4 *ang = (A4 *)(smem_raw + L.ang);       /* [AM] */
     double *shred = (double *)(smem_raw + L.shred); /* [NRED * blockDim] */
 
-    /* grid (pulse slot, chunk, block row): the slots of one chunk run side by
-       side, so the shared maps and angular tables come from L2 for all but one */
+    /* grid (pulse slot, segment): the slots of one segment run side by side,
+       so the shared maps and angular tables come from L2 for all but one */
     const int pulse = P.plist ? P.plist[blockIdx.x] : 0;
     if (!red_select(red, pulse)) return;
-    {
-        const long long vo = (long long)pulse * P.vstride;
-        x += vo;
-        if (V.out0) V.out0 = (C *)V.out0 + vo;
-        if (V.out1) V.out1 = (C *)V.out1 + vo;
-        if (V.out2) V.out2 = (C *)V.out2 + vo;
-        if (V.in0) V.in0 = (const C *)V.in0 + vo;
-        if (V.in1) V.in1 = (const C *)V.in1 + vo;
-        if (RC) P.M = (const typename R4<R>::T *)P.M + (size_t)pulse * P.mstride;
-        else P.M = (const C4<C> *)P.M + (size_t)pulse * P.mstride;
-        P.Hst_ell = (const C *)P.Hst_ell + (size_t)pulse * P.dstride;
-        P.D_ell = (const C *)P.D_ell + (size_t)pulse * P.dstride;
-    }
-    const int q = blockIdx.y, r = blockIdx.z / P.nsplit, sp = blockIdx.z - r * P.nsplit;
+    /* the pulse's vectors and tables: offsets applied where they are used,
+       so the pointers stay in the parameter space across the pieces */
+    x += (long long)pulse * P.vstride;
     const int tid = threadIdx.x, nt = blockDim.x;
     const int B = P.B, W = P.W, CM = P.CM;
+    if (tid == 0) {                           /* the zero column: empty slots and columns past a chunk */
+        const C z = mk<C>(0, 0);
+        xr[CM] = z; xs[CM] = z; ds[CM] = z;
+        C4<C> z4; z4.a = z; z4.b = z; z4.c = z; z4.d = z;
+        for (int g = 0; g < G; g++) ub[g * CS + CM] = z4;
+    }
+    /* this CTA's segment: pieces (unit, order range) in sequence order.  The
+       piece's scalars are kept in shared memory and read back after the
+       order loop, which leaves the loop its registers */
+    __shared__ int s_pc, s_pw;
+    for (int pc = P.seg_ptr[blockIdx.y]; pc < P.seg_ptr[blockIdx.y + 1]; pc = *(volatile int *)&s_pc + 1) {
+    const int4 pd = P.pieces[pc];
+    const int u = pd.x, r = u / P.nchunk, q = u - r * P.nchunk;
+    if (tid == 0) { s_pc = pc; s_pw = pd.w; }
     const int kk = P.row_kidx[r];
     const int nrows = P.chunk_nrows[q], ncols = P.chunk_ncols[q];
     /* two threads per output row, each with half of the ELL slots */
@@ -547,15 +571,10 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 8 && SEP) ? 2 : 3)
     const int nj = je - jb;                   /* <= HJ */
     const int *cols = P.chunk_cols + (size_t)q * CM;
     const C *xb = x + (size_t)r * B;
+    __syncthreads();                          /* the previous piece is done with shared memory */
     {
         const int *gl = P.chunk_lcol + (size_t)q * W * P.RM;
         for (int e = tid; e < W * P.RM; e += nt) { const int v = gl[e]; lcs[e] = v < 0 ? CM : v; }
-        if (tid == 0) {
-            const C z = mk<C>(0, 0);
-            xr[CM] = z; xs[CM] = z; ds[CM] = z;
-            C4<C> z4; z4.a = z; z4.b = z; z4.c = z; z4.d = z;
-            for (int g = 0; g < G; g++) ub[g * CS + CM] = z4;
-        }
     }
     const int ea = P.ang_ptr[r * P.lmax], eb = P.ang_ptr[r * P.lmax + P.lmax];
     for (int e = tid; e < eb - ea; e += nt) {
@@ -579,7 +598,8 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 8 && SEP) ? 2 : 3)
 
     for (int c = tid; c < ncols; c += nt) xr[c] = xb[cols[c]];
     if (mode == AX_MIX) {
-        const C *xn = (const C *)V.in0 + (size_t)r * B, *dn = (const C *)V.in1 + (size_t)r * B;
+        const size_t vo = (size_t)pulse * P.vstride + (size_t)r * B;
+        const C *xn = (const C *)V.in0 + vo, *dn = (const C *)V.in1 + vo;
         for (int c = tid; c < ncols; c += nt) { xs[c] = xn[cols[c]]; ds[c] = dn[cols[c]]; }
     }
     __syncthreads();
@@ -587,20 +607,26 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 8 && SEP) ? 2 : 3)
     /* this thread's slots: local column (CM when empty or past the half);
        table rows advance by B per slot and stay on the half's last slot
        past its end (the product is zero there) */
-    int lco[HJ];
+    /* two 16-bit local columns per register (CM < 2^16) */
+    unsigned lcp[(HJ + 1) / 2];
 #pragma unroll
-    for (int t = 0; t < HJ; t++) lco[t] = (t < nj && trow < P.RM) ? lcs[(jb + t) * P.RM + trow] : CM;
+    for (int t = 0; t < HJ; t += 2) {
+        const unsigned c0 = (t < nj && trow < P.RM) ? lcs[(jb + t) * P.RM + trow] : CM;
+        const unsigned c1 = (t + 1 < HJ && t + 1 < nj && trow < P.RM) ? lcs[(jb + t + 1) * P.RM + trow] : CM;
+        lcp[t / 2] = c0 | (c1 << 16);
+    }
+#define LCO(t) ((int)(((t) & 1) ? (lcp[(t) >> 1] >> 16) : (lcp[(t) >> 1] & 0xffffu)))
     const int jB = jb * B;
 
     C accS = mk<C>(0, 0), accH = mk<C>(0, 0), accD = mk<C>(0, 0);
-    if (i >= 0 && sp == 0) {                  /* diagonal blocks: the first split */
+    if (i >= 0 && (pd.w & 0xffff) == 0) {     /* diagonal blocks: the unit's first piece */
         if (SEP && mode == AX_MIX) {
             /* x = w = 2 x_n + delta: S x_n, S delta and (i h dt/2 h0) w */
             const C *Se = (const C *)P.S_ell + (size_t)kk * W * B + i + jB;
-            const C *He = (const C *)P.Hst_ell + (size_t)kk * W * B + i + jB;
+            const C *He = (const C *)P.Hst_ell + (size_t)pulse * P.dstride + (size_t)kk * W * B + i + jB;
 #pragma unroll
             for (int t = 0; t < HJ; t++) {
-                const int lc = lco[t];
+                const int lc = LCO(t);
                 const C sv = *Se;
                 cfma(accS, sv, xs[lc]);
                 cfma(accD, sv, ds[lc]);
@@ -609,33 +635,26 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 8 && SEP) ? 2 : 3)
             }
         } else if (SEP) {
             const C *Se = (const C *)P.S_ell + (size_t)kk * W * B + i + jB;
-            const C *He = (const C *)P.Hst_ell + (size_t)kk * W * B + i + jB;
+            const C *He = (const C *)P.Hst_ell + (size_t)pulse * P.dstride + (size_t)kk * W * B + i + jB;
 #pragma unroll
             for (int t = 0; t < HJ; t++) {
-                const C xv = xr[lco[t]];
+                const C xv = xr[LCO(t)];
                 cfma(accS, *Se, xv);
                 cfma(accH, *He, xv);
                 if (t + 1 < nj) { Se += B; He += B; }
             }
         } else {
-            const C *De = (const C *)P.D_ell + (size_t)kk * W * B + i + jB;
+            const C *De = (const C *)P.D_ell + (size_t)pulse * P.dstride + (size_t)kk * W * B + i + jB;
 #pragma unroll
             for (int t = 0; t < HJ; t++) {
-                cfma(accH, *De, xr[lco[t]]);
+                cfma(accH, *De, xr[LCO(t)]);
                 if (t + 1 < nj) De += B;
             }
         }
     }
 
-    int a_beg = P.act_ptr[r], a_end = P.act_ptr[r + 1];
-    if (P.nsplit > 1) {                       /* this CTA's share of the orders, whole gather groups */
-        const int na = a_end - a_beg;
-        const int per = ((na + P.nsplit - 1) / P.nsplit + G - 1) / G * G;
-        const int b0 = a_beg + sp * per < a_end ? a_beg + sp * per : a_end;
-        a_end = b0 + per < a_end ? b0 + per : a_end;
-        a_beg = b0;
-    }
-    for (int ag = a_beg; ag < a_end; ag += G) {
+    const int a_end = pd.z;
+    for (int ag = pd.y; ag < a_end; ag += G) {
         const int ng = a_end - ag < G ? a_end - ag : G;
         __syncthreads();     /* staging done / previous group's apply done */
         /* gather u, w, u', w' of ng orders at once: (order, column) items */
@@ -649,25 +668,25 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 8 && SEP) ? 2 : 3)
                second-half column no w */
             const bool qcol = gc >= (B >> 1);
             const bool need_b = !Z || !qcol, need_d = !Z || qcol;
-            C4<C> u;
-            u.a = mk<C>(0, 0); u.b = u.a; u.c = u.a; u.d = u.a;
+            C4<C> uv;
+            uv.a = mk<C>(0, 0); uv.b = uv.a; uv.c = uv.a; uv.d = uv.a;
 #pragma unroll 4
             for (int e = e0; e < e1; e++) {
                 const C xv = xc[(size_t)angc[e] * B];
                 const A4 a = ang[e];
                 if constexpr (RC) {
-                    rfma(u.a, a.a, xv);
-                    if (need_b) rfma(u.b, a.b, xv);
-                    rfma(u.c, a.c, xv);
-                    if (need_d) rfma(u.d, a.d, xv);
+                    rfma(uv.a, a.a, xv);
+                    if (need_b) rfma(uv.b, a.b, xv);
+                    rfma(uv.c, a.c, xv);
+                    if (need_d) rfma(uv.d, a.d, xv);
                 } else {
-                    cfma(u.a, a.a, xv);
-                    if (need_b) cfma(u.b, a.b, xv);
-                    cfma(u.c, a.c, xv);
-                    if (need_d) cfma(u.d, a.d, xv);
+                    cfma(uv.a, a.a, xv);
+                    if (need_b) cfma(uv.b, a.b, xv);
+                    cfma(uv.c, a.c, xv);
+                    if (need_d) cfma(uv.d, a.d, xv);
                 }
             }
-            ub[g * CS + c] = u;
+            ub[g * CS + c] = uv;
         }
         __syncthreads();
         if (i >= 0) {
@@ -676,36 +695,36 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 8 && SEP) ? 2 : 3)
                 const C4<C> *ug = ub + g * CS;
                 if constexpr (RC) {
                     typedef typename R4<R>::T Q4;
-                    const Q4 *Mt = (const Q4 *)P.M + ((size_t)l * P.nk + kk) * W * B + i + jB;
+                    const Q4 *Mt = (const Q4 *)P.M + (size_t)pulse * P.mstride + ((size_t)l * P.nk + kk) * W * B + i + jB;
                     const bool second = half == 1;
 #pragma unroll
                     for (int t = 0; t < HJ; t++) {
                         const Q4 m = *Mt;
-                        const C4<C> u = ug[lco[t]];
-                        rfma(accH, m.a, u.a);
-                        rfma(accH, m.c, u.c);
+                        const C4<C> uv = ug[LCO(t)];
+                        rfma(accH, m.a, uv.a);
+                        rfma(accH, m.c, uv.c);
                         if (Z) {
-                            rfma(accH, second ? m.d : m.b, second ? u.d : u.b);
+                            rfma(accH, second ? m.d : m.b, second ? uv.d : uv.b);
                         } else {
-                            rfma(accH, m.b, u.b);
-                            rfma(accH, m.d, u.d);
+                            rfma(accH, m.b, uv.b);
+                            rfma(accH, m.d, uv.d);
                         }
                         if (t + 1 < nj) Mt += B;
                     }
                 } else {
-                    const C4<C> *Mt = (const C4<C> *)P.M + ((size_t)l * P.nk + kk) * W * B + i + jB;
+                    const C4<C> *Mt = (const C4<C> *)P.M + (size_t)pulse * P.mstride + ((size_t)l * P.nk + kk) * W * B + i + jB;
                     const bool second = half == 1;
 #pragma unroll
                     for (int t = 0; t < HJ; t++) {
                         const C4<C> m = *Mt;
-                        const C4<C> u = ug[lco[t]];
-                        cfma(accH, m.a, u.a);
-                        cfma(accH, m.c, u.c);
+                        const C4<C> uv = ug[LCO(t)];
+                        cfma(accH, m.a, uv.a);
+                        cfma(accH, m.c, uv.c);
                         if (Z) {
-                            cfma(accH, second ? m.d : m.b, second ? u.d : u.b);
+                            cfma(accH, second ? m.d : m.b, second ? uv.d : uv.b);
                         } else {
-                            cfma(accH, m.b, u.b);
-                            cfma(accH, m.d, u.d);
+                            cfma(accH, m.b, uv.b);
+                            cfma(accH, m.d, uv.d);
                         }
                         if (t + 1 < nj) Mt += B;
                     }
@@ -714,6 +733,7 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 8 && SEP) ? 2 : 3)
         }
     }
 
+#undef LCO
     /* combine the two halves of every row */
     __syncthreads();
     {
@@ -733,42 +753,45 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 8 && SEP) ? 2 : 3)
         }
         __syncthreads();
     }
-    if (P.nsplit > 1) {
-        /* partial row sums of this split; the last split of the (chunk, row)
-           sums all of them in split order and runs the epilogue */
-        __shared__ int split_last;
-        const size_t n = (size_t)P.nblk * B;
-        C *acc = (C *)P.split_acc;
-        const size_t gi = (size_t)r * B + i;
+    const int pw = *(volatile int *)&s_pw;
+    const int pi = pw & 0xffff, np = pw >> 16;          /* piece index within the unit, pieces of the unit */
+    if (np > 1) {
+        /* a unit cut into pieces: partial row sums per piece; the last piece
+           to arrive sums them in piece order and runs the epilogue */
+        const int pc = *(volatile int *)&s_pc;
+        __shared__ int piece_last;
+        C *acc = (C *)P.piece_acc;
+        const size_t RM3 = (size_t)3 * P.RM;
         if (half == 0 && i >= 0) {
-            acc[((size_t)sp * 3 + 1) * n + gi] = accH;
-            if (SEP) { acc[((size_t)sp * 3) * n + gi] = accS; acc[((size_t)sp * 3 + 2) * n + gi] = accD; }
+            acc[pc * RM3 + P.RM + trow] = accH;
+            if (SEP) { acc[pc * RM3 + trow] = accS; acc[pc * RM3 + 2 * P.RM + trow] = accD; }
         }
         __threadfence();
         __syncthreads();
         if (tid == 0) {
-            const unsigned t = atomicAdd(&P.split_tick[(size_t)q * P.nblk + r], 1u);
-            split_last = (t == (unsigned)P.nsplit - 1u);
+            const unsigned t = atomicAdd(&P.unit_tick[u], 1u);
+            piece_last = (t == (unsigned)np - 1u);
         }
         __syncthreads();
-        if (!split_last) return;
+        if (!piece_last) continue;
         __threadfence();
         if (half == 0 && i >= 0) {
             accS = mk<C>(0, 0); accH = accS; accD = accS;
-            for (int k = 0; k < P.nsplit; k++) {
-                accH = cadd(accH, __ldcg(&acc[((size_t)k * 3 + 1) * n + gi]));
+            for (int k = 0; k < np; k++) {
+                const size_t pk = (size_t)(pc - pi + k) * RM3;
+                accH = cadd(accH, __ldcg(&acc[pk + P.RM + trow]));
                 if (SEP) {
-                    accS = cadd(accS, __ldcg(&acc[((size_t)k * 3) * n + gi]));
-                    accD = cadd(accD, __ldcg(&acc[((size_t)k * 3 + 2) * n + gi]));
+                    accS = cadd(accS, __ldcg(&acc[pk + trow]));
+                    accD = cadd(accD, __ldcg(&acc[pk + 2 * P.RM + trow]));
                 }
             }
         }
-        if (tid == 0) P.split_tick[(size_t)q * P.nblk + r] = 0u;
+        if (tid == 0) P.unit_tick[u] = 0u;
     }
     /* epilogue */
     double v[NRED] = {0, 0, 0, 0};
     if (half == 0 && i >= 0) {
-        const size_t gi = (size_t)r * B + i;
+        const size_t gi = (size_t)pulse * P.vstride + (size_t)r * B + i;
         const C ax = SEP ? cadd(accH, accS) : accH;
         switch (mode) {
         case AX_PLAIN:
@@ -823,7 +846,11 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 8 && SEP) ? 2 : 3)
         }
         }
     }
-    if (red.kind != RED_NONE) reduce_finish(red, v, shred, gridDim.y * (gridDim.z / P.nsplit), r * gridDim.y + q);
+    /* the unit's dot partials, indexed by unit (not by CTA): the final sum
+       has the same order for every partition */
+    if (red.kind != RED_NONE) reduce_part(red, v, shred, (unsigned)u);
+    }
+    if (red.kind != RED_NONE) reduce_tail(red, shred, gridDim.y, (unsigned)(P.nchunk * P.nblk));
 }
 
 /* ------------------------------------------------------------------ */
@@ -1211,6 +1238,14 @@ __global__ void k_mixed_ctl(BPred bp)
 /* ------------------------------------------------------------------ */
 /* solver object                                                       */
 /* ------------------------------------------------------------------ */
+/* one partition of the operator's units into CTA segments (see OpP) */
+struct PartList {
+    int nseg = 0, npieces = 0;
+    int multi = 0;              /* some unit has more than one piece */
+    int *d_seg_ptr = nullptr;
+    int4 *d_pieces = nullptr;
+};
+
 struct gade_solver {
     int device;
     cudaStream_t stream;
@@ -1265,14 +1300,22 @@ struct gade_solver {
     double2 *xprev, *delta64;
     DevScal *d_sc2, *h_sc2;
     int *d_hprev;               /* [pulse] x_prev exists (batched mixed precision) */
-    /* order split of the operator kernel (single-pulse solvers) */
+    /* partition of the operator's work into CTAs (single-pulse solvers):
+       order split 1-4 (nsplit) or balanced segments (nsplit 0, one list per
+       resident-CTAs-per-SM count of the kernel instance) */
     int nsplit;
-    void *d_split_acc;
-    unsigned int *d_split_tick;
     int nsm;
-    float split_ms[5];          /* autotuner: FP64 (+ complex64) apply time per split count */
+    float split_ms[5];          /* timed FP64 (+ complex64) applies: [0] balanced, [1..4] order splits */
+    PartList part_split[5];
+    PartList part_bal[9];
+    int occ[2][2];              /* resident CTAs per SM of the operator instances [complex64][sep] */
+    void *d_piece_acc;
+    size_t piece_cap;           /* pieces the partial-sum scratch holds */
+    unsigned int *d_unit_tick;
+    /* host copy of the work model: active orders per block row, their
+       angular term counts, rows and columns per chunk */
+    std::vector<int> h_act_ptr, h_act_ne, h_chunk_nrows, h_chunk_ncols;
     gade_batch *engine;         /* step engine of a single-pulse solver (device control, graphs) */
-    int split_cap;              /* splits the scratch holds */
     int zskip;                  /* the DKB zero blocks hold for every pulse's tables */
 };
 
@@ -1400,6 +1443,8 @@ extern "C" void gade_solver_free(gade_solver *s)
     delete s;
 }
 
+static int part_reset(gade_solver *s);
+
 static int choose_chunk_splines(int nblk, int B, int nsm)
 {
     int half = (B % 2 == 0) ? B / 2 : B;
@@ -1456,7 +1501,17 @@ static int set_chunking(gade_solver *s, const gade_setup *su)
             fmas += terms * fma_c * (double)s->blk_nnz;            /* radial tables */
         }
     s->apply_flops = 2.0 * fmas;
-    return GADE_OK;
+    /* host copy of the work model for the partitions */
+    s->h_act_ptr.assign(su->act_ptr, su->act_ptr + s->nblk + 1);
+    s->h_act_ne.assign((size_t)su->act_ptr[s->nblk], 0);
+    for (int r = 0; r < s->nblk; r++)
+        for (int a = su->act_ptr[r]; a < su->act_ptr[r + 1]; a++) {
+            const int l = su->act_l[a];
+            s->h_act_ne[a] = su->ang_ptr[r * s->lmax + l + 1] - su->ang_ptr[r * s->lmax + l];
+        }
+    s->h_chunk_nrows.assign(su->chunk_nrows, su->chunk_nrows + s->nchunk);
+    s->h_chunk_ncols.assign(su->chunk_ncols, su->chunk_ncols + s->nchunk);
+    return part_reset(s);
 }
 
 /* chunk-packed block-LU factors of one pulse: [nk][nch][Linv | masked band] */
@@ -1821,8 +1876,9 @@ static OpP op_params(const gade_solver *s)
     P.chunk_cols = s->d_chunk_cols; P.chunk_lcol = s->d_chunk_lcol;
     P.M = s->d_M; P.S_ell = s->d_S_ell; P.Hst_ell = s->d_Hst_ell; P.D_ell = s->d_D_ell;
     P.plist = s->d_plist; P.vstride = s->n; P.mstride = s->mstride; P.dstride = s->dstride;
-    P.nsplit = s->nsplit > 1 ? s->nsplit : 1;
-    P.split_acc = s->d_split_acc; P.split_tick = s->d_split_tick;
+    P.nchunk = s->nchunk;
+    P.seg_ptr = s->part_split[1].d_seg_ptr; P.pieces = s->part_split[1].d_pieces;
+    P.piece_acc = s->d_piece_acc; P.unit_tick = s->d_unit_tick;
     return P;
 }
 
@@ -1864,12 +1920,185 @@ static void k_apply_launch(const gade_solver *s, dim3 grid, int nt, size_t smem,
 #undef KA
 }
 
+/* resident CTAs per SM of the operator instance for a precision and mode class */
+template <typename R>
+static int apply_occupancy(const gade_solver *s, bool sep)
+{
+    int nt;
+    size_t smem;
+    apply_dims(s, sizeof(typename Cx<R>::T), &nt, &smem);
+    int n = 0;
+    cudaError_t e = cudaSuccess;
+#define OC(RC_, SEP_, Z_) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_apply<R, RC_, SEP_, Z_>, nt, smem)
+    if (s->zskip) {
+        if (s->rc) { if (sep) OC(true, true, true); else OC(true, false, true); }
+        else { if (sep) OC(false, true, true); else OC(false, false, true); }
+    } else {
+        if (s->rc) { if (sep) OC(true, true, false); else OC(true, false, false); }
+        else { if (sep) OC(false, true, false); else OC(false, false, false); }
+    }
+#undef OC
+    if (e != cudaSuccess || n < 1) { cudaGetLastError(); n = 1; }
+    return n > 8 ? 8 : n;
+}
+
+static void part_release(gade_solver *s, PartList &pl)
+{
+    dev_release(s, pl.d_seg_ptr);
+    dev_release(s, pl.d_pieces);
+    pl = PartList();
+}
+
+static int part_upload(gade_solver *s, PartList &pl, const std::vector<int> &seg, const std::vector<int4> &pcs)
+{
+    part_release(s, pl);
+    int rc;
+    if ((rc = dev_upload(s, &pl.d_seg_ptr, seg.data(), seg.size()))) return rc;
+    if ((rc = dev_upload(s, &pl.d_pieces, pcs.data(), pcs.size()))) return rc;
+    pl.nseg = (int)seg.size() - 1;
+    pl.npieces = (int)pcs.size();
+    for (const int4 &pc : pcs)
+        if ((pc.w >> 16) > 1) pl.multi = 1;
+    if (pl.multi && (size_t)pl.npieces > s->piece_cap) {
+        dev_release(s, s->d_piece_acc);
+        s->d_piece_acc = nullptr;
+        s->piece_cap = 0;
+        double2 *acc = nullptr;
+        if ((rc = dev_upload(s, &acc, (const double2 *)nullptr, (size_t)pl.npieces * 3 * s->RM))) return rc;
+        s->d_piece_acc = acc;
+        s->piece_cap = (size_t)pl.npieces;
+    }
+    return GADE_OK;
+}
+
+/* Order split: ns pieces per unit, each with a share of the active orders
+   (whole FP64 gather groups), one piece per segment. */
+static int part_build_split(gade_solver *s, int ns)
+{
+    std::vector<int> seg(1, 0);
+    std::vector<int4> pcs;
+    const int nunit = s->nchunk * s->nblk;
+    for (int u = 0; u < nunit; u++) {
+        const int r = u / s->nchunk;
+        const int a0 = s->h_act_ptr[r], a1 = s->h_act_ptr[r + 1], na = a1 - a0;
+        const int per = ((na + ns - 1) / ns + 1) / 2 * 2;
+        for (int sp = 0; sp < ns; sp++) {
+            const int b0 = std::min(a0 + sp * per, a1), b1 = std::min(b0 + per, a1);
+            pcs.push_back(make_int4(u, b0, b1, sp | (ns << 16)));
+            seg.push_back((int)pcs.size());
+        }
+    }
+    return part_upload(s, s->part_split[ns], seg, pcs);
+}
+
+/* Balanced segments: the units' work, in unit order, laid on one line by a
+   cost model (FMAs of the gather and the table products of every active
+   order, the diagonal blocks and the staging of a unit) and cut into nseg
+   equal lengths, one segment per resident CTA; an order goes to the segment
+   that holds its midpoint, so a unit's orders fall into consecutive pieces.
+   With every segment resident at once, the SMs finish together. */
+static int part_build_balanced(gade_solver *s, int nseg, PartList &pl)
+{
+    const int nunit = s->nchunk * s->nblk;
+    const double terms = s->zskip ? 3.0 : 4.0, fc = s->rc ? 2.0 : 4.0;
+    auto ocost = [&](int a, int q) {
+        return terms * fc * ((double)s->h_act_ne[a] * s->h_chunk_ncols[q] + (double)s->h_chunk_nrows[q] * s->W);
+    };
+    auto ufix = [&](int q) { return 6.0 * s->h_chunk_nrows[q] * s->W; };
+    double total = 0;
+    for (int u = 0; u < nunit; u++) {
+        const int r = u / s->nchunk, q = u - r * s->nchunk;
+        total += ufix(q);
+        for (int a = s->h_act_ptr[r]; a < s->h_act_ptr[r + 1]; a++) total += ocost(a, q);
+    }
+    const double T = total / nseg;
+    auto seg_of = [&](double mid) { int k = (int)(mid / T); return k < 0 ? 0 : (k >= nseg ? nseg - 1 : k); };
+    std::vector<int4> pcs;
+    std::vector<int> pseg;                 /* segment of each piece */
+    double pos = 0;
+    for (int u = 0; u < nunit; u++) {
+        const int r = u / s->nchunk, q = u - r * s->nchunk;
+        const int a0 = s->h_act_ptr[r], a1 = s->h_act_ptr[r + 1];
+        const double f = ufix(q);
+        const size_t first = pcs.size();
+        if (a0 == a1) {
+            pcs.push_back(make_int4(u, a0, a0, 0));
+            pseg.push_back(seg_of(pos + 0.5 * f));
+        }
+        pos += f;
+        int cur = -1, b0 = a0;
+        for (int a = a0; a < a1; a++) {
+            const double c = ocost(a, q);
+            const int sg = seg_of(pos + 0.5 * c);
+            pos += c;
+            if (sg != cur) {
+                if (cur >= 0) { pcs.push_back(make_int4(u, b0, a, 0)); pseg.push_back(cur); }
+                cur = sg;
+                b0 = a;
+            }
+        }
+        if (a1 > a0) { pcs.push_back(make_int4(u, b0, a1, 0)); pseg.push_back(cur); }
+        const int np = (int)(pcs.size() - first);
+        for (int k = 0; k < np; k++) pcs[first + k].w = k | (np << 16);
+    }
+    std::vector<int> seg((size_t)nseg + 1, 0);
+    for (int sg : pseg) seg[sg + 1]++;
+    for (int k = 0; k < nseg; k++) seg[k + 1] += seg[k];
+    return part_upload(s, pl, seg, pcs);
+}
+
+/* the balanced lists of every operator instance the solver launches */
+static int part_build_balanced_all(gade_solver *s)
+{
+    for (int f = 0; f < 2; f++) {
+        if (f == 1 && s->prec != GADE_PREC_MIXED) continue;
+        for (int sep = 0; sep < 2; sep++) {
+            const int o = s->occ[f][sep];
+            if (s->part_bal[o].nseg) continue;
+            int rc = part_build_balanced(s, o * s->nsm, s->part_bal[o]);
+            if (rc) return rc;
+        }
+    }
+    return GADE_OK;
+}
+
+/* after (re)chunking: the plain one-piece-per-unit list, nothing else */
+static int part_reset(gade_solver *s)
+{
+    for (PartList &pl : s->part_split) part_release(s, pl);
+    for (PartList &pl : s->part_bal) part_release(s, pl);
+    dev_release(s, s->d_piece_acc);
+    s->d_piece_acc = nullptr;
+    s->piece_cap = 0;
+    dev_release(s, s->d_unit_tick);
+    s->d_unit_tick = nullptr;
+    int rc;
+    if ((rc = dev_upload(s, &s->d_unit_tick, (const unsigned *)nullptr, (size_t)s->nchunk * s->nblk))) return rc;
+    for (int f = 0; f < 2; f++)
+        for (int sep = 0; sep < 2; sep++)
+            s->occ[f][sep] = f ? apply_occupancy<float>(s, sep) : apply_occupancy<double>(s, sep);
+    s->nsplit = 1;
+    return part_build_split(s, 1);
+}
+
+/* the partition a launch uses: its segment list in P, the segment count returned */
+static int op_partition(const gade_solver *s, OpP &P, bool fp32, int mode)
+{
+    const bool sep = mode == AX_RHS || mode == AX_PARTS || mode == AX_MIX;
+    const PartList *pl = &s->part_split[1];
+    if (s->nsplit >= 2 && s->nsplit <= 4 && s->part_split[s->nsplit].nseg) pl = &s->part_split[s->nsplit];
+    else if (s->nsplit == 0 && s->part_bal[s->occ[fp32][sep]].nseg) pl = &s->part_bal[s->occ[fp32][sep]];
+    P.seg_ptr = pl->d_seg_ptr;
+    P.pieces = pl->d_pieces;
+    return pl->nseg;
+}
+
 static int launch_apply(gade_solver *s, const double2 *x, int mode, VecP V, int redkind, cudaStream_t st,
                         int pred = PRED_NONE, DevScal *pb = nullptr)
 {
     OpP P = op_params(s);
     RedP red = make_red(s, s->d_sc, redkind, pred, nullptr, pb);
-    dim3 grid(s->nslot, s->nchunk, s->nblk * P.nsplit);
+    dim3 grid(s->nslot, op_partition(s, P, false, mode));
     int nt;
     size_t smem;
     apply_dims(s, sizeof(double2), &nt, &smem);
@@ -2067,7 +2296,7 @@ static int launch_apply32(gade_solver *s, const float2 *x, int mode, VecP V, int
 {
     OpP P = op_params32(s);
     RedP red = make_red(s, sc, redkind, pred);
-    dim3 grid(s->nslot, s->nchunk, s->nblk * P.nsplit);
+    dim3 grid(s->nslot, op_partition(s, P, true, mode));
     int nt;
     size_t smem;
     apply_dims(s, sizeof(float2), &nt, &smem);
@@ -2094,11 +2323,13 @@ static int launch_precond32(gade_solver *s, int mode, const float2 *in0, const f
 }
 
 /*
- * Order split of a single pulse: when one pulse's (chunk, block row) CTAs
- * are too few to balance the SMs, 2-4 CTAs share each (chunk, block row),
- * each with a part of the Bessel orders.  The count is chosen by timing the
+ * Partition of a single pulse's operator work: when one pulse's (chunk, block
+ * row) units are too few or too uneven to balance the SMs, either 2-4 CTAs
+ * share each unit (order split) or the balanced segments cut the work into
+ * one equal share per resident CTA.  The choice is made by timing the
  * operator (FP64, plus two complex64 applies in mixed precision) for every
- * candidate on the zeroed tables, once at creation.
+ * candidate on the zeroed tables, once at creation; a candidate after the
+ * plain layout is kept only for a clear gain.
  */
 static int choose_split(gade_solver *s)
 {
@@ -2106,16 +2337,17 @@ static int choose_split(gade_solver *s)
     int maxs = (int)((8LL * s->nsm + ctas - 1) / ctas);
     if (maxs > 4) maxs = 4;
     for (int k = 0; k < 5; k++) s->split_ms[k] = 0.f;
-    if (maxs <= 1) return GADE_OK;
     int rc;
-    if ((rc = dev_upload(s, (double2 **)&s->d_split_acc, (const double2 *)nullptr, (size_t)maxs * 3 * s->n))) return rc;
-    if ((rc = dev_upload(s, &s->d_split_tick, (const unsigned *)nullptr, (size_t)ctas))) return rc;
-    s->split_cap = maxs;
+    for (int ns = 2; ns <= maxs; ns++)
+        if ((rc = part_build_split(s, ns))) return rc;
+    if ((rc = part_build_balanced_all(s))) return rc;
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1));
     float best = 1e30f;
     int best_ns = 1;
-    for (int ns = 1; ns <= maxs; ns++) {
+    /* candidates in order: plain, order splits, balanced (0) */
+    for (int c = 0; c <= maxs; c++) {
+        const int ns = c < maxs ? c + 1 : 0;
         s->nsplit = ns;
         for (int rep = 0; rep < 4; rep++) {
             if (rep == 1) CK(cudaEventRecord(e0, s->stream));
@@ -2132,7 +2364,7 @@ static int choose_split(gade_solver *s)
         float ms = 0;
         CK(cudaEventElapsedTime(&ms, e0, e1));
         s->split_ms[ns] = ms / 3;
-        if (ms < best * 0.98f) { best = ms; best_ns = ns; }    /* more splits only for a clear gain */
+        if (ms < best * 0.98f) { best = ms; best_ns = ns; }
     }
     cudaEventDestroy(e0); cudaEventDestroy(e1);
     s->nsplit = best_ns;
@@ -2276,21 +2508,24 @@ extern "C" int gade_probe_fp64_peak(int32_t device, double *tflops)
 extern "C" int gade_solver_set_split(gade_solver *s, int32_t nsplit)
 {
     if (!s) return fail(GADE_ERR_ARG, "gade_solver_set_split: NULL solver");
-    if (nsplit < 1 || nsplit > 4) return fail(GADE_ERR_ARG, "gade_solver_set_split: nsplit %d not in 1..4", nsplit);
-    if (nsplit > 1 && !s->d_split_acc) {
-        /* the scratch of the largest split */
-        CK(cudaSetDevice(s->device));
-        const long long ctas = (long long)s->nchunk * s->nblk;
-        int rc;
-        if ((rc = dev_upload(s, (double2 **)&s->d_split_acc, (const double2 *)nullptr, (size_t)4 * 3 * s->n))) return rc;
-        if ((rc = dev_upload(s, &s->d_split_tick, (const unsigned *)nullptr, (size_t)ctas))) return rc;
-        s->split_cap = 4;
-    }
-    if (nsplit > s->split_cap && nsplit > 1)
-        return fail(GADE_ERR_ARG, "gade_solver_set_split: scratch holds %d splits", s->split_cap);
+    if (nsplit < 0 || nsplit > 4) return fail(GADE_ERR_ARG, "gade_solver_set_split: nsplit %d not in 0..4", nsplit);
+    CK(cudaSetDevice(s->device));
     CK(cudaStreamSynchronize(s->stream));
     if (s->engine) batch_drop_graphs(s->engine);
+    int rc;
+    if (nsplit >= 2 && !s->part_split[nsplit].nseg && (rc = part_build_split(s, nsplit))) return rc;
+    if (nsplit == 0 && (rc = part_build_balanced_all(s))) return rc;
     s->nsplit = nsplit;
+    return GADE_OK;
+}
+
+extern "C" int gade_solver_balanced(const gade_solver *s, int32_t *segments, int32_t *pieces, float *ms)
+{
+    if (!s) return fail(GADE_ERR_ARG, "gade_solver_balanced: NULL solver");
+    const PartList &pl = s->part_bal[s->occ[0][0]];
+    if (segments) *segments = pl.nseg;
+    if (pieces) *pieces = pl.npieces;
+    if (ms) *ms = s->split_ms[0];
     return GADE_OK;
 }
 
@@ -2357,14 +2592,13 @@ extern "C" int gade_solver_apply_dot_noalloc(gade_solver *s, const void *x_dev, 
     unsigned int *ticket = (unsigned int *)(base + (size_t)GADE_NOALLOC_MAX_CTAS * NRED);
     /* the arrival ticket must start at zero */
     CK(cudaMemsetAsync(ticket, 0, sizeof(unsigned int), st));
-    OpP P = op_params(s);
-    P.nsplit = 1;                /* the split's partial sums would need scratch */
+    OpP P = op_params(s);        /* one piece per unit: no partial-sum scratch */
     RedP red = make_red(s, s->d_sc, RED_DOT_OUT, PRED_NONE);
     red.part = base; red.ticket = ticket; red.out = (double *)dot_dev;
     VecP V = {};
     V.out0 = y_dev;
     V.in0 = r0_dev;
-    dim3 grid(1, s->nchunk, s->nblk);
+    dim3 grid(1, s->part_split[1].nseg);
     int nt;
     size_t smem;
     apply_dims(s, sizeof(double2), &nt, &smem);

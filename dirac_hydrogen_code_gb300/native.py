@@ -85,6 +85,8 @@ _SIGS = {
     "gade_solver_flops": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "gade_solver_split": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.c_void_p]),
     "gade_solver_set_split": (C.c_int, [C.c_void_p, C.c_int32]),
+    "gade_solver_balanced": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                       C.POINTER(C.c_float)]),
     "gade_solver_apply_dot_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                                 C.c_void_p]),
     "gade_batch_create": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_double, C.c_int32,
@@ -288,7 +290,8 @@ class Solver:
         return {k: getattr(kt, k) for k, _ in KernelTimes._fields_}
 
     def split(self) -> tuple[int, list[float]]:
-        """(order split of the operator kernel, timed apply ms for 1-4 splits)."""
+        """(partition of the operator kernel: 0 balanced, 1-4 order split;
+        timed apply ms for 1-4 splits)."""
         ns = C.c_int32()
         ms = (C.c_float * 4)()
         _check(load_library().gade_solver_split(self._h, C.byref(ns), ms))
@@ -296,6 +299,12 @@ class Solver:
 
     def set_split(self, nsplit: int):
         _check(load_library().gade_solver_set_split(self._h, int(nsplit)))
+
+    def balanced(self) -> dict:
+        """Balanced partition of the FP64 operator: segments (CTAs), pieces, timed ms."""
+        seg, pcs, ms = C.c_int32(), C.c_int32(), C.c_float()
+        _check(load_library().gade_solver_balanced(self._h, C.byref(seg), C.byref(pcs), C.byref(ms)))
+        return {"segments": int(seg.value), "pieces": int(pcs.value), "ms": float(ms.value)}
 
     def flops(self) -> tuple[float, float]:
         """(FP64 flops of one operator apply, of one preconditioner solve)."""

@@ -149,16 +149,23 @@ int gade_solver_profile(gade_solver *s, int32_t enable);
 /* Synchronises, returns the accumulated times and resets them. */
 int gade_solver_kernel_times(gade_solver *s, gade_kernel_times *out);
 
-/* Order split of the operator kernel chosen at creation (no reference
- * counterpart): when one pulse has too few (row chunk, block row) work units
- * to balance the SMs, nsplit CTAs share each unit, each with a part of the
- * Bessel orders, and the last one combines their partial sums in a fixed
+/* Partition of the operator kernel's work chosen at creation (no reference
+ * counterpart).  The work units are (row chunk, block row) pairs.  nsplit
+ * 1-4: order split, nsplit CTAs share each unit, each with a part of the
+ * Bessel orders; nsplit 0: balanced segments, the units' work cut by a cost
+ * model into one equal share per resident CTA (a unit may be cut into
+ * pieces).  A unit in several pieces is combined by its last piece in a fixed
  * order.  split_ms (4 floats, may be NULL) receives the timed apply for 1-4
  * splits (0 where not timed). */
 int gade_solver_split(const gade_solver *s, int32_t *nsplit, float *split_ms);
-/* Forces the order split (1-4) instead of the timed choice; results differ
- * from the unsplit operator only by the order of summation. */
+/* Forces the partition (0 balanced, 1-4 order split) instead of the timed
+ * choice; results differ from the plain layout only by the order of
+ * summation. */
 int gade_solver_set_split(gade_solver *s, int32_t nsplit);
+/* The balanced partition of the FP64 BiCGSTAB operator: its CTAs (segments),
+ * pieces and timed apply ms (0 where not built or not timed; any pointer may
+ * be NULL). */
+int gade_solver_balanced(const gade_solver *s, int32_t *segments, int32_t *pieces, float *ms);
 
 /* FP64 flops (2 per FMA) executed by one operator apply and one
  * preconditioner solve, counted exactly from the set-up structure. */

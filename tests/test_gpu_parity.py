@@ -242,17 +242,22 @@ def test_drop_in_executable(workdirs, native_lib, tmp_path):
 
 
 def test_order_split_matches_unsplit(workdirs, native_lib):
-    """The operator with 1-4 order splits (partial sums combined by the last
-    CTA) gives the same steps up to the order of summation."""
+    """The operator with 1-4 order splits and with the balanced segments
+    (partial sums of a unit's pieces combined by its last piece) gives the
+    same steps up to the order of summation."""
     d, params, info, T, dt = _setup(workdirs, "tiny_nondipole")
     prob = Problem(d, info["lmax"])
     psi, _ = prob.psi0()
     fts = [pulse(params["Intensity"], params["Omega"], params["Cycles"], t) for _, t in step_times(T, params["Ntime"])[1][:6]]
     ref = None
-    for ns in (1, 2, 3, 4):
+    for ns in (1, 2, 3, 4, 0):
         sol = Solver(prob, dt)
         sol.set_split(ns)
         assert sol.split()[0] == ns
+        if ns == 0:
+            bal = sol.balanced()
+            # a tiny problem on a whole GPU: units cut into many pieces
+            assert bal["segments"] > 0 and bal["pieces"] > prob.info["nblk"]
         sol.set_x(psi)
         its = [sol.step(ft, maxit=500, tol=1e-12)["iters"] for ft in fts]
         x = sol.get_x()
@@ -262,3 +267,22 @@ def test_order_split_matches_unsplit(workdirs, native_lib):
             assert its == ref[1]
             assert _rel(x, ref[0]) < 1e-13, ns
         sol.close()
+
+
+def test_balanced_partition_mixed_precision(workdirs, native_lib):
+    """Mixed precision with the balanced segments (complex64 operator cut into
+    pieces too) reaches the same states as with the plain layout."""
+    d, params, info, T, dt = _setup(workdirs, "tiny_nondipole")
+    prob = Problem(d, info["lmax"])
+    psi, _ = prob.psi0()
+    fts = [pulse(params["Intensity"], params["Omega"], params["Cycles"], t) for _, t in step_times(T, params["Ntime"])[1][:6]]
+    out = []
+    for ns in (1, 0):
+        sol = Solver(prob, dt, precision="mixed")
+        sol.set_split(ns)
+        sol.set_x(psi)
+        for ft in fts:
+            sol.step(ft, maxit=500, tol=1e-10)
+        out.append(sol.get_x())
+        sol.close()
+    assert _rel(out[1], out[0]) < 1e-8
