@@ -390,25 +390,28 @@ __device__ void reduce_finish(RedP red, double (&v)[NRED], double *sh, unsigned 
 /* ------------------------------------------------------------------ */
 struct TabP {
     int lmax, nk, W, B;
-    const int *kvals;
+    const double *kvals;
     const void *g, *gt;           /* [pulse][lmax][3][4][W][B]: ELL slot layout, zero on empty slots
                                      (a in the l-parity set) */
     void *M;                      /* [pulse][lmax][nk][W][B] */
-    const int *plist;             /* grid y -> pulse (NULL: pulse 0) */
+    const int *plist;             /* grid z -> pulse (NULL: pulse 0) */
     size_t gstride, mstride;      /* elements per pulse of g / gt and of M */
 };
 
 /* coef[l*3 + ia]: SoL * i h dt/2 * f_a for a = (l%2+1)%2 + 2 ia.
  * RC: imaginary parts only (pg is imaginary, the stored table is -Im M). */
+/* grid (slot blocks, order l, pulse slot): no integer division, so the FP64
+   pipe only carries the table arithmetic */
 template <typename R, bool RC>
 __global__ void k_tables(TabP T, const double2 *__restrict__ coef)
 {
     typedef typename Cx<R>::T C;
-    const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const long long per_l = (long long)T.W * T.B;
-    if (tid >= per_l * T.lmax) return;
+    const int per_l = T.W * T.B;
+    const int l = blockIdx.y;
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;     /* j*B + i: consecutive threads stream g, gt and M */
+    if (slot >= per_l) return;
     {
-        const int pulse = T.plist ? T.plist[blockIdx.y] : 0;
+        const int pulse = T.plist ? T.plist[blockIdx.z] : 0;
         coef += (size_t)pulse * T.lmax * 3;
         if (RC) {
             T.g = (const double *)T.g + (size_t)pulse * T.gstride;
@@ -420,15 +423,13 @@ __global__ void k_tables(TabP T, const double2 *__restrict__ coef)
             T.M = (C4<C> *)T.M + (size_t)pulse * T.mstride;
         }
     }
-    const int l = (int)(tid / per_l);
-    const int slot = (int)(tid % per_l);      /* j*B + i: consecutive threads stream g, gt and M */
     if (RC) {
         typedef typename R4<R>::T Q4;
         double pg[4] = {0, 0, 0, 0}, pgt[4] = {0, 0, 0, 0};
         {
             const double *g = (const double *)T.g, *gt = (const double *)T.gt;
             for (int ia = 0; ia < 3; ia++) {
-                const double c = coef[l * 3 + ia].y;
+                const double c = -coef[l * 3 + ia].y;     /* the stored table is -Im M */
                 for (int q = 0; q < 4; q++) {
                     const size_t off = (((size_t)l * 3 + ia) * 4 + q) * per_l + slot;
                     pg[q] = fma(c, g[off], pg[q]);
@@ -438,12 +439,12 @@ __global__ void k_tables(TabP T, const double2 *__restrict__ coef)
         }
         Q4 *M = (Q4 *)T.M;
         for (int kk = 0; kk < T.nk; kk++) {
-            const double kap = (double)T.kvals[kk];
+            const double kap = T.kvals[kk];
             Q4 m;
-            m.a = (R)(-fma(kap, pg[1], pg[0]));
-            m.b = (R)(-fma(kap, pg[3], pg[2]));
-            m.c = (R)(-fma(kap, pgt[2], pgt[0]));
-            m.d = (R)(-fma(kap, pgt[3], pgt[1]));
+            m.a = (R)fma(kap, pg[1], pg[0]);
+            m.b = (R)fma(kap, pg[3], pg[2]);
+            m.c = (R)fma(kap, pgt[2], pgt[0]);
+            m.d = (R)fma(kap, pgt[3], pgt[1]);
             M[((size_t)l * T.nk + kk) * per_l + slot] = m;
         }
     } else {
@@ -462,7 +463,7 @@ __global__ void k_tables(TabP T, const double2 *__restrict__ coef)
         }
         C4<C> *M = (C4<C> *)T.M;
         for (int kk = 0; kk < T.nk; kk++) {
-            const double kap = (double)T.kvals[kk];
+            const double kap = T.kvals[kk];
             C4<C> m;
             m.a = mk<C>(fma(kap, pg[1].x, pg[0].x), fma(kap, pg[1].y, pg[0].y));
             m.b = mk<C>(fma(kap, pg[3].x, pg[2].x), fma(kap, pg[3].y, pg[2].y));
@@ -911,8 +912,9 @@ __device__ __forceinline__ void tma_bulk_load(void *dst, const void *src, unsign
 /* 4 warps per block row, one per SM sub-partition (each has its own FP64
  * unit): in every 32-row step warp w applies band terms d = 4w+1..4w+4 and
  * the inverse-block columns j = 8w..8w+7.  Partial sums meet in shared
- * memory and warp 0 (its lanes are the chunk's rows) combines them once per
- * row; the other warps read the combined values as broadcasts. */
+ * memory and are combined once per row, spread over all four warps (two
+ * adds per lane); the inverse-block products read the combined values as
+ * broadcasts. */
 template <typename R, int BWP>
 __global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const typename Cx<R>::T *__restrict__ in0,
                                                      const typename Cx<R>::T *__restrict__ in1,
@@ -930,6 +932,8 @@ __global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const type
     __shared__ __align__(8) uint64_t bar[2];
     __shared__ int all_ok;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    /* combining lane: row 8 wid + lane / 4, component (lane / 2) & 1, pair lane & 1 */
+    const int crow = wid * 8 + (lane >> 2), ccomp = (lane >> 1) & 1, ch = lane & 1;
     const int r = blockIdx.y;
     if (r >= Q.nblk) return;
     const int pulse = Q.plist ? Q.plist[blockIdx.x] : 0;
@@ -1026,9 +1030,14 @@ __global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const type
         }
         pt[wid * 32 + lane] = t;
         __syncthreads();
-        if (wid == 0)                      /* the row's t from the four partials, once */
-            pt[lane] = mk<C>((t.x + pt[32 + lane].x) + (pt[64 + lane].x + pt[96 + lane].x),
-                             (t.y + pt[32 + lane].y) + (pt[64 + lane].y + pt[96 + lane].y));
+        {
+            /* the row's t = (p0 + p1) + (p2 + p3), once: warp w sums rows
+               8w..8w+7, a lane one pair of one component, a shuffle the pairs */
+            R *pr = (R *)pt;
+            R sum = pr[((2 * ch) * 32 + crow) * 2 + ccomp] + pr[((2 * ch + 1) * 32 + crow) * 2 + ccomp];
+            sum += __shfl_xor_sync(0xffffffffu, sum, 1);
+            if (ch == 0) pr[crow * 2 + ccomp] = sum;
+        }
         __syncthreads();
         /* this warp's 8 columns of the inverse block */
         C a0 = mk<C>(0, 0), a1 = a0;
@@ -1040,9 +1049,12 @@ __global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const type
         }
         py[wid * 32 + lane] = mk<C>(a0.x + a1.x, a0.y + a1.y);
         __syncthreads();
-        if (wid == 0)
-            buf[o] = mk<C>((py[lane].x + py[32 + lane].x) + (py[64 + lane].x + py[96 + lane].x),
-                                  (py[lane].y + py[32 + lane].y) + (py[64 + lane].y + py[96 + lane].y));
+        {
+            const R *pr = (const R *)py;
+            R sum = pr[((2 * ch) * 32 + crow) * 2 + ccomp] + pr[((2 * ch + 1) * 32 + crow) * 2 + ccomp];
+            sum += __shfl_xor_sync(0xffffffffu, sum, 1);
+            if (ch == 0) ((R *)buf)[(32 * c + crow) * 2 + ccomp] = sum;
+        }
         __syncthreads();
     }
     if (!all_ok) {
@@ -1265,7 +1277,7 @@ struct gade_solver {
     void *d_ang_a0, *d_ang_a0k, *d_ang_a1, *d_ang_a1k;
     int *d_chunk_nrows, *d_chunk_ncols, *d_chunk_rows, *d_chunk_cols, *d_chunk_lcol;
     void *d_M, *d_S_ell, *d_Hst_ell, *d_D_ell;
-    int *d_kvals;
+    double *d_kvals;            /* the distinct kappa values, as doubles for the table kernel */
     void *d_g, *d_gt;
     int blk_nnz;
     /* preconditioner */
@@ -1688,7 +1700,10 @@ static int solver_create(const gade_problem *p, int npulse, const double *dts, c
         int rc = set_chunking(s, su);
         if (rc) { gade_setup_release(su); gade_solver_free(s); return rc; }
     }
-    UP(s->d_kvals, su->kvals, s->nk);
+    {
+        std::vector<double> kd(su->kvals, su->kvals + s->nk);
+        UP(s->d_kvals, kd.data(), s->nk);
+    }
     UP(s->d_ord, su->ord, s->B);
     {
         double2 *d;
@@ -2160,9 +2175,8 @@ static int launch_table_kernels(gade_solver *s, int which, cudaStream_t st)
     T.lmax = s->lmax; T.nk = s->nk; T.W = s->W; T.B = s->B;
     T.kvals = s->d_kvals; T.g = s->d_g; T.gt = s->d_gt; T.M = s->d_M;
     T.plist = s->d_plist; T.gstride = s->gstride; T.mstride = s->mstride;
-    long long total = (long long)s->lmax * s->W * s->B;
-    int nt = 256;
-    dim3 grid((unsigned)((total + nt - 1) / nt), s->nslot);
+    const int per_l = s->W * s->B, nt = 256;
+    dim3 grid((unsigned)((per_l + nt - 1) / nt), s->lmax, s->nslot);
     if (which & 1) {            /* FP64 tables */
         prof_begin(s, st);
         if (s->rc) k_tables<double, true><<<grid, nt, 0, st>>>(T, s->d_coef);
