@@ -190,7 +190,8 @@ def run_ours(args):
     partition = {"chosen": "balanced" if ns == 0 else f"order split {ns}",
                  "apply_ms_timed_at_creation": {"balanced": bal["ms"],
                                                 **{f"split{k + 1}": v for k, v in enumerate(split_ms) if v > 0}},
-                 "balanced_ctas": bal["segments"], "balanced_pieces": bal["pieces"]}
+                 "balanced_ctas": bal["segments"], "balanced_pieces": bal["pieces"],
+                 "balanced_gather_weight": bal["gather_weight"]}
     psi, _ = prob.psi0()
     sol.set_x(psi)
     stream = torch.cuda.ExternalStream(sol.stream(), device=device)

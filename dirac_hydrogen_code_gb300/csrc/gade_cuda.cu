@@ -182,6 +182,7 @@ enum { AX_PLAIN = 0, AX_PARTS, AX_R0V, AX_TS, AX_RHS, AX_RESTART, AX_MIX };
 enum { PC_PLAIN = 0, PC_P, PC_S };
 
 #define NRED 4   /* values per partial: up to 4 doubles */
+#define APPLY_G64 3   /* Bessel orders per gather phase of the FP64 operator */
 
 /* ------------------------------------------------------------------ */
 /* operator parameters                                                 */
@@ -527,8 +528,9 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 8 && SEP) ? 2 : 3)
     typedef typename Cx<R>::T C;
     typedef typename std::conditional<RC, typename R4<R>::T, C4<C>>::type A4;   /* a0, a0 k_c, a1, a1 k_c */
     extern __shared__ __align__(32) unsigned char smem_raw[];
-    /* G orders per gather phase: 2 (FP64) or 4 (FP32) */
-    constexpr int G = sizeof(R) == 8 ? 2 : 4;
+    /* G orders per gather phase: 3 (FP64) or 4 (FP32); with ~150 columns a
+       chunk's G x columns gather items fill the CTA's threads twice */
+    constexpr int G = sizeof(R) == 8 ? APPLY_G64 : 4;
     const int CS = (P.CM + 2) & ~1;           /* column stride: CM + the zero column, even */
     const ApplySmem L = apply_smem(CS, P.W, P.RM, P.AM, G, sizeof(C), sizeof(A4), blockDim.x);
     C *xr = (C *)(smem_raw + L.xr);           /* [CS] */
@@ -1327,6 +1329,7 @@ struct gade_solver {
     /* host copy of the work model: active orders per block row, their
        angular term counts, rows and columns per chunk */
     std::vector<int> h_act_ptr, h_act_ne, h_chunk_nrows, h_chunk_ncols;
+    double bal_gamma;           /* weight of the gather in the balanced cost model (timed at creation) */
     gade_batch *engine;         /* step engine of a single-pulse solver (device control, graphs) */
     int zskip;                  /* the DKB zero blocks hold for every pulse's tables */
 };
@@ -1912,7 +1915,7 @@ static void apply_dims(const gade_solver *s, size_t elem, int *nt, size_t *smem)
     int t = 2 * s->RM > s->CM ? 2 * s->RM : s->CM;   /* two threads per row */
     t = (t + 31) / 32 * 32;
     *nt = t;
-    const int G = elem == sizeof(double2) ? 2 : 4;
+    const int G = elem == sizeof(double2) ? APPLY_G64 : 4;
     const unsigned ang4 = s->rc ? (unsigned)(2 * elem) : (unsigned)(4 * elem);   /* four angular factors */
     const int CS = (s->CM + 2) & ~1;                 /* columns + the zero column, even */
     *smem = apply_smem(CS, s->W, s->RM, s->AM, G, (unsigned)elem, ang4, t).total;
@@ -1996,7 +1999,7 @@ static int part_build_split(gade_solver *s, int ns)
     for (int u = 0; u < nunit; u++) {
         const int r = u / s->nchunk;
         const int a0 = s->h_act_ptr[r], a1 = s->h_act_ptr[r + 1], na = a1 - a0;
-        const int per = ((na + ns - 1) / ns + 1) / 2 * 2;
+        const int per = ((na + ns - 1) / ns + APPLY_G64 - 1) / APPLY_G64 * APPLY_G64;
         for (int sp = 0; sp < ns; sp++) {
             const int b0 = std::min(a0 + sp * per, a1), b1 = std::min(b0 + per, a1);
             pcs.push_back(make_int4(u, b0, b1, sp | (ns << 16)));
@@ -2016,8 +2019,9 @@ static int part_build_balanced(gade_solver *s, int nseg, PartList &pl)
 {
     const int nunit = s->nchunk * s->nblk;
     const double terms = s->zskip ? 3.0 : 4.0, fc = s->rc ? 2.0 : 4.0;
+    const double gw = s->bal_gamma > 0 ? s->bal_gamma : 1.0;
     auto ocost = [&](int a, int q) {
-        return terms * fc * ((double)s->h_act_ne[a] * s->h_chunk_ncols[q] + (double)s->h_chunk_nrows[q] * s->W);
+        return terms * fc * (gw * s->h_act_ne[a] * s->h_chunk_ncols[q] + (double)s->h_chunk_nrows[q] * s->W);
     };
     auto ufix = [&](int q) { return 6.0 * s->h_chunk_nrows[q] * s->W; };
     double total = 0;
@@ -2359,9 +2363,17 @@ static int choose_split(gade_solver *s)
     CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1));
     float best = 1e30f;
     int best_ns = 1;
-    /* candidates in order: plain, order splits, balanced (0) */
-    for (int c = 0; c <= maxs; c++) {
+    double best_gamma = 1.0;
+    /* candidates in order: plain, order splits, balanced (0) with five
+       weights of the gather in its cost model */
+    const double gammas[5] = {1.0, 0.7, 1.4, 0.5, 2.0};
+    for (int c = 0; c < maxs + 5; c++) {
         const int ns = c < maxs ? c + 1 : 0;
+        if (ns == 0) {
+            s->bal_gamma = gammas[c - maxs];
+            for (PartList &pl : s->part_bal) part_release(s, pl);
+            if ((rc = part_build_balanced_all(s))) { cudaEventDestroy(e0); cudaEventDestroy(e1); return rc; }
+        }
         s->nsplit = ns;
         for (int rep = 0; rep < 4; rep++) {
             if (rep == 1) CK(cudaEventRecord(e0, s->stream));
@@ -2377,10 +2389,20 @@ static int choose_split(gade_solver *s)
         CK(cudaEventSynchronize(e1));
         float ms = 0;
         CK(cudaEventElapsedTime(&ms, e0, e1));
+        if (ns == 0 && s->split_ms[0] > 0.f && ms / 3 >= s->split_ms[0]) continue;   /* keep the best weight's time */
         s->split_ms[ns] = ms / 3;
-        if (ms < best * 0.98f) { best = ms; best_ns = ns; }
+        if (ms < best * 0.98f || (ns == 0 && best_ns == 0 && ms < best)) {
+            best = ms;
+            best_ns = ns;
+            if (ns == 0) best_gamma = s->bal_gamma;
+        }
     }
     cudaEventDestroy(e0); cudaEventDestroy(e1);
+    if (s->bal_gamma != best_gamma) {
+        s->bal_gamma = best_gamma;
+        for (PartList &pl : s->part_bal) part_release(s, pl);
+        if ((rc = part_build_balanced_all(s))) return rc;
+    }
     s->nsplit = best_ns;
     return GADE_OK;
 }
@@ -2533,13 +2555,15 @@ extern "C" int gade_solver_set_split(gade_solver *s, int32_t nsplit)
     return GADE_OK;
 }
 
-extern "C" int gade_solver_balanced(const gade_solver *s, int32_t *segments, int32_t *pieces, float *ms)
+extern "C" int gade_solver_balanced(const gade_solver *s, int32_t *segments, int32_t *pieces, float *ms,
+                                    double *gather_weight)
 {
     if (!s) return fail(GADE_ERR_ARG, "gade_solver_balanced: NULL solver");
     const PartList &pl = s->part_bal[s->occ[0][0]];
     if (segments) *segments = pl.nseg;
     if (pieces) *pieces = pl.npieces;
     if (ms) *ms = s->split_ms[0];
+    if (gather_weight) *gather_weight = s->bal_gamma > 0 ? s->bal_gamma : 1.0;
     return GADE_OK;
 }
 

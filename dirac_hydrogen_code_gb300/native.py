@@ -86,7 +86,7 @@ _SIGS = {
     "gade_solver_split": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.c_void_p]),
     "gade_solver_set_split": (C.c_int, [C.c_void_p, C.c_int32]),
     "gade_solver_balanced": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
-                                       C.POINTER(C.c_float)]),
+                                       C.POINTER(C.c_float), C.POINTER(C.c_double)]),
     "gade_solver_apply_dot_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                                 C.c_void_p]),
     "gade_batch_create": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_double, C.c_int32,
@@ -302,9 +302,10 @@ class Solver:
 
     def balanced(self) -> dict:
         """Balanced partition of the FP64 operator: segments (CTAs), pieces, timed ms."""
-        seg, pcs, ms = C.c_int32(), C.c_int32(), C.c_float()
-        _check(load_library().gade_solver_balanced(self._h, C.byref(seg), C.byref(pcs), C.byref(ms)))
-        return {"segments": int(seg.value), "pieces": int(pcs.value), "ms": float(ms.value)}
+        seg, pcs, ms, gw = C.c_int32(), C.c_int32(), C.c_float(), C.c_double()
+        _check(load_library().gade_solver_balanced(self._h, C.byref(seg), C.byref(pcs), C.byref(ms), C.byref(gw)))
+        return {"segments": int(seg.value), "pieces": int(pcs.value), "ms": float(ms.value),
+                "gather_weight": float(gw.value)}
 
     def flops(self) -> tuple[float, float]:
         """(FP64 flops of one operator apply, of one preconditioner solve)."""

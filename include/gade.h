@@ -163,9 +163,10 @@ int gade_solver_split(const gade_solver *s, int32_t *nsplit, float *split_ms);
  * summation. */
 int gade_solver_set_split(gade_solver *s, int32_t nsplit);
 /* The balanced partition of the FP64 BiCGSTAB operator: its CTAs (segments),
- * pieces and timed apply ms (0 where not built or not timed; any pointer may
- * be NULL). */
-int gade_solver_balanced(const gade_solver *s, int32_t *segments, int32_t *pieces, float *ms);
+ * pieces, timed apply ms (0 where not built or not timed) and the weight of
+ * the gather in its cost model, chosen by timing (any pointer may be NULL). */
+int gade_solver_balanced(const gade_solver *s, int32_t *segments, int32_t *pieces, float *ms,
+                         double *gather_weight);
 
 /* FP64 flops (2 per FMA) executed by one operator apply and one
  * preconditioner solve, counted exactly from the set-up structure. */
