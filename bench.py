@@ -133,14 +133,43 @@ def cpu_reference_time(workdir, params, info, T, nsteps: int, warmup: int = 0):
     return sum(r.elapsed for r in timed) / len(timed), T / params["Ntime"]
 
 
+# one thread per CPU process: the port's SpMV, ILU solves and BiCGSTAB are
+# single-threaded like one reference rank, and the dots stay on that thread
+CPU_THREAD_ENV = {"OMP_NUM_THREADS": "1", "OPENBLAS_NUM_THREADS": "1", "MKL_NUM_THREADS": "1"}
+
+
+def cpu_processes(workdir, lmax: int, nsteps: int, warmup: int, nproc: int) -> list[float]:
+    """s/step of nproc concurrent single-threaded oracle-port processes, each
+    stepping its own copy of the pulse in workdir (started together)."""
+    env = dict(os.environ, **CPU_THREAD_ENV)
+    cmd = [sys.executable, os.path.abspath(__file__), "--cpu-worker", workdir, str(lmax), str(nsteps), str(warmup)]
+    procs = [subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.PIPE, env=env) for _ in range(nproc)]
+    out = []
+    for p in procs:
+        o, e = p.communicate()
+        if p.returncode != 0:
+            raise RuntimeError(f"CPU worker failed: {e.decode()[-500:]}")
+        out.append(float(o.decode().strip().splitlines()[-1]))
+    return out
+
+
+def cpu_worker(argv) -> int:
+    workdir, lmax, nsteps, warmup = argv
+    from dirac_hydrogen_code_gb300.gen import CONFIGS
+    params = CONFIGS[WORKLOAD]
+    T = params["Cycles"] * 2 * math.pi / params["Omega"]
+    s, _ = cpu_reference_time(workdir, params, {"lmax": int(lmax)}, T, int(nsteps), warmup=int(warmup))
+    print(s)
+    return 0
+
+
 def run_reference(args):
     ws, rank, local = _dist()
     if rank != 0:
         return 0
     with tempfile.TemporaryDirectory() as d:
         params, info, T = _gen(d)
-        ncores = os.cpu_count()
-        s_per_step, dt = cpu_reference_time(d, params, info, T, args.steps, warmup=args.warmup)
+        s_per_step = cpu_processes(d, info["lmax"], args.steps, args.warmup, 1)[0]
     v = 1.0 / s_per_step
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": args.gpus,
@@ -148,8 +177,10 @@ def run_reference(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
         "data": "synthetic (generated dumpCouplings inputs)",
         "config": {"workload": WORKLOAD, "N": info["n"], "nnz_equiv": info["nnz_full"], "tol": TOL},
-        "cpu_baseline": {"value": v, "unit": "steps/s", "cores": ncores, "kind": "port",
-                         "sample": f"{args.steps} CN steps of {WORKLOAD} after {args.warmup} warm-up steps"},
+        "cpu_baseline": {"value": v, "unit": "steps/s", "cores": 1, "kind": "port",
+                         "sample": f"{args.steps} CN steps of {WORKLOAD} after {args.warmup} warm-up steps; "
+                                   "one process, one thread: one pulse is one reference rank (its SpMV, "
+                                   "SuperLU solves and BiCGSTAB are single-threaded)"},
         "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -262,6 +293,22 @@ def run_ours(args):
     te = max_over_ranks(time.perf_counter() - t0, dist, f"cuda:{device}")
     e2e = ws * args.steps / te
 
+    # step quality after the timed steps (outside every timed region): the
+    # true residual |b - A x_{n+1}| / |b| of one more step, its recursive
+    # residual, and the drift of the S-norm psi^H S psi from psi0's
+    x_prev = sol.get_x()
+    st_q = sol.step(fts[idx % len(fts)], MAXIT, TOL)
+    idx += 1
+    x_new = sol.get_x()
+    _, sxp, hxp = sol.apply(x_prev, parts=True)
+    b_rhs = sxp - hxp
+    true_res = float(np.linalg.norm(b_rhs - sol.apply(x_new)) / np.linalg.norm(b_rhs))
+    _, sx_new, _ = sol.apply(x_new, parts=True)
+    _, s_psi0, _ = sol.apply(psi, parts=True)
+    sn0 = float(np.vdot(psi, s_psi0).real)
+    quality = {"true_residual": true_res, "recursive_residual": float(st_q["tol_error"]),
+               "steps_taken": idx, "snorm_drift_rel": abs(float(np.vdot(x_new, sx_new).real) - sn0) / sn0}
+
     # roofline of the dominant kernel (matrix-free operator)
     apply_ms = kt["apply_ms"] / max(kt["apply_launches"], 1)
     nnz = info["nnz_full"]
@@ -270,6 +317,7 @@ def run_ours(args):
     achieved = csr_bytes / (apply_ms * 1e-3) / 1e9
     fp64_peak = native.fp64_peak_tflops(device)
     mf_flops, pc_flops = sol.flops()
+    mf_bytes = sol.apply_bytes()
     roof = {
         "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
         "traffic": _ncu_traffic(), "peak_kind": peak_kind,
@@ -280,6 +328,12 @@ def run_ours(args):
         "fp64": {"achieved_tflops": mf_flops / (apply_ms * 1e-3) / 1e12, "peak_tflops": fp64_peak,
                  "frac": mf_flops / (apply_ms * 1e-3) / 1e12 / fp64_peak, "flops_per_launch": mf_flops,
                  "peak_kind": "measured (own FP64 FMA kernel)"},
+        "matrix_free_bytes": {"compulsory_bytes_per_launch": mf_bytes,
+                              "achieved_gbs": mf_bytes / (apply_ms * 1e-3) / 1e9,
+                              "frac": mf_bytes / (apply_ms * 1e-3) / 1e9 / hbm_peak,
+                              "formula": "table slabs of the used (order, kappa) pairs x W x B x 32 B + "
+                                         "diagonal blocks nk x W x B x 16 B + angular terms x 36 B + "
+                                         "slot maps + 48 N (x, r0 in; v out)"},
         "apply_ms": apply_ms, "precond_ms": kt["precond_ms"] / max(kt["precond_launches"], 1),
         "kernel_share": {"apply": kt["apply_ms"], "precond": kt["precond_ms"], "other": kt["other_ms"]},
     }
@@ -296,10 +350,19 @@ def run_ours(args):
     # CPU baseline on a bounded sample (rank 0, N=1)
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
-        s_per_step, _ = cpu_reference_time(tmp.name, params, info, T, args.cpu_steps, warmup=1)
-        cpu = {"value": 1.0 / s_per_step, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": f"{args.cpu_steps} CN steps of {WORKLOAD} (oracle port: reference assembly, "
-                         "scipy CSR SpMV, SuperLU ILU, BiCGSTAB at tol 1e-12)"}
+        s_per_step = cpu_processes(tmp.name, info["lmax"], args.cpu_steps, 1, 1)[0]
+        cpu = {"value": 1.0 / s_per_step, "unit": "steps/s", "cores": 1, "kind": "port",
+               "sample": f"{args.cpu_steps} CN steps of {WORKLOAD} after 1 warm-up step (oracle port: "
+                         "reference assembly, scipy CSR SpMV, SuperLU ILU, BiCGSTAB at tol 1e-12; one "
+                         "process, one thread, as one reference rank)"}
+        if variants is not None and "batch64" in variants:
+            # throughput comparison for the batch: one single-threaded process per host core
+            nproc = os.cpu_count() or 1
+            per = cpu_processes(tmp.name, info["lmax"], args.cpu_steps, 1, nproc)
+            variants["batch64"]["cpu_aggregate"] = {
+                "value": sum(1.0 / x for x in per), "unit": "pulse-steps/s", "processes": nproc, "cores": nproc,
+                "kind": "port", "sample": f"{nproc} concurrent single-threaded processes, each {args.cpu_steps} "
+                                          f"CN steps of one {WORKLOAD} pulse after 1 warm-up step"}
 
     if rank == 0:
         line = {
@@ -311,6 +374,7 @@ def run_ours(args):
                        "l2": "flushed (256 MB write) between timed steps", "parallelism": f"replicas x{ws}",
                        "iters_per_step": sorted(set(iters)),
                        "iters_counting": "tools/bicgstab.c: the iteration that meets the tolerance is not counted",
+                       "step_quality": quality,
                        "operator_partition": partition},
             "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": 16 * N, "d2h_bytes_per_step": 16 * N},
             "gpu_launches": launches,
@@ -576,6 +640,8 @@ def main():
     ap.add_argument("--learned-steps", type=int, default=200, help="steps per pulse of the learned variant")
     ap.add_argument("--profile-precision", default=None, choices=["fp64", "mixed"],
                     help="only run this precision's steps (for profiler captures)")
+    if len(sys.argv) > 1 and sys.argv[1] == "--cpu-worker":
+        return cpu_worker(sys.argv[2:])
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

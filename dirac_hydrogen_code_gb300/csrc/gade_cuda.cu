@@ -1306,6 +1306,7 @@ struct gade_solver {
     long long prof_n[3];
     double prof_ms[3];
     double apply_flops, precond_flops;   /* FP64 flops of one launch */
+    double apply_bytes;                  /* compulsory DRAM bytes of one FP64 BiCGSTAB apply */
     /* mixed precision (GADE_PREC_MIXED) */
     void *d_M32, *d_S32, *d_H32, *d_D32;
     void *d_a32[4];
@@ -1516,6 +1517,22 @@ static int set_chunking(gade_solver *s, const gade_setup *su)
             fmas += terms * fma_c * (double)s->blk_nnz;            /* radial tables */
         }
     s->apply_flops = 2.0 * fmas;
+    {
+        /* compulsory bytes of one apply (mode AX_R0V): the table slabs of the
+           distinct (order, kappa) pairs the block rows use, the diagonal
+           blocks, the angular terms, the slot maps and x, r0 in, v out */
+        std::vector<char> used((size_t)s->lmax * s->nk, 0);
+        for (int r = 0; r < s->nblk; r++)
+            for (int a = su->act_ptr[r]; a < su->act_ptr[r + 1]; a++)
+                used[(size_t)su->act_l[a] * s->nk + su->row_kidx[r]] = 1;
+        double slabs = 0;
+        for (char u : used) slabs += u;
+        const double entry = s->rc ? 32.0 : 64.0;            /* four table values per ELL slot */
+        const double nang = su->ang_ptr[(size_t)s->nblk * s->lmax];
+        s->apply_bytes = slabs * s->W * s->B * entry + (double)s->nk * s->W * s->B * 16.0
+                       + nang * (4.0 + (s->rc ? 32.0 : 64.0)) + (double)s->nchunk * s->W * s->RM * 4.0
+                       + 48.0 * (double)s->n;
+    }
     /* host copy of the work model for the partitions */
     s->h_act_ptr.assign(su->act_ptr, su->act_ptr + s->nblk + 1);
     s->h_act_ne.assign((size_t)su->act_ptr[s->nblk], 0);
@@ -2580,6 +2597,13 @@ extern "C" int gade_solver_flops(const gade_solver *s, double *apply_flops, doub
     if (!s) return fail(GADE_ERR_ARG, "gade_solver_flops: NULL solver");
     if (apply_flops) *apply_flops = s->apply_flops;
     if (precond_flops) *precond_flops = s->precond_flops;
+    return GADE_OK;
+}
+
+extern "C" int gade_solver_apply_bytes(const gade_solver *s, double *bytes)
+{
+    if (!s || !bytes) return fail(GADE_ERR_ARG, "gade_solver_apply_bytes: NULL argument");
+    *bytes = s->apply_bytes;
     return GADE_OK;
 }
 

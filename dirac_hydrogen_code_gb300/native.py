@@ -85,6 +85,7 @@ _SIGS = {
     "gade_solver_flops": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "gade_solver_split": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.c_void_p]),
     "gade_solver_set_split": (C.c_int, [C.c_void_p, C.c_int32]),
+    "gade_solver_apply_bytes": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "gade_solver_balanced": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                        C.POINTER(C.c_float), C.POINTER(C.c_double)]),
     "gade_solver_apply_dot_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -306,6 +307,12 @@ class Solver:
         _check(load_library().gade_solver_balanced(self._h, C.byref(seg), C.byref(pcs), C.byref(ms), C.byref(gw)))
         return {"segments": int(seg.value), "pieces": int(pcs.value), "ms": float(ms.value),
                 "gather_weight": float(gw.value)}
+
+    def apply_bytes(self) -> float:
+        """Compulsory DRAM bytes of one FP64 BiCGSTAB operator apply."""
+        b = C.c_double()
+        _check(load_library().gade_solver_apply_bytes(self._h, C.byref(b)))
+        return float(b.value)
 
     def flops(self) -> tuple[float, float]:
         """(FP64 flops of one operator apply, of one preconditioner solve)."""

@@ -171,6 +171,11 @@ int gade_solver_balanced(const gade_solver *s, int32_t *segments, int32_t *piece
 /* FP64 flops (2 per FMA) executed by one operator apply and one
  * preconditioner solve, counted exactly from the set-up structure. */
 int gade_solver_flops(const gade_solver *s, double *apply_flops, double *precond_flops);
+/* Compulsory DRAM bytes of one FP64 BiCGSTAB operator apply (no reference
+ * counterpart): the radial-table slabs of the distinct (order, kappa) pairs
+ * the block rows use, the diagonal blocks, the angular terms and slot maps,
+ * and the vectors read and written (x, r0 in; v out). */
+int gade_solver_apply_bytes(const gade_solver *s, double *bytes);
 
 /* y = (S + H(t)) x and dot = sum_i conj(r0_i) y_i (2 doubles, re and im), all
  * device pointers in HBM, with the tables of the last set_time/step; no
