@@ -1331,6 +1331,7 @@ struct gade_solver {
        angular term counts, rows and columns per chunk */
     std::vector<int> h_act_ptr, h_act_ne, h_chunk_nrows, h_chunk_ncols;
     double bal_gamma;           /* weight of the gather in the balanced cost model (timed at creation) */
+    int bal_waves;              /* balanced segments per resident CTA slot (timed at creation) */
     gade_batch *engine;         /* step engine of a single-pulse solver (device control, graphs) */
     int zskip;                  /* the DKB zero blocks hold for every pulse's tables */
 };
@@ -2029,9 +2030,11 @@ static int part_build_split(gade_solver *s, int ns)
 /* Balanced segments: the units' work, in unit order, laid on one line by a
    cost model (FMAs of the gather and the table products of every active
    order, the diagonal blocks and the staging of a unit) and cut into nseg
-   equal lengths, one segment per resident CTA; an order goes to the segment
-   that holds its midpoint, so a unit's orders fall into consecutive pieces.
-   With every segment resident at once, the SMs finish together. */
+   equal lengths, one (or a few) segments per resident CTA slot; an order goes
+   to the segment that holds its midpoint, so a unit's orders fall into
+   consecutive pieces.  With one segment per slot every segment is resident at
+   once and the SMs finish together; with more, the block scheduler gives the
+   later segments to the slots that free first. */
 static int part_build_balanced(gade_solver *s, int nseg, PartList &pl)
 {
     const int nunit = s->nchunk * s->nblk;
@@ -2091,7 +2094,7 @@ static int part_build_balanced_all(gade_solver *s)
         for (int sep = 0; sep < 2; sep++) {
             const int o = s->occ[f][sep];
             if (s->part_bal[o].nseg) continue;
-            int rc = part_build_balanced(s, o * s->nsm, s->part_bal[o]);
+            int rc = part_build_balanced(s, o * s->nsm * (s->bal_waves > 0 ? s->bal_waves : 1), s->part_bal[o]);
             if (rc) return rc;
         }
     }
@@ -2381,13 +2384,18 @@ static int choose_split(gade_solver *s)
     float best = 1e30f;
     int best_ns = 1;
     double best_gamma = 1.0;
-    /* candidates in order: plain, order splits, balanced (0) with five
-       weights of the gather in its cost model */
-    const double gammas[5] = {1.0, 0.7, 1.4, 0.5, 2.0};
+    int best_waves = 1;
+    /* candidates in order: plain, order splits, balanced (0) with three
+       weights of the gather in its cost model, then with two and three
+       segments per resident CTA slot (the block scheduler hands the later
+       ones to the CTA slots that free first) */
+    const double gammas[5] = {1.0, 0.7, 1.4, 1.0, 1.0};
+    const int waves[5] = {1, 1, 1, 2, 3};
     for (int c = 0; c < maxs + 5; c++) {
         const int ns = c < maxs ? c + 1 : 0;
         if (ns == 0) {
             s->bal_gamma = gammas[c - maxs];
+            s->bal_waves = waves[c - maxs];
             for (PartList &pl : s->part_bal) part_release(s, pl);
             if ((rc = part_build_balanced_all(s))) { cudaEventDestroy(e0); cudaEventDestroy(e1); return rc; }
         }
@@ -2411,12 +2419,13 @@ static int choose_split(gade_solver *s)
         if (ms < best * 0.98f || (ns == 0 && best_ns == 0 && ms < best)) {
             best = ms;
             best_ns = ns;
-            if (ns == 0) best_gamma = s->bal_gamma;
+            if (ns == 0) { best_gamma = s->bal_gamma; best_waves = s->bal_waves; }
         }
     }
     cudaEventDestroy(e0); cudaEventDestroy(e1);
-    if (s->bal_gamma != best_gamma) {
+    if (s->bal_gamma != best_gamma || s->bal_waves != best_waves) {
         s->bal_gamma = best_gamma;
+        s->bal_waves = best_waves;
         for (PartList &pl : s->part_bal) part_release(s, pl);
         if ((rc = part_build_balanced_all(s))) return rc;
     }
