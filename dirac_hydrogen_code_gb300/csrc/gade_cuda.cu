@@ -861,7 +861,7 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 8 && SEP) ? 2 : 3)
 /* ------------------------------------------------------------------ */
 /* Factor data of one 32-row chunk is contiguous in HBM:
  *   [Linv (32x32, column-major [j][lane])][band: BWP rows [d][lane] holding
- *   L(o, o-d-1) only where that source row lies before the chunk, else 0]
+ *   -L(o, o-d-1) (negated) only where that source row lies before the chunk, else 0]
  * (and the same for U with the sources after the chunk).  One elected lane
  * streams chunk k+1 into shared memory with cp.async.bulk on an mbarrier
  * while the warp computes chunk k.  Every wait is bounded: on timeout the
@@ -916,7 +916,8 @@ __device__ __forceinline__ void tma_bulk_load(void *dst, const void *src, unsign
  * the inverse-block columns j = 8w..8w+7.  Partial sums meet in shared
  * memory and are combined once per row, spread over all four warps (two
  * adds per lane); the inverse-block products read the combined values as
- * broadcasts. */
+ * broadcasts.  The sweeps are bound by the FP64 instructions each warp
+ * issues (54 per step): fewer partial sums and no negations. */
 template <typename R, int BWP>
 __global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const typename Cx<R>::T *__restrict__ in0,
                                                      const typename Cx<R>::T *__restrict__ in1,
@@ -1025,8 +1026,7 @@ __global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const type
 #pragma unroll
         for (int q = 0; q < DPW; q++) {
             const int d = wid * DPW + q + 1;
-            C bv = F[1024 + (d - 1) * 32 + lane];
-            bv.x = -bv.x; bv.y = -bv.y;
+            const C bv = F[1024 + (d - 1) * 32 + lane];     /* stored negated */
             const int src = fwd ? (o - d >= 0 ? o - d : 0) : (o + d < Bp ? o + d : Bp - 1);
             cfma(t, bv, buf[src]);
         }
@@ -1547,7 +1547,8 @@ static int set_chunking(gade_solver *s, const gade_setup *su)
     return part_reset(s);
 }
 
-/* chunk-packed block-LU factors of one pulse: [nk][nch][Linv | masked band] */
+/* chunk-packed block-LU factors of one pulse: [nk][nch][Linv | masked band],
+   the band stored negated (the sweep adds -L(o, o-d) y(o-d)) */
 static void pack_factors(const gade_setup *su, int nk, int nch, int bw, int bwp, int B, int Bp,
                          double2 *FL, double2 *FU)
 {
@@ -1570,8 +1571,8 @@ static void pack_factors(const gade_setup *su, int nk, int nch, int bw, int bwp,
                         gc64 v = su->Ub[((size_t)kk * bw + d - 1) * Bp + o];
                         uv = make_double2(v.re, v.im);
                     }
-                    fl[1024 + (d - 1) * 32 + lane] = lv;
-                    fu[1024 + (d - 1) * 32 + lane] = uv;
+                    fl[1024 + (d - 1) * 32 + lane] = make_double2(-lv.x, -lv.y);
+                    fu[1024 + (d - 1) * 32 + lane] = make_double2(-uv.x, -uv.y);
                 }
         }
 }
