@@ -1042,14 +1042,15 @@ __global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const type
         }
         __syncthreads();
         /* this warp's 8 columns of the inverse block */
-        C a0 = mk<C>(0, 0), a1 = a0;
+        /* one accumulator: the sweeps are bound by the FP64 instructions a
+           warp issues, not by the length of the DFMA chain (measured) */
+        C a0 = mk<C>(0, 0);
 #pragma unroll
-        for (int q = 0; q < 8; q += 2) {
-            const int j0 = wid * 8 + q, j1 = j0 + 1;
+        for (int q = 0; q < 8; q++) {
+            const int j0 = wid * 8 + q;
             cfma(a0, F[j0 * 32 + lane], pt[j0]);
-            cfma(a1, F[j1 * 32 + lane], pt[j1]);
         }
-        py[wid * 32 + lane] = mk<C>(a0.x + a1.x, a0.y + a1.y);
+        py[wid * 32 + lane] = a0;
         __syncthreads();
         {
             const R *pr = (const R *)py;
