@@ -394,7 +394,7 @@ struct TabP {
     const double *kvals;
     const void *g, *gt;           /* [pulse][lmax][3][4][W][B]: ELL slot layout, zero on empty slots
                                      (a in the l-parity set) */
-    void *M;                      /* [pulse][lmax][nk][W][B] */
+    void *M, *M32;                /* [pulse][lmax][nk][W][B]: FP64 tables, complex64 copies */
     const int *plist;             /* grid z -> pulse (NULL: pulse 0) */
     size_t gstride, mstride;      /* elements per pulse of g / gt and of M */
 };
@@ -403,32 +403,23 @@ struct TabP {
  * RC: imaginary parts only (pg is imaginary, the stored table is -Im M). */
 /* grid (slot blocks, order l, pulse slot): no integer division, so the FP64
    pipe only carries the table arithmetic */
-template <typename R, bool RC>
+template <bool RC, int OUT>
 __global__ void k_tables(TabP T, const double2 *__restrict__ coef)
 {
-    typedef typename Cx<R>::T C;
+    /* OUT: 1 the FP64 tables M, 2 the complex64 copies M32 (rounded from the
+       same FP64 values), 3 both from one pass */
     const int per_l = T.W * T.B;
     const int l = blockIdx.y;
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;     /* j*B + i: consecutive threads stream g, gt and M */
     if (slot >= per_l) return;
-    {
-        const int pulse = T.plist ? T.plist[blockIdx.z] : 0;
-        coef += (size_t)pulse * T.lmax * 3;
-        if (RC) {
-            T.g = (const double *)T.g + (size_t)pulse * T.gstride;
-            T.gt = (const double *)T.gt + (size_t)pulse * T.gstride;
-            T.M = (typename R4<R>::T *)T.M + (size_t)pulse * T.mstride;
-        } else {
-            T.g = (const double2 *)T.g + (size_t)pulse * T.gstride;
-            T.gt = (const double2 *)T.gt + (size_t)pulse * T.gstride;
-            T.M = (C4<C> *)T.M + (size_t)pulse * T.mstride;
-        }
-    }
+    const int pulse = T.plist ? T.plist[blockIdx.z] : 0;
+    coef += (size_t)pulse * T.lmax * 3;
+    const size_t mo = (size_t)pulse * T.mstride;
     if (RC) {
-        typedef typename R4<R>::T Q4;
         double pg[4] = {0, 0, 0, 0}, pgt[4] = {0, 0, 0, 0};
         {
-            const double *g = (const double *)T.g, *gt = (const double *)T.gt;
+            const double *g = (const double *)T.g + (size_t)pulse * T.gstride;
+            const double *gt = (const double *)T.gt + (size_t)pulse * T.gstride;
             for (int ia = 0; ia < 3; ia++) {
                 const double c = -coef[l * 3 + ia].y;     /* the stored table is -Im M */
                 for (int q = 0; q < 4; q++) {
@@ -438,21 +429,27 @@ __global__ void k_tables(TabP T, const double2 *__restrict__ coef)
                 }
             }
         }
-        Q4 *M = (Q4 *)T.M;
         for (int kk = 0; kk < T.nk; kk++) {
             const double kap = T.kvals[kk];
-            Q4 m;
-            m.a = (R)fma(kap, pg[1], pg[0]);
-            m.b = (R)fma(kap, pg[3], pg[2]);
-            m.c = (R)fma(kap, pgt[2], pgt[0]);
-            m.d = (R)fma(kap, pgt[3], pgt[1]);
-            M[((size_t)l * T.nk + kk) * per_l + slot] = m;
+            R4<double>::T m;
+            m.a = fma(kap, pg[1], pg[0]);
+            m.b = fma(kap, pg[3], pg[2]);
+            m.c = fma(kap, pgt[2], pgt[0]);
+            m.d = fma(kap, pgt[3], pgt[1]);
+            const size_t e = mo + ((size_t)l * T.nk + kk) * per_l + slot;
+            if (OUT & 1) ((R4<double>::T *)T.M)[e] = m;
+            if (OUT & 2) {
+                R4<float>::T f;
+                f.a = (float)m.a; f.b = (float)m.b; f.c = (float)m.c; f.d = (float)m.d;
+                ((R4<float>::T *)T.M32)[e] = f;
+            }
         }
     } else {
         double2 pg[4], pgt[4];
         for (int q = 0; q < 4; q++) { pg[q] = make_double2(0, 0); pgt[q] = make_double2(0, 0); }
         {
-            const double2 *g = (const double2 *)T.g, *gt = (const double2 *)T.gt;
+            const double2 *g = (const double2 *)T.g + (size_t)pulse * T.gstride;
+            const double2 *gt = (const double2 *)T.gt + (size_t)pulse * T.gstride;
             for (int ia = 0; ia < 3; ia++) {
                 const double2 c = coef[l * 3 + ia];
                 for (int q = 0; q < 4; q++) {
@@ -462,15 +459,21 @@ __global__ void k_tables(TabP T, const double2 *__restrict__ coef)
                 }
             }
         }
-        C4<C> *M = (C4<C> *)T.M;
         for (int kk = 0; kk < T.nk; kk++) {
             const double kap = T.kvals[kk];
-            C4<C> m;
-            m.a = mk<C>(fma(kap, pg[1].x, pg[0].x), fma(kap, pg[1].y, pg[0].y));
-            m.b = mk<C>(fma(kap, pg[3].x, pg[2].x), fma(kap, pg[3].y, pg[2].y));
-            m.c = mk<C>(fma(kap, pgt[2].x, pgt[0].x), fma(kap, pgt[2].y, pgt[0].y));
-            m.d = mk<C>(fma(kap, pgt[3].x, pgt[1].x), fma(kap, pgt[3].y, pgt[1].y));
-            M[((size_t)l * T.nk + kk) * per_l + slot] = m;
+            C4<double2> m;
+            m.a = make_double2(fma(kap, pg[1].x, pg[0].x), fma(kap, pg[1].y, pg[0].y));
+            m.b = make_double2(fma(kap, pg[3].x, pg[2].x), fma(kap, pg[3].y, pg[2].y));
+            m.c = make_double2(fma(kap, pgt[2].x, pgt[0].x), fma(kap, pgt[2].y, pgt[0].y));
+            m.d = make_double2(fma(kap, pgt[3].x, pgt[1].x), fma(kap, pgt[3].y, pgt[1].y));
+            const size_t e = mo + ((size_t)l * T.nk + kk) * per_l + slot;
+            if (OUT & 1) ((C4<double2> *)T.M)[e] = m;
+            if (OUT & 2) {
+                C4<float2> f;
+                f.a = make_float2((float)m.a.x, (float)m.a.y); f.b = make_float2((float)m.b.x, (float)m.b.y);
+                f.c = make_float2((float)m.c.x, (float)m.c.y); f.d = make_float2((float)m.d.x, (float)m.d.y);
+                ((C4<float2> *)T.M32)[e] = f;
+            }
         }
     }
 }
@@ -2194,31 +2197,28 @@ static int fill_coef(gade_solver *s, int k, const double *ft)
     return GADE_OK;
 }
 
-/* per-step radial tables of the listed pulses from d_coef (which: 1 FP64, 2 FP32) */
+/* per-step radial tables of the listed pulses from d_coef (which: 1 FP64, 2
+   FP32, 3 both in one pass) */
 static int launch_table_kernels(gade_solver *s, int which, cudaStream_t st)
 {
     TabP T;
     T.lmax = s->lmax; T.nk = s->nk; T.W = s->W; T.B = s->B;
-    T.kvals = s->d_kvals; T.g = s->d_g; T.gt = s->d_gt; T.M = s->d_M;
+    T.kvals = s->d_kvals; T.g = s->d_g; T.gt = s->d_gt; T.M = s->d_M; T.M32 = s->d_M32;
     T.plist = s->d_plist; T.gstride = s->gstride; T.mstride = s->mstride;
+    if (!s->d_M32) which &= 1;
+    if (!which) return GADE_OK;
     const int per_l = s->W * s->B, nt = 256;
     dim3 grid((unsigned)((per_l + nt - 1) / nt), s->lmax, s->nslot);
-    if (which & 1) {            /* FP64 tables */
-        prof_begin(s, st);
-        if (s->rc) k_tables<double, true><<<grid, nt, 0, st>>>(T, s->d_coef);
-        else k_tables<double, false><<<grid, nt, 0, st>>>(T, s->d_coef);
-        prof_end(s, st, 2);
-        CKL();
-        s->has_time = 1;
-    }
-    if ((which & 2) && s->d_M32) {   /* FP32 tables (mixed precision) */
-        T.M = s->d_M32;
-        prof_begin(s, st);
-        if (s->rc) k_tables<float, true><<<grid, nt, 0, st>>>(T, s->d_coef);
-        else k_tables<float, false><<<grid, nt, 0, st>>>(T, s->d_coef);
-        prof_end(s, st, 2);
-        CKL();
-    }
+    prof_begin(s, st);
+#define KT(OUT_) do { if (s->rc) k_tables<true, OUT_><<<grid, nt, 0, st>>>(T, s->d_coef); \
+                      else k_tables<false, OUT_><<<grid, nt, 0, st>>>(T, s->d_coef); } while (0)
+    if (which == 3) KT(3);
+    else if (which == 1) KT(1);
+    else KT(2);
+#undef KT
+    prof_end(s, st, 2);
+    CKL();
+    if (which & 1) s->has_time = 1;
     return GADE_OK;
 }
 
