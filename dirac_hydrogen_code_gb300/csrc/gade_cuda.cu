@@ -484,13 +484,13 @@ __global__ void k_tables(TabP T, const double2 *__restrict__ coef)
 /* Shared-memory carve-up of k_apply, computed the same way on the host
    (launch size) and in the kernel: every piece starts on a 32-byte boundary. */
 struct ApplySmem {
-    unsigned xr, ub, xs, ds, lcs, angc, ang, shred, total;
+    unsigned xr, ub, xs, ds, lcs, angc, ang, ord, shred, total;
 };
 
 __host__ __device__ __forceinline__ unsigned up32(unsigned o) { return (o + 31u) & ~31u; }
 
 __host__ __device__ __forceinline__ ApplySmem apply_smem(int CS, int W, int RM, int AM, int G, unsigned elem,
-                                                         unsigned ang4, int nt)
+                                                         unsigned ang4, int nt, int lmax)
 {
     ApplySmem s;
     unsigned o = 0;
@@ -501,6 +501,7 @@ __host__ __device__ __forceinline__ ApplySmem apply_smem(int CS, int W, int RM, 
     s.lcs = o;   o = up32(o + 4u * W * RM);
     s.angc = o;  o = up32(o + 4u * AM);
     s.ang = o;   o = up32(o + ang4 * AM);
+    s.ord = o;   o = up32(o + 16u * lmax);
     s.shred = o; o = up32(o + 8u * NRED * nt);
     s.total = o;
     return s;
@@ -535,7 +536,7 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 8 && SEP) ? 2 : 3)
        chunk's G x columns gather items fill the CTA's threads twice */
     constexpr int G = sizeof(R) == 8 ? APPLY_G64 : 4;
     const int CS = (P.CM + 2) & ~1;           /* column stride: CM + the zero column, even */
-    const ApplySmem L = apply_smem(CS, P.W, P.RM, P.AM, G, sizeof(C), sizeof(A4), blockDim.x);
+    const ApplySmem L = apply_smem(CS, P.W, P.RM, P.AM, G, sizeof(C), sizeof(A4), blockDim.x, P.lmax);
     C *xr = (C *)(smem_raw + L.xr);           /* [CS] */
     C4<C> *ub = (C4<C> *)(smem_raw + L.ub);   /* [G][CS] u, w, u', w' of a column */
     C *xs = (C *)(smem_raw + L.xs);           /* [CS] AX_MIX: x_n slice   */
@@ -543,6 +544,7 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 8 && SEP) ? 2 : 3)
     int *lcs = (int *)(smem_raw + L.lcs);     /* [W][RM] local column of each ELL slot (CM: empty) */
     int *angc = (int *)(smem_raw + L.angc);   /* [AM] coupled block of each angular term of row r */
     A4 *ang = (A4 *)(smem_raw + L.ang);       /* [AM] */
+    int4 *oinf = (int4 *)(smem_raw + L.ord);  /* [lmax] the piece's orders: l, first and end angular term */
     double *shred = (double *)(smem_raw + L.shred); /* [NRED * blockDim] */
 
     /* grid (pulse slot, segment): the slots of one segment run side by side,
@@ -602,6 +604,10 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 8 && SEP) ? 2 : 3)
         }
     }
 
+    for (int k = tid; k < pd.z - pd.y; k += nt) {
+        const int l = P.act_l[pd.y + k];
+        oinf[k] = make_int4(l, P.ang_ptr[r * P.lmax + l] - ea, P.ang_ptr[r * P.lmax + l + 1] - ea, 0);
+    }
     for (int c = tid; c < ncols; c += nt) xr[c] = xb[cols[c]];
     if (mode == AX_MIX) {
         const size_t vo = (size_t)pulse * P.vstride + (size_t)r * B;
@@ -666,8 +672,8 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 8 && SEP) ? 2 : 3)
         /* gather u, w, u', w' of ng orders at once: (order, column) items */
         for (int item = tid; item < ng * ncols; item += nt) {
             const int g = item / ncols, c = item - g * ncols;
-            const int l = P.act_l[ag + g];
-            const int e0 = P.ang_ptr[r * P.lmax + l] - ea, e1 = P.ang_ptr[r * P.lmax + l + 1] - ea;
+            const int4 oi = oinf[ag - pd.y + g];
+            const int e0 = oi.y, e1 = oi.z;
             const int gc = cols[c];
             const C *xc = x + gc;
             /* with the DKB zero blocks a first-half column needs no w' and a
@@ -697,7 +703,7 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 8 && SEP) ? 2 : 3)
         __syncthreads();
         if (i >= 0) {
             for (int g = 0; g < ng; g++) {
-                const int l = P.act_l[ag + g];
+                const int l = oinf[ag - pd.y + g].x;
                 const C4<C> *ug = ub + g * CS;
                 if constexpr (RC) {
                     typedef typename R4<R>::T Q4;
@@ -1941,7 +1947,7 @@ static void apply_dims(const gade_solver *s, size_t elem, int *nt, size_t *smem)
     const int G = elem == sizeof(double2) ? APPLY_G64 : 4;
     const unsigned ang4 = s->rc ? (unsigned)(2 * elem) : (unsigned)(4 * elem);   /* four angular factors */
     const int CS = (s->CM + 2) & ~1;                 /* columns + the zero column, even */
-    *smem = apply_smem(CS, s->W, s->RM, s->AM, G, (unsigned)elem, ang4, t).total;
+    *smem = apply_smem(CS, s->W, s->RM, s->AM, G, (unsigned)elem, ang4, t, s->lmax).total;
 }
 
 /* the operator kernel instance for a precision, coupling class and mode class */
