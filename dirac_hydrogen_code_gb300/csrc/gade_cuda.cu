@@ -36,6 +36,8 @@
 #include <cstdlib>
 #include <cstring>
 #include <type_traits>
+#include <algorithm>
+#include <utility>
 #include <vector>
 
 #include "gade_internal.h"
@@ -209,6 +211,11 @@ struct OpP {
     const int4 *pieces;
     void *piece_acc;
     unsigned int *unit_tick;
+    /* assembled operator (k_apply_asm): this step's coupling values
+       A[pair][W][B] and the coupled block of every (block row, block) pair;
+       a piece's order range is then a pair range */
+    const double *A;
+    const int *pair_c;
 };
 
 struct VecP {
@@ -478,6 +485,67 @@ __global__ void k_tables(TabP T, const double2 *__restrict__ coef)
     }
 }
 
+/* Outputs and dot partials of one row of the operator kernels, by mode:
+   accH = A x (or H x where S x is apart in accS), accD = S delta (AX_MIX). */
+template <typename C, bool SEP>
+__device__ __forceinline__ void apply_epilogue(int mode, const VecP &V, size_t gi, C accS, C accH, C accD,
+                                               double (&v)[NRED])
+{
+    const C ax = SEP ? cadd(accH, accS) : accH;
+    switch (mode) {
+    case AX_PLAIN:
+        ((C *)V.out0)[gi] = ax;
+        break;
+    case AX_PARTS:
+        ((C *)V.out0)[gi] = accS;
+        ((C *)V.out1)[gi] = accH;
+        break;
+    case AX_R0V: {          /* v = A y ; <r0, v> */
+        ((C *)V.out0)[gi] = ax;
+        const C r0 = ((const C *)V.in0)[gi];
+        v[0] = (double)r0.x * ax.x + (double)r0.y * ax.y;
+        v[1] = (double)r0.x * ax.y - (double)r0.y * ax.x;
+        break;
+    }
+    case AX_TS: {           /* t = A z ; <t,t>, <t,s> */
+        ((C *)V.out0)[gi] = ax;
+        const C sv = ((const C *)V.in0)[gi];
+        v[0] = (double)ax.x * ax.x + (double)ax.y * ax.y;
+        v[1] = (double)ax.x * sv.x + (double)ax.y * sv.y;
+        v[2] = (double)ax.x * sv.y - (double)ax.y * sv.x;
+        break;
+    }
+    case AX_RHS: {          /* rhs = -Hx + Sx ; r = rhs - (Hx + Sx) ; r0 = r */
+        const C rhs = csub(accS, accH);
+        const C rv = csub(rhs, ax);
+        ((C *)V.out0)[gi] = rhs;
+        ((C *)V.out1)[gi] = rv;
+        ((C *)V.out2)[gi] = rv;
+        v[0] = (double)rv.x * rv.x + (double)rv.y * rv.y;
+        v[1] = (double)rhs.x * rhs.x + (double)rhs.y * rhs.y;
+        break;
+    }
+    case AX_MIX: {          /* r = -S delta - H w ; b = S x_n - H w / 2 ; x_n^H S x_n */
+        const C rv = mk<C>(-accD.x - accH.x, -accD.y - accH.y);
+        ((C *)V.out0)[gi] = rv;
+        const C b = mk<C>(accS.x - 0.5 * accH.x, accS.y - 0.5 * accH.y);
+        v[0] = (double)b.x * b.x + (double)b.y * b.y;
+        v[1] = (double)rv.x * rv.x + (double)rv.y * rv.y;
+        const C xi = ((const C *)V.in0)[gi];
+        v[2] = (double)xi.x * accS.x + (double)xi.y * accS.y;
+        break;
+    }
+    case AX_RESTART: {      /* r = rhs - A x ; r0 = r */
+        const C rhs = ((const C *)V.in0)[gi];
+        const C rv = csub(rhs, ax);
+        ((C *)V.out1)[gi] = rv;
+        ((C *)V.out2)[gi] = rv;
+        v[0] = (double)rv.x * rv.x + (double)rv.y * rv.y;
+        break;
+    }
+    }
+}
+
 /* ------------------------------------------------------------------ */
 /* matrix-free operator                                                */
 /* ------------------------------------------------------------------ */
@@ -569,7 +637,6 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 8 && SEP) ? 2 : 3)
     for (int pc = P.seg_ptr[blockIdx.y]; pc < P.seg_ptr[blockIdx.y + 1]; pc = *(volatile int *)&s_pc + 1) {
     const int4 pd = P.pieces[pc];
     const int u = pd.x, r = u / P.nchunk, q = u - r * P.nchunk;
-    if (tid == 0) { s_pc = pc; s_pw = pd.w; }
     const int kk = P.row_kidx[r];
     const int nrows = P.chunk_nrows[q], ncols = P.chunk_ncols[q];
     /* two threads per output row, each with half of the ELL slots */
@@ -580,6 +647,7 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 8 && SEP) ? 2 : 3)
     const int *cols = P.chunk_cols + (size_t)q * CM;
     const C *xb = x + (size_t)r * B;
     __syncthreads();                          /* the previous piece is done with shared memory */
+    if (tid == 0) { s_pc = pc; s_pw = pd.w; } /* read back after the next barrier */
     {
         const int *gl = P.chunk_lcol + (size_t)q * W * P.RM;
         for (int e = tid; e < W * P.RM; e += nt) { const int v = gl[e]; lcs[e] = v < 0 ? CM : v; }
@@ -804,62 +872,279 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 8 && SEP) ? 2 : 3)
     double v[NRED] = {0, 0, 0, 0};
     if (half == 0 && i >= 0) {
         const size_t gi = (size_t)pulse * P.vstride + (size_t)r * B + i;
-        const C ax = SEP ? cadd(accH, accS) : accH;
-        switch (mode) {
-        case AX_PLAIN:
-            ((C *)V.out0)[gi] = ax;
-            break;
-        case AX_PARTS:
-            ((C *)V.out0)[gi] = accS;
-            ((C *)V.out1)[gi] = accH;
-            break;
-        case AX_R0V: {          /* v = A y ; <r0, v> */
-            ((C *)V.out0)[gi] = ax;
-            const C r0 = ((const C *)V.in0)[gi];
-            v[0] = (double)r0.x * ax.x + (double)r0.y * ax.y;
-            v[1] = (double)r0.x * ax.y - (double)r0.y * ax.x;
-            break;
-        }
-        case AX_TS: {           /* t = A z ; <t,t>, <t,s> */
-            ((C *)V.out0)[gi] = ax;
-            const C sv = ((const C *)V.in0)[gi];
-            v[0] = (double)ax.x * ax.x + (double)ax.y * ax.y;
-            v[1] = (double)ax.x * sv.x + (double)ax.y * sv.y;
-            v[2] = (double)ax.x * sv.y - (double)ax.y * sv.x;
-            break;
-        }
-        case AX_RHS: {          /* rhs = -Hx + Sx ; r = rhs - (Hx + Sx) ; r0 = r */
-            const C rhs = csub(accS, accH);
-            const C rv = csub(rhs, ax);
-            ((C *)V.out0)[gi] = rhs;
-            ((C *)V.out1)[gi] = rv;
-            ((C *)V.out2)[gi] = rv;
-            v[0] = (double)rv.x * rv.x + (double)rv.y * rv.y;
-            v[1] = (double)rhs.x * rhs.x + (double)rhs.y * rhs.y;
-            break;
-        }
-        case AX_MIX: {          /* r = -S delta - H w ; b = S x_n - H w / 2 ; x_n^H S x_n */
-            const C rv = mk<C>(-accD.x - accH.x, -accD.y - accH.y);
-            ((C *)V.out0)[gi] = rv;
-            const C b = mk<C>(accS.x - 0.5 * accH.x, accS.y - 0.5 * accH.y);
-            v[0] = (double)b.x * b.x + (double)b.y * b.y;
-            v[1] = (double)rv.x * rv.x + (double)rv.y * rv.y;
-            const C xi = ((const C *)V.in0)[gi];
-            v[2] = (double)xi.x * accS.x + (double)xi.y * accS.y;
-            break;
-        }
-        case AX_RESTART: {      /* r = rhs - A x ; r0 = r */
-            const C rhs = ((const C *)V.in0)[gi];
-            const C rv = csub(rhs, ax);
-            ((C *)V.out1)[gi] = rv;
-            ((C *)V.out2)[gi] = rv;
-            v[0] = (double)rv.x * rv.x + (double)rv.y * rv.y;
-            break;
-        }
-        }
+        apply_epilogue<C, SEP>(mode, V, gi, accS, accH, accD, v);
     }
     /* the unit's dot partials, indexed by unit (not by CTA): the final sum
        has the same order for every partition */
+    if (red.kind != RED_NONE) reduce_part(red, v, shred, (unsigned)u);
+    }
+    if (red.kind != RED_NONE) reduce_tail(red, shred, gridDim.y, (unsigned)(P.nchunk * P.nblk));
+}
+
+
+/* ------------------------------------------------------------------ */
+/* assembled operator (one FP64 pulse, real couplings)                 */
+/* ------------------------------------------------------------------ */
+/*
+ * The couplings of H(t) are linear in the six pulse factors, so for real
+ * couplings every off-diagonal value is A(t) = sum_a w_a(t) K_a with K_a
+ * the values for a unit factor a (built once from the matrix-free tables)
+ * and w_a(t) the step's coefficient of a.  An apply then costs 2 FMAs per
+ * stored value (a real value times a complex x) against ~4.4 in the
+ * matrix-free form, for an assembly of 3 FMAs per value once per step (the
+ * orders coupling a pair share a parity, which selects three of the six
+ * factors).
+ * Values are stored per (block row, coupled block) pair in the ELL slot
+ * layout [pair][W][B] of the radial tables, so one slot map serves every
+ * pair.
+ */
+
+/* K[pair][ia][slot][row] = sum over the pair's (order l, angular term e) of
+   M0(l,k_r) a0[e] + M1 a0k[e] + M2 a1[e] + M3 a1k[e], from the tables of a
+   unit factor a.  The orders coupling one pair share a parity (the angular
+   selection rules), and order l uses the factors a = (l%2+1)%2 + 2 ia, so a
+   pair stores three values per slot, ia = 0..2; the pairs of the other
+   parity are skipped.  grid (slot blocks, pairs) */
+__global__ void k_build_K(double *__restrict__ K, const R4<double>::T *__restrict__ M, int nk, int WB, int a,
+                          const int *__restrict__ pair_r, const int *__restrict__ pair_par,
+                          const int *__restrict__ row_kidx,
+                          const int *__restrict__ le_ptr, const int *__restrict__ le_l, const int *__restrict__ le_e,
+                          const double *__restrict__ a0, const double *__restrict__ a0k,
+                          const double *__restrict__ a1, const double *__restrict__ a1k)
+{
+    const int p = blockIdx.y;
+    const int e_in = blockIdx.x * blockDim.x + threadIdx.x;
+    const int base = (pair_par[p] + 1) % 2;      /* the parity's first factor */
+    if (e_in >= WB || base != a % 2) return;
+    const int ia = (a - base) / 2;
+    const int kk = row_kidx[pair_r[p]];
+    double acc = 0.0;
+    for (int k = le_ptr[p]; k < le_ptr[p + 1]; k++) {
+        const int l = le_l[k], e = le_e[k];
+        const R4<double>::T m = M[((size_t)l * nk + kk) * WB + e_in];
+        acc = fma(m.a, a0[e], acc);
+        acc = fma(m.b, a0k[e], acc);
+        acc = fma(m.c, a1[e], acc);
+        acc = fma(m.d, a1k[e], acc);
+    }
+    K[((size_t)p * 3 + ia) * WB + e_in] = acc;
+}
+
+/* this step's couplings A[pair] = sum_ia w_ia K[pair][ia], w_ia the
+   imaginary part of the step's coefficient of order parity par(pair) and
+   factor ia (coef[lpar * 3 + ia], lpar the first order of that parity).
+   grid (element blocks of a pair, pairs); two values per thread */
+__global__ void k_assemble(double2 *__restrict__ A, const double2 *__restrict__ K, int WB2,
+                           const int *__restrict__ pair_par, const double2 *__restrict__ coef, int2 lpar)
+{
+    const int p = blockIdx.y;
+    const int par = pair_par[p];
+    const int cb = 3 * (par ? lpar.y : lpar.x);
+    const double w0 = coef[cb].y, w1 = coef[cb + 1].y, w2 = coef[cb + 2].y;
+    const double2 *Kp = K + (size_t)p * 3 * WB2;
+    double2 *Ap = A + (size_t)p * WB2;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < WB2; e += gridDim.x * blockDim.x) {
+        const double2 k0 = __ldcs(&Kp[e]), k1 = __ldcs(&Kp[WB2 + e]), k2 = __ldcs(&Kp[2 * WB2 + e]);
+        double2 v;
+        v.x = fma(w2, k2.x, fma(w1, k1.x, w0 * k0.x));
+        v.y = fma(w2, k2.y, fma(w1, k1.y, w0 * k0.y));
+        Ap[e] = v;
+    }
+}
+
+#define ASM_GB 4   /* coupled blocks staged per phase */
+
+/* shared memory of k_apply_asm: x slices (x_r, x_n, delta), the staged
+   windows of ASM_GB coupled blocks, the slot map, the reduction buffer */
+__host__ __device__ __forceinline__ unsigned asm_smem(int CS, int W, int RM, int nt, unsigned *o_xw, unsigned *o_lcs,
+                                                      unsigned *o_red)
+{
+    unsigned o = up32(3u * 16u * CS);
+    *o_xw = o;  o = up32(o + 16u * ASM_GB * CS);
+    *o_lcs = o; o = up32(o + 4u * W * RM);
+    *o_red = o; o = up32(o + 8u * NRED * nt);
+    return o;
+}
+
+/*
+ * y = (S + H(t)) x with the assembled couplings: grid (pulse slot, segment)
+ * over the same units and pieces as k_apply (a piece's range is a range of
+ * (block row, coupled block) pairs).  Two threads per row, 15 ELL slots each
+ * with their local columns in registers; per group of ASM_GB coupled blocks
+ * the CTA stages the blocks' x windows in shared memory, then every thread
+ * streams its rows' values and adds value x window[column].
+ */
+template <bool SEP>
+__global__ void __launch_bounds__(256, 3)
+    k_apply_asm(OpP P, const double2 *__restrict__ x, int mode, VecP V, RedP red)
+{
+    constexpr int HJ = 15;
+    typedef double2 C;
+    extern __shared__ __align__(32) unsigned char smem_raw[];
+    const int CS = (P.CM + 2) & ~1;
+    unsigned oxw, olcs, ored;
+    asm_smem(CS, P.W, P.RM, blockDim.x, &oxw, &olcs, &ored);
+    C *xr = (C *)smem_raw, *xs = xr + CS, *ds = xs + CS;
+    C *xw = (C *)(smem_raw + oxw);
+    int *lcs = (int *)(smem_raw + olcs);
+    double *shred = (double *)(smem_raw + ored);
+
+    const int pulse = P.plist ? P.plist[blockIdx.x] : 0;
+    if (!red_select(red, pulse)) return;
+    x += (long long)pulse * P.vstride;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int B = P.B, W = P.W, CM = P.CM;
+    if (tid == 0) {
+        const C z = make_double2(0, 0);
+        xr[CM] = z; xs[CM] = z; ds[CM] = z;
+        for (int g = 0; g < ASM_GB; g++) xw[g * CS + CM] = z;
+    }
+    __shared__ int s_pc, s_pw;
+    for (int pc = P.seg_ptr[blockIdx.y]; pc < P.seg_ptr[blockIdx.y + 1]; pc = *(volatile int *)&s_pc + 1) {
+    const int4 pd = P.pieces[pc];
+    const int u = pd.x, r = u / P.nchunk, q = u - r * P.nchunk;
+    const int kk = P.row_kidx[r];
+    const int nrows = P.chunk_nrows[q], ncols = P.chunk_ncols[q];
+    const int half = tid / P.RM, trow = tid - half * P.RM;
+    const int i = (half < 2 && trow < nrows) ? P.chunk_rows[q * P.RM + trow] : -1;
+    const int jb = half == 0 ? 0 : (W + 1) / 2, je = half == 0 ? (W + 1) / 2 : W;
+    const int nj = je - jb;
+    const int *cols = P.chunk_cols + (size_t)q * CM;
+    const C *xb = x + (size_t)r * B;
+    __syncthreads();                          /* the previous piece is done with shared memory */
+    if (tid == 0) { s_pc = pc; s_pw = pd.w; } /* read back after the next barrier */
+    {
+        const int *gl = P.chunk_lcol + (size_t)q * W * P.RM;
+        for (int e = tid; e < W * P.RM; e += nt) { const int v = gl[e]; lcs[e] = v < 0 ? CM : v; }
+    }
+    for (int c = tid; c < ncols; c += nt) xr[c] = xb[cols[c]];
+    if (mode == AX_MIX) {
+        const size_t vo = (size_t)pulse * P.vstride + (size_t)r * B;
+        const C *xn = (const C *)V.in0 + vo, *dn = (const C *)V.in1 + vo;
+        for (int c = tid; c < ncols; c += nt) { xs[c] = xn[cols[c]]; ds[c] = dn[cols[c]]; }
+    }
+    __syncthreads();
+    unsigned lcp[(HJ + 1) / 2];
+#pragma unroll
+    for (int t = 0; t < HJ; t += 2) {
+        const unsigned c0 = (t < nj && trow < P.RM) ? lcs[(jb + t) * P.RM + trow] : CM;
+        const unsigned c1 = (t + 1 < HJ && t + 1 < nj && trow < P.RM) ? lcs[(jb + t + 1) * P.RM + trow] : CM;
+        lcp[t / 2] = c0 | (c1 << 16);
+    }
+#define LCO(t) ((int)(((t) & 1) ? (lcp[(t) >> 1] >> 16) : (lcp[(t) >> 1] & 0xffffu)))
+    const int jB = jb * B;
+    C accS = make_double2(0, 0), accH = accS, accD = accS;
+    if (i >= 0 && (pd.w & 0xffff) == 0) {     /* diagonal blocks: the unit's first piece */
+        if (SEP && mode == AX_MIX) {
+            const C *Se = (const C *)P.S_ell + (size_t)kk * W * B + i + jB;
+            const C *He = (const C *)P.Hst_ell + (size_t)pulse * P.dstride + (size_t)kk * W * B + i + jB;
+#pragma unroll
+            for (int t = 0; t < HJ; t++) {
+                const int lc = LCO(t);
+                const C sv = *Se;
+                cfma(accS, sv, xs[lc]);
+                cfma(accD, sv, ds[lc]);
+                cfma(accH, *He, xr[lc]);
+                if (t + 1 < nj) { Se += B; He += B; }
+            }
+        } else if (SEP) {
+            const C *Se = (const C *)P.S_ell + (size_t)kk * W * B + i + jB;
+            const C *He = (const C *)P.Hst_ell + (size_t)pulse * P.dstride + (size_t)kk * W * B + i + jB;
+#pragma unroll
+            for (int t = 0; t < HJ; t++) {
+                const C xv = xr[LCO(t)];
+                cfma(accS, *Se, xv);
+                cfma(accH, *He, xv);
+                if (t + 1 < nj) { Se += B; He += B; }
+            }
+        } else {
+            const C *De = (const C *)P.D_ell + (size_t)pulse * P.dstride + (size_t)kk * W * B + i + jB;
+#pragma unroll
+            for (int t = 0; t < HJ; t++) {
+                cfma(accH, *De, xr[LCO(t)]);
+                if (t + 1 < nj) De += B;
+            }
+        }
+    }
+    const size_t WB = (size_t)W * B;
+    for (int pg = pd.y; pg < pd.z; pg += ASM_GB) {
+        const int ng = pd.z - pg < ASM_GB ? pd.z - pg : ASM_GB;
+        __syncthreads();     /* staging done / previous group's products done */
+        for (int item = tid; item < ng * ncols; item += nt) {
+            const int g = item / ncols, c = item - g * ncols;
+            xw[g * CS + c] = x[(size_t)P.pair_c[pg + g] * B + cols[c]];
+        }
+        __syncthreads();
+        if (i >= 0) {
+            for (int g = 0; g < ng; g++) {
+                const double *Av = P.A + (size_t)(pg + g) * WB + i + jB;
+                const C *xg = xw + g * CS;
+#pragma unroll
+                for (int t = 0; t < HJ; t++) {
+                    rfma(accH, __ldcs(Av), xg[LCO(t)]);
+                    if (t + 1 < nj) Av += B;
+                }
+            }
+        }
+    }
+#undef LCO
+    /* combine the two halves of every row */
+    __syncthreads();
+    {
+        C *xch = (C *)shred;
+        if (SEP) {
+            if (half == 1 && i >= 0) { xch[3 * trow] = accS; xch[3 * trow + 1] = accH; xch[3 * trow + 2] = accD; }
+            __syncthreads();
+            if (half == 0 && i >= 0) {
+                accS = cadd(accS, xch[3 * trow]);
+                accH = cadd(accH, xch[3 * trow + 1]);
+                accD = cadd(accD, xch[3 * trow + 2]);
+            }
+        } else {
+            if (half == 1 && i >= 0) xch[trow] = accH;
+            __syncthreads();
+            if (half == 0 && i >= 0) accH = cadd(accH, xch[trow]);
+        }
+        __syncthreads();
+    }
+    const int pw = *(volatile int *)&s_pw;
+    const int pi = pw & 0xffff, np = pw >> 16;
+    if (np > 1) {
+        const int pcc = *(volatile int *)&s_pc;
+        __shared__ int piece_last;
+        C *acc = (C *)P.piece_acc;
+        const size_t RM3 = (size_t)3 * P.RM;
+        if (half == 0 && i >= 0) {
+            acc[pcc * RM3 + P.RM + trow] = accH;
+            if (SEP) { acc[pcc * RM3 + trow] = accS; acc[pcc * RM3 + 2 * P.RM + trow] = accD; }
+        }
+        __threadfence();
+        __syncthreads();
+        if (tid == 0) {
+            const unsigned t = atomicAdd(&P.unit_tick[u], 1u);
+            piece_last = (t == (unsigned)np - 1u);
+        }
+        __syncthreads();
+        if (!piece_last) continue;
+        __threadfence();
+        if (half == 0 && i >= 0) {
+            accS = make_double2(0, 0); accH = accS; accD = accS;
+            for (int k = 0; k < np; k++) {
+                const size_t pk = (size_t)(pcc - pi + k) * RM3;
+                accH = cadd(accH, __ldcg(&acc[pk + P.RM + trow]));
+                if (SEP) {
+                    accS = cadd(accS, __ldcg(&acc[pk + trow]));
+                    accD = cadd(accD, __ldcg(&acc[pk + 2 * P.RM + trow]));
+                }
+            }
+        }
+        if (tid == 0) P.unit_tick[u] = 0u;
+    }
+    double v[NRED] = {0, 0, 0, 0};
+    if (half == 0 && i >= 0) {
+        const size_t gi = (size_t)pulse * P.vstride + (size_t)r * B + i;
+        apply_epilogue<C, SEP>(mode, V, gi, accS, accH, accD, v);
+    }
     if (red.kind != RED_NONE) reduce_part(red, v, shred, (unsigned)u);
     }
     if (red.kind != RED_NONE) reduce_tail(red, shred, gridDim.y, (unsigned)(P.nchunk * P.nblk));
@@ -1344,6 +1629,20 @@ struct gade_solver {
     int bal_waves;              /* balanced segments per resident CTA slot (timed at creation) */
     gade_batch *engine;         /* step engine of a single-pulse solver (device control, graphs) */
     int zskip;                  /* the DKB zero blocks hold for every pulse's tables */
+    /* assembled operator (one FP64 pulse, real couplings): A(t) = sum_a w_a(t) K_a */
+    int asm_ok;                 /* K_a built */
+    int use_asm;                /* applies and steps use it */
+    int asm_part;               /* its partition: 0 plain, 1 balanced */
+    int npairs;                 /* (block row, coupled block) pairs */
+    int *d_pair_c;
+    double *d_K, *d_A;          /* [pairs][3][W][B], [pairs][W][B] */
+    int *d_pair_par;            /* [pairs] parity of the orders coupling the pair */
+    int lpar[2];                /* first order of each parity (-1: none) */
+    std::vector<int> h_pair_ptr, h_pair_r, h_pair_par, h_le_ptr, h_le_l, h_le_e;   /* pairs per block row; (order, term) per pair */
+    PartList part_asm[3];       /* plain, balanced (one accumulator), balanced (S, H apart) */
+    int occ_asm[2];
+    float asm_ms[2];            /* timed FP64 apply: [0] plain, [1] balanced partition */
+    float mf_ms;                /* best timed matrix-free apply */
 };
 
 static int solver_engine_step(gade_solver *s, const double *ft, int32_t maxit, double tol, gade_step_stats *stats);
@@ -1902,6 +2201,43 @@ static int solver_create(const gade_problem *p, int npulse, const double *dts, c
     }
     /* block solves: per lane and chunk, bw band terms + 32 inverse terms, 2 sweeps */
     s->precond_flops = 2.0 * 4.0 * (double)s->nblk * 32.0 * s->nch * 2.0 * (s->bwp + 32);
+    if (npulse == 1 && s->rc && precision == GADE_PREC_FP64) {
+        /* (block row, coupled block) pairs and the (order, angular term) list
+           of every pair, for the assembled operator */
+        s->h_pair_ptr.assign(1, 0);
+        for (int r = 0; r < s->nblk; r++) {
+            std::vector<std::pair<int, std::pair<int, int>>> ent;   /* (c, (l, e)) */
+            for (int l = 0; l < s->lmax; l++)
+                for (int e = su->ang_ptr[r * s->lmax + l]; e < su->ang_ptr[r * s->lmax + l + 1]; e++)
+                    ent.push_back({su->ang_c[e], {l, e}});
+            std::stable_sort(ent.begin(), ent.end(),
+                             [](const std::pair<int, std::pair<int, int>> &a, const std::pair<int, std::pair<int, int>> &b) {
+                                 return a.first < b.first;
+                             });
+            for (size_t k = 0; k < ent.size(); k++) {
+                if (k == 0 || ent[k].first != ent[k - 1].first) {
+                    s->h_pair_r.push_back(r);
+                    s->h_pair_par.push_back(ent[k].second.first % 2);
+                    s->h_le_ptr.push_back((int)s->h_le_l.size());
+                    s->npairs++;
+                }
+                if (ent[k].second.first % 2 != s->h_pair_par.back()) s->h_pair_par.back() = -1;   /* mixed parity */
+                s->h_le_l.push_back(ent[k].second.first);
+                s->h_le_e.push_back(ent[k].second.second);
+            }
+            s->h_pair_ptr.push_back(s->npairs);
+        }
+        s->h_le_ptr.push_back((int)s->h_le_l.size());
+        std::vector<int> pc;
+        for (int r = 0; r < s->nblk; r++) {
+            int last = -1;
+            std::vector<int> cs;
+            for (int e = su->ang_ptr[r * s->lmax]; e < su->ang_ptr[(r + 1) * s->lmax]; e++) cs.push_back(su->ang_c[e]);
+            std::sort(cs.begin(), cs.end());
+            for (int c : cs) if (c != last) { pc.push_back(c); last = c; }
+        }
+        UP(s->d_pair_c, pc.data(), pc.size());
+    }
     gade_setup_release(su);
 #undef UP
 #define UP(dst, src, cnt) do { int rc_ = dev_upload(s, &(dst), (src), (size_t)(cnt)); if (rc_) { gade_solver_free(s); return rc_; } } while (0)
@@ -2143,9 +2479,182 @@ static int op_partition(const gade_solver *s, OpP &P, bool fp32, int mode)
     return pl->nseg;
 }
 
+static int launch_table_kernels(gade_solver *s, int which, cudaStream_t st);
+
+/* the assembled operator's partitions: plain (one piece per unit) and
+   balanced (units laid on a line by work: 2 FMAs per stored value, plus the
+   staging of a coupled block's x window and a unit's diagonal blocks) */
+static int asm_partitions(gade_solver *s)
+{
+    const int nunit = s->nchunk * s->nblk;
+    int rc;
+    {
+        std::vector<int> seg(1, 0);
+        std::vector<int4> pcs;
+        for (int u = 0; u < nunit; u++) {
+            const int r = u / s->nchunk;
+            pcs.push_back(make_int4(u, s->h_pair_ptr[r], s->h_pair_ptr[r + 1], 0 | (1 << 16)));
+            seg.push_back((int)pcs.size());
+        }
+        if ((rc = part_upload(s, s->part_asm[0], seg, pcs))) return rc;
+    }
+    auto pcost = [&](int q) { return 2.0 * s->h_chunk_nrows[q] * s->W + 2.0 * s->h_chunk_ncols[q]; };
+    auto ufix = [&](int q) { return 4.0 * s->h_chunk_nrows[q] * s->W; };
+    for (int cls = 0; cls < 2; cls++) {
+        const int nseg = s->occ_asm[cls] * s->nsm;
+        double total = 0;
+        for (int u = 0; u < nunit; u++) {
+            const int r = u / s->nchunk, q = u - r * s->nchunk;
+            total += ufix(q) + pcost(q) * (s->h_pair_ptr[r + 1] - s->h_pair_ptr[r]);
+        }
+        const double T = total / nseg;
+        auto seg_of = [&](double mid) { int k = (int)(mid / T); return k < 0 ? 0 : (k >= nseg ? nseg - 1 : k); };
+        std::vector<int4> pcs;
+        std::vector<int> pseg;
+        double pos = 0;
+        for (int u = 0; u < nunit; u++) {
+            const int r = u / s->nchunk, q = u - r * s->nchunk;
+            const int a0 = s->h_pair_ptr[r], a1 = s->h_pair_ptr[r + 1];
+            const size_t first = pcs.size();
+            if (a0 == a1) { pcs.push_back(make_int4(u, a0, a0, 0)); pseg.push_back(seg_of(pos + 0.5 * ufix(q))); }
+            pos += ufix(q);
+            int cur = -1, b0 = a0;
+            for (int a = a0; a < a1; a++) {
+                const int sg = seg_of(pos + 0.5 * pcost(q));
+                pos += pcost(q);
+                if (sg != cur) {
+                    if (cur >= 0) { pcs.push_back(make_int4(u, b0, a, 0)); pseg.push_back(cur); }
+                    cur = sg;
+                    b0 = a;
+                }
+            }
+            if (a1 > a0) { pcs.push_back(make_int4(u, b0, a1, 0)); pseg.push_back(cur); }
+            const int np = (int)(pcs.size() - first);
+            for (int k = 0; k < np; k++) pcs[first + k].w = k | (np << 16);
+        }
+        std::vector<int> seg((size_t)nseg + 1, 0);
+        for (int sg : pseg) seg[sg + 1]++;
+        for (int k = 0; k < nseg; k++) seg[k + 1] += seg[k];
+        if ((rc = part_upload(s, s->part_asm[1 + cls], seg, pcs))) return rc;
+    }
+    return GADE_OK;
+}
+
+static size_t asm_smem_bytes(const gade_solver *s)
+{
+    unsigned a, b, c;
+    return asm_smem((s->CM + 2) & ~1, s->W, s->RM, 256, &a, &b, &c);
+}
+
+/* Builds K_a for every pulse factor a that some Bessel order uses: the
+   tables of a unit factor, then every pair's values from them.  Skipped
+   (the solver stays matrix-free) when K would take more than half of the
+   free device memory. */
+static int asm_build(gade_solver *s)
+{
+    if (s->npulse != 1 || !s->rc || s->prec != GADE_PREC_FP64 || s->npairs == 0 || s->asm_ok) return GADE_OK;
+    for (int par : s->h_pair_par)
+        if (par < 0) return GADE_OK;             /* a pair coupled by both parities: stay matrix-free */
+    const size_t WB = (size_t)s->W * s->B, per = (size_t)s->npairs * WB;
+    if (WB % 2) return GADE_OK;
+    s->lpar[0] = s->lmax > 0 ? 0 : -1;
+    s->lpar[1] = s->lmax > 1 ? 1 : -1;
+    size_t fr = 0, tot = 0;
+    CK(cudaMemGetInfo(&fr, &tot));
+    if (sizeof(double) * per * 4 > fr / 2) return GADE_OK;
+    int rc;
+    if ((rc = dev_upload(s, &s->d_K, (const double *)nullptr, per * 3))) return rc;
+    if ((rc = dev_upload(s, &s->d_A, (const double *)nullptr, per))) return rc;
+    if ((rc = dev_upload(s, &s->d_pair_par, s->h_pair_par.data(), s->h_pair_par.size()))) return rc;
+    int *d_pr = nullptr, *d_lp = nullptr, *d_ll = nullptr, *d_le = nullptr;
+    if ((rc = dev_upload(s, &d_pr, s->h_pair_r.data(), s->h_pair_r.size()))) return rc;
+    if ((rc = dev_upload(s, &d_lp, s->h_le_ptr.data(), s->h_le_ptr.size()))) return rc;
+    if ((rc = dev_upload(s, &d_ll, s->h_le_l.data(), s->h_le_l.size()))) return rc;
+    if ((rc = dev_upload(s, &d_le, s->h_le_e.data(), s->h_le_e.size()))) return rc;
+    const int prof = s->profile;
+    s->profile = 0;
+    for (int a = 0; a < 6 && !rc; a++) {
+        int l0 = -1;
+        for (int l = 0; l < s->lmax && l0 < 0; l++)
+            if ((l % 2 + 1) % 2 == a % 2) l0 = l;
+        if (l0 < 0) continue;
+        const int ia = (a - (l0 % 2 + 1) % 2) / 2;
+        /* the previous factor's coefficient copy reads the pinned buffer
+           when it runs: wait for it before rewriting the buffer */
+        if (cudaStreamSynchronize(s->stream) != cudaSuccess) { rc = fail(GADE_ERR_CUDA, "assembled operator: K build failed"); break; }
+        /* coefficients of a unit factor a: imaginary part 1 in every order of its parity */
+        for (int l = 0; l < s->lmax; l++)
+            for (int j = 0; j < 3; j++)
+                s->h_coef[l * 3 + j] = make_double2(0.0, ((l % 2 + 1) % 2 == a % 2 && j == ia) ? 1.0 : 0.0);
+        if (cudaMemcpyAsync(s->d_coef, s->h_coef, sizeof(double2) * s->lmax * 3, cudaMemcpyHostToDevice,
+                            s->stream) != cudaSuccess) { rc = fail(GADE_ERR_CUDA, "assembled operator: coefficient upload failed"); break; }
+        if ((rc = launch_table_kernels(s, 1, s->stream))) break;
+        dim3 grid((unsigned)((WB + 255) / 256), (unsigned)s->npairs);
+        k_build_K<<<grid, 256, 0, s->stream>>>(s->d_K, (const R4<double>::T *)s->d_M, s->nk, (int)WB, a, d_pr,
+                                               s->d_pair_par, s->d_row_kidx, d_lp, d_ll, d_le,
+                                               (const double *)s->d_ang_a0, (const double *)s->d_ang_a0k,
+                                               (const double *)s->d_ang_a1, (const double *)s->d_ang_a1k);
+        if (cudaGetLastError() != cudaSuccess) { rc = fail(GADE_ERR_CUDA, "assembled operator: K build launch failed"); break; }
+    }
+    if (!rc && cudaStreamSynchronize(s->stream) != cudaSuccess) rc = fail(GADE_ERR_CUDA, "assembled operator: K build failed");
+    s->profile = prof;
+    s->has_time = 0;             /* the tables held a unit factor */
+    dev_release(s, d_pr); dev_release(s, d_lp); dev_release(s, d_ll); dev_release(s, d_le);
+    if (rc) return rc;
+    for (int sep = 0; sep < 2; sep++) {
+        int n = 0;
+        cudaError_t e = sep ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_apply_asm<true>, 256, asm_smem_bytes(s))
+                            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_apply_asm<false>, 256, asm_smem_bytes(s));
+        if (e != cudaSuccess || n < 1) { cudaGetLastError(); n = 1; }
+        s->occ_asm[sep] = n > 8 ? 8 : n;
+    }
+    if ((rc = asm_partitions(s))) return rc;
+    s->asm_ok = 1;
+    return GADE_OK;
+}
+
+/* this step's assembled couplings from d_coef */
+static int launch_assemble(gade_solver *s, cudaStream_t st)
+{
+    const int WB2 = s->W * s->B / 2;
+    prof_begin(s, st);
+    k_assemble<<<dim3((unsigned)((WB2 + 255) / 256), (unsigned)s->npairs), 256, 0, st>>>(
+        (double2 *)s->d_A, (const double2 *)s->d_K, WB2, s->d_pair_par, s->d_coef, make_int2(s->lpar[0], s->lpar[1]));
+    prof_end(s, st, 2);
+    CKL();
+    s->has_time = 1;
+    return GADE_OK;
+}
+
+/* the step's FP64 tables: assembled couplings or the matrix-free radial tables */
+static int launch_step_tables(gade_solver *s, cudaStream_t st)
+{
+    return s->use_asm ? launch_assemble(s, st) : launch_table_kernels(s, 1, st);
+}
+
+static int launch_apply_asm(gade_solver *s, const double2 *x, int mode, VecP V, RedP red, cudaStream_t st)
+{
+    OpP P = op_params(s);
+    P.A = s->d_A;
+    P.pair_c = s->d_pair_c;
+    const bool sep = mode == AX_RHS || mode == AX_PARTS || mode == AX_MIX;
+    const PartList &pl = s->asm_part ? s->part_asm[1 + (sep ? 1 : 0)] : s->part_asm[0];
+    P.seg_ptr = pl.d_seg_ptr;
+    P.pieces = pl.d_pieces;
+    dim3 grid(s->nslot, pl.nseg);
+    const size_t smem = asm_smem_bytes(s);
+    prof_begin(s, st);
+    if (sep) k_apply_asm<true><<<grid, 256, smem, st>>>(P, x, mode, V, red);
+    else k_apply_asm<false><<<grid, 256, smem, st>>>(P, x, mode, V, red);
+    prof_end(s, st, 0);
+    CKL();
+    return GADE_OK;
+}
+
 static int launch_apply(gade_solver *s, const double2 *x, int mode, VecP V, int redkind, cudaStream_t st,
                         int pred = PRED_NONE, DevScal *pb = nullptr)
 {
+    if (s->use_asm) return launch_apply_asm(s, x, mode, V, make_red(s, s->d_sc, redkind, pred, nullptr, pb), st);
     OpP P = op_params(s);
     RedP red = make_red(s, s->d_sc, redkind, pred, nullptr, pb);
     dim3 grid(s->nslot, op_partition(s, P, false, mode));
@@ -2233,6 +2742,11 @@ static int launch_tables(gade_solver *s, const double *ft, int which = 1)
     int rc = fill_coef(s, 0, ft);
     if (rc) return rc;
     CK(cudaMemcpyAsync(s->d_coef, s->h_coef, sizeof(double2) * (size_t)s->lmax * 3, cudaMemcpyHostToDevice, s->stream));
+    if (s->use_asm && (which & 1)) {
+        if ((rc = launch_assemble(s, s->stream))) return rc;
+        which &= ~1;
+        if (!which) return GADE_OK;
+    }
     return launch_table_kernels(s, which, s->stream);
 }
 
@@ -2441,6 +2955,82 @@ static int choose_split(gade_solver *s)
     return GADE_OK;
 }
 
+/* ms per FP64 apply (R0V) of the current operator and partition */
+static int time_fp64_apply(gade_solver *s, float *ms)
+{
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    int rc = GADE_OK;
+    for (int rep = 0; rep < 4 && !rc; rep++) {
+        if (rep == 1 && cudaEventRecord(e0, s->stream) != cudaSuccess) rc = fail(GADE_ERR_CUDA, "event record failed");
+        VecP V = {}; V.out0 = s->tmp1; V.in0 = s->r0;
+        if (!rc) rc = launch_apply(s, s->x, AX_R0V, V, RED_R0V, s->stream);
+    }
+    float t = 0;
+    if (!rc && (cudaEventRecord(e1, s->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                cudaEventElapsedTime(&t, e0, e1) != cudaSuccess))
+        rc = fail(GADE_ERR_CUDA, "apply timing failed");
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms = t / 3;
+    return rc;
+}
+
+/*
+ * Matrix-free or assembled operator for one FP64 pulse with real couplings:
+ * the assembled values (K_a) are built, both of their partitions timed, and
+ * the assembled operator is kept when its apply is clearly faster than the
+ * matrix-free one chosen by choose_split (its per-step assembly replaces the
+ * radial tables).
+ */
+static int choose_operator(gade_solver *s)
+{
+    s->mf_ms = s->split_ms[s->nsplit >= 1 && s->nsplit <= 4 ? s->nsplit : 0];
+    s->asm_ms[0] = s->asm_ms[1] = 0.f;
+    int rc = asm_build(s);
+    if (rc || !s->asm_ok) return rc;
+    s->use_asm = 1;
+    for (int part = 0; part < 2 && !rc; part++) {
+        s->asm_part = part;
+        rc = time_fp64_apply(s, &s->asm_ms[part]);
+    }
+    if (rc) { s->use_asm = 0; return rc; }
+    s->asm_part = s->asm_ms[1] < s->asm_ms[0] ? 1 : 0;
+    const float best = s->asm_ms[s->asm_part];
+    s->use_asm = (s->mf_ms <= 0.f || best < 0.98f * s->mf_ms) ? 1 : 0;
+    return GADE_OK;
+}
+
+extern "C" int gade_solver_set_operator(gade_solver *s, int32_t assembled)
+{
+    if (!s) return fail(GADE_ERR_ARG, "gade_solver_set_operator: NULL solver");
+    if (assembled != 0 && assembled != 1)
+        return fail(GADE_ERR_ARG, "gade_solver_set_operator: %d is neither 0 (matrix-free) nor 1 (assembled)", assembled);
+    CK(cudaSetDevice(s->device));
+    CK(cudaStreamSynchronize(s->stream));
+    int rc;
+    if (assembled && !s->asm_ok) {
+        if ((rc = asm_build(s))) return rc;
+        if (!s->asm_ok)
+            return fail(GADE_ERR_ARG, "gade_solver_set_operator: the assembled operator needs one FP64 pulse with "
+                                      "real couplings and device memory for its values");
+        s->asm_part = 1;
+    }
+    if (s->engine) batch_drop_graphs(s->engine);
+    s->use_asm = assembled;
+    s->has_time = 0;             /* the next set_time or step fills the chosen operator's tables */
+    return GADE_OK;
+}
+
+extern "C" int gade_solver_operator(const gade_solver *s, int32_t *assembled, float *ms)
+{
+    if (!s) return fail(GADE_ERR_ARG, "gade_solver_operator: NULL solver");
+    if (assembled) *assembled = s->use_asm;
+    if (ms) { ms[0] = s->mf_ms; ms[1] = s->asm_ms[0]; ms[2] = s->asm_ms[1]; }
+    return GADE_OK;
+}
+
 extern "C" int gade_solver_create(const gade_problem *p, double dt, double h, int32_t precision,
                                   int32_t device, gade_solver **out)
 {
@@ -2452,6 +3042,7 @@ extern "C" int gade_solver_create(const gade_problem *p, double dt, double h, in
     int rc = solver_create(p, 1, &dt, nullptr, h, precision, device, 0, out);
     if (rc) return rc;
     if ((rc = choose_split(*out))) { gade_solver_free(*out); *out = nullptr; return rc; }
+    if ((rc = choose_operator(*out))) { gade_solver_free(*out); *out = nullptr; return rc; }
     return GADE_OK;
 }
 
@@ -2677,6 +3268,17 @@ extern "C" int gade_solver_apply_dot_noalloc(gade_solver *s, const void *x_dev, 
     VecP V = {};
     V.out0 = y_dev;
     V.in0 = r0_dev;
+    if (s->use_asm) {
+        /* the assembled operator, one piece per unit */
+        P.A = s->d_A;
+        P.pair_c = s->d_pair_c;
+        P.seg_ptr = s->part_asm[0].d_seg_ptr;
+        P.pieces = s->part_asm[0].d_pieces;
+        k_apply_asm<false><<<dim3(1, s->part_asm[0].nseg), 256, asm_smem_bytes(s), st>>>(
+            P, (const double2 *)x_dev, AX_R0V, V, red);
+        CKL();
+        return GADE_OK;
+    }
     dim3 grid(1, s->part_split[1].nseg);
     int nt;
     size_t smem;
@@ -2801,7 +3403,7 @@ static int batch_seq_first(gade_batch *b, cudaStream_t st)
         CKL();
         return batch_seq_sweep(b, b->kiter, st);
     }
-    if ((rc = launch_table_kernels(s, 1, st))) return rc;
+    if ((rc = launch_step_tables(s, st))) return rc;
     VecP V = {};
     V.out0 = s->rhs; V.out1 = s->r; V.out2 = s->r0;
     if ((rc = launch_apply(s, s->x, AX_RHS, V, RED_RHS, st, PRED_NONE))) return rc;

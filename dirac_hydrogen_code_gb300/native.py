@@ -86,6 +86,8 @@ _SIGS = {
     "gade_solver_split": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.c_void_p]),
     "gade_solver_set_split": (C.c_int, [C.c_void_p, C.c_int32]),
     "gade_solver_apply_bytes": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
+    "gade_solver_set_operator": (C.c_int, [C.c_void_p, C.c_int32]),
+    "gade_solver_operator": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.c_void_p]),
     "gade_solver_balanced": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                        C.POINTER(C.c_float), C.POINTER(C.c_double)]),
     "gade_solver_apply_dot_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -307,6 +309,18 @@ class Solver:
         _check(load_library().gade_solver_balanced(self._h, C.byref(seg), C.byref(pcs), C.byref(ms), C.byref(gw)))
         return {"segments": int(seg.value), "pieces": int(pcs.value), "ms": float(ms.value),
                 "gather_weight": float(gw.value)}
+
+    def operator(self) -> dict:
+        """Operator in use (0 matrix-free, 1 assembled) and the timed FP64
+        applies: matrix-free, assembled with the plain and the balanced partition."""
+        a = C.c_int32()
+        ms = (C.c_float * 3)()
+        _check(load_library().gade_solver_operator(self._h, C.byref(a), ms))
+        return {"assembled": int(a.value), "matrix_free_ms": float(ms[0]),
+                "assembled_plain_ms": float(ms[1]), "assembled_balanced_ms": float(ms[2])}
+
+    def set_operator(self, assembled: int):
+        _check(load_library().gade_solver_set_operator(self._h, int(assembled)))
 
     def apply_bytes(self) -> float:
         """Compulsory DRAM bytes of one FP64 BiCGSTAB operator apply."""

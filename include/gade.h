@@ -168,6 +168,21 @@ int gade_solver_set_split(gade_solver *s, int32_t nsplit);
 int gade_solver_balanced(const gade_solver *s, int32_t *segments, int32_t *pieces, float *ms,
                          double *gather_weight);
 
+/* Operator of a single FP64 pulse with real couplings (no reference
+ * counterpart): matrix-free (0) or assembled (1).  The couplings of H(t) are
+ * linear in the six pulse factors, so the solver can store the coupling
+ * values of each unit factor once (K_a, built from the radial tables) and
+ * form this step's values as sum_a w_a(t) K_a; an apply then streams the
+ * values (2 FMAs each).  gade_solver_create times both and keeps the faster
+ * (the assembled one needs 7 x 8 bytes per stored coupling value of device
+ * memory).  gade_solver_operator reports the choice and, in ms (3 floats,
+ * may be NULL), the timed matrix-free apply and the assembled one with the
+ * plain and the balanced partition (0 where not timed).  After
+ * gade_solver_set_operator the next gade_solver_set_time or step fills the
+ * chosen operator's tables. */
+int gade_solver_set_operator(gade_solver *s, int32_t assembled);
+int gade_solver_operator(const gade_solver *s, int32_t *assembled, float *ms);
+
 /* FP64 flops (2 per FMA) executed by one operator apply and one
  * preconditioner solve, counted exactly from the set-up structure. */
 int gade_solver_flops(const gade_solver *s, double *apply_flops, double *precond_flops);

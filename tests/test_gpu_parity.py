@@ -36,13 +36,18 @@ def _setup(workdirs, name):
     return d, params, info, T, dt
 
 
+@pytest.mark.parametrize("op", [0, 1])
 @pytest.mark.parametrize("name", ["tiny_dipole", "tiny_nondipole", "dipole_small"])
-def test_operator_matches_oracle(workdirs, native_lib, name):
+def test_operator_matches_oracle(workdirs, native_lib, name, op):
+    """Matrix-free (0) and assembled (1) operator against the oracle's
+    assembly of the reference's matrices."""
     d, params, info, T, dt = _setup(workdirs, name)
     p = O.load_problem(d, info["lmax"])
     prob = Problem(d, info["lmax"])
     assert prob.info["real_coupling"] == 1
     sol = Solver(prob, dt)
+    sol.set_operator(op)
+    assert sol.operator()["assembled"] == op
     rng = np.random.default_rng(7)
     x = rng.standard_normal(p.n) + 1j * rng.standard_normal(p.n)
     for t in (0.25 * T, 0.8 * T):
@@ -286,3 +291,51 @@ def test_balanced_partition_mixed_precision(workdirs, native_lib):
         out.append(sol.get_x())
         sol.close()
     assert _rel(out[1], out[0]) < 1e-8
+
+
+@pytest.mark.parametrize("name", ["tiny_dipole", "tiny_nondipole"])
+def test_assembled_operator_steps_match_matrix_free(workdirs, native_lib, name):
+    """CN steps with the assembled couplings (sum of unit-factor values
+    weighted by the step's pulse factors) match the matrix-free ones: same
+    iterations, states within summation-order differences."""
+    d, params, info, T, dt = _setup(workdirs, name)
+    prob = Problem(d, info["lmax"])
+    psi, _ = prob.psi0()
+    fts = [pulse(params["Intensity"], params["Omega"], params["Cycles"], t)
+           for _, t in step_times(T, params["Ntime"])[1][:8]]
+    out = []
+    for op in (0, 1):
+        sol = Solver(prob, dt)
+        sol.set_operator(op)
+        sol.set_x(psi)
+        its = [sol.step(ft, maxit=500, tol=1e-12)["iters"] for ft in fts]
+        out.append((sol.get_x(), its))
+        sol.close()
+    assert out[1][1] == out[0][1]
+    assert _rel(out[1][0], out[0][0]) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["tiny_nondipole", "dipole_small"])
+def test_partitions_give_deterministic_applies(workdirs, native_lib, name):
+    """Every partition (balanced segments, plain, order split) and both
+    operators give the same bits for repeated applies, and A x = S x + H x
+    with the parts computed apart (units cut into pieces combine their
+    partial sums in a fixed order)."""
+    d, params, info, T, dt = _setup(workdirs, name)
+    prob = Problem(d, info["lmax"])
+    sol = Solver(prob, dt)
+    rng = np.random.default_rng(11)
+    x = rng.standard_normal(prob.n) + 1j * rng.standard_normal(prob.n)
+    ft = pulse(params["Intensity"], params["Omega"], params["Cycles"], 0.4 * T)
+    for op, splits in ((0, (0, 1, 2)), (1, (1,))):
+        sol.set_operator(op)
+        for ns in splits:
+            if op == 0:
+                sol.set_split(ns)
+            sol.set_time(ft)
+            y = sol.apply(x)
+            _, sx, hx = sol.apply(x, parts=True)
+            y3 = sol.apply(x)
+            assert np.array_equal(y, y3), (op, ns)
+            assert _rel(y, sx + hx) < 1e-14, (op, ns)
+    sol.close()
