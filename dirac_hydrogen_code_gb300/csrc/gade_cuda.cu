@@ -1642,6 +1642,8 @@ struct gade_solver {
     PartList part_asm[3];       /* plain, balanced (one accumulator), balanced (S, H apart) */
     int occ_asm[2];
     float asm_ms[2];            /* timed FP64 apply: [0] plain, [1] balanced partition */
+    double asm_flops, asm_bytes;          /* one assembled apply: FP64 flops, compulsory DRAM bytes */
+    double asmb_flops, asmb_bytes;        /* one step's assembly */
     float mf_ms;                /* best timed matrix-free apply */
 };
 
@@ -2609,6 +2611,12 @@ static int asm_build(gade_solver *s)
         s->occ_asm[sep] = n > 8 ? 8 : n;
     }
     if ((rc = asm_partitions(s))) return rc;
+    /* costs: 2 FMAs per stored value of the pairs' nonzero slots plus the
+       diagonal blocks (complex, 4 FMAs); the values stream once per apply */
+    s->asm_flops = 2.0 * (2.0 * (double)s->npairs * s->blk_nnz + 4.0 * (double)s->nblk * s->blk_nnz);
+    s->asm_bytes = 8.0 * (double)per + 16.0 * (double)s->nk * WB + 4.0 * s->npairs + 48.0 * (double)s->n;
+    s->asmb_flops = 2.0 * 3.0 * (double)per;
+    s->asmb_bytes = 8.0 * 4.0 * (double)per;
     s->asm_ok = 1;
     return GADE_OK;
 }
@@ -3203,7 +3211,7 @@ extern "C" int gade_solver_split(const gade_solver *s, int32_t *nsplit, float *s
 extern "C" int gade_solver_flops(const gade_solver *s, double *apply_flops, double *precond_flops)
 {
     if (!s) return fail(GADE_ERR_ARG, "gade_solver_flops: NULL solver");
-    if (apply_flops) *apply_flops = s->apply_flops;
+    if (apply_flops) *apply_flops = s->use_asm ? s->asm_flops : s->apply_flops;
     if (precond_flops) *precond_flops = s->precond_flops;
     return GADE_OK;
 }
@@ -3211,7 +3219,15 @@ extern "C" int gade_solver_flops(const gade_solver *s, double *apply_flops, doub
 extern "C" int gade_solver_apply_bytes(const gade_solver *s, double *bytes)
 {
     if (!s || !bytes) return fail(GADE_ERR_ARG, "gade_solver_apply_bytes: NULL argument");
-    *bytes = s->apply_bytes;
+    *bytes = s->use_asm ? s->asm_bytes : s->apply_bytes;
+    return GADE_OK;
+}
+
+extern "C" int gade_solver_assembly_cost(const gade_solver *s, double *flops, double *bytes)
+{
+    if (!s) return fail(GADE_ERR_ARG, "gade_solver_assembly_cost: NULL solver");
+    if (flops) *flops = s->use_asm ? s->asmb_flops : 0.0;
+    if (bytes) *bytes = s->use_asm ? s->asmb_bytes : 0.0;
     return GADE_OK;
 }
 

@@ -87,6 +87,7 @@ _SIGS = {
     "gade_solver_set_split": (C.c_int, [C.c_void_p, C.c_int32]),
     "gade_solver_apply_bytes": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "gade_solver_set_operator": (C.c_int, [C.c_void_p, C.c_int32]),
+    "gade_solver_assembly_cost": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "gade_solver_operator": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.c_void_p]),
     "gade_solver_balanced": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                        C.POINTER(C.c_float), C.POINTER(C.c_double)]),
@@ -321,6 +322,12 @@ class Solver:
 
     def set_operator(self, assembled: int):
         _check(load_library().gade_solver_set_operator(self._h, int(assembled)))
+
+    def assembly_cost(self) -> tuple[float, float]:
+        """(FP64 flops, compulsory DRAM bytes) of one step's coupling assembly."""
+        f, b = C.c_double(), C.c_double()
+        _check(load_library().gade_solver_assembly_cost(self._h, C.byref(f), C.byref(b)))
+        return float(f.value), float(b.value)
 
     def apply_bytes(self) -> float:
         """Compulsory DRAM bytes of one FP64 BiCGSTAB operator apply."""

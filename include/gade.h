@@ -187,10 +187,17 @@ int gade_solver_operator(const gade_solver *s, int32_t *assembled, float *ms);
  * preconditioner solve, counted exactly from the set-up structure. */
 int gade_solver_flops(const gade_solver *s, double *apply_flops, double *precond_flops);
 /* Compulsory DRAM bytes of one FP64 BiCGSTAB operator apply (no reference
- * counterpart): the radial-table slabs of the distinct (order, kappa) pairs
- * the block rows use, the diagonal blocks, the angular terms and slot maps,
- * and the vectors read and written (x, r0 in; v out). */
+ * counterpart).  Matrix-free: the radial-table slabs of the distinct (order,
+ * kappa) pairs the block rows use, the diagonal blocks, the angular terms
+ * and slot maps, and the vectors read and written (x, r0 in; v out).
+ * Assembled: the stored coupling values, the diagonal blocks and the
+ * vectors. */
 int gade_solver_apply_bytes(const gade_solver *s, double *bytes);
+/* FP64 flops and compulsory DRAM bytes of one step's assembly of the
+ * coupling values (0 with the matrix-free operator); no reference
+ * counterpart.  gade_solver_flops and gade_solver_apply_bytes describe the
+ * operator in use. */
+int gade_solver_assembly_cost(const gade_solver *s, double *flops, double *bytes);
 
 /* y = (S + H(t)) x and dot = sum_i conj(r0_i) y_i (2 doubles, re and im), all
  * device pointers in HBM, with the tables of the last set_time/step; no
