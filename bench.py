@@ -217,6 +217,8 @@ def run_ours(args):
     prob = native.Problem(tmp.name, info["lmax"])
     dt, steps = step_times(T, params["Ntime"])
     sol = native.Solver(prob, dt, 1.0, precision="fp64", device=device)
+    if args.operator != "auto":
+        sol.set_operator(1 if args.operator == "assembled" else 0)
     ns, split_ms = sol.split()
     bal = sol.balanced()
     partition = {"chosen": "balanced" if ns == 0 else f"order split {ns}",
@@ -651,6 +653,9 @@ def main():
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-guess variant")
     ap.add_argument("--batch-steps", type=int, default=10, help="timed batch steps of the batch variant")
     ap.add_argument("--learned-steps", type=int, default=200, help="steps per pulse of the learned variant")
+    ap.add_argument("--operator", default="auto", choices=["auto", "assembled", "matrix-free"],
+                    help="operator of the headline solver (auto: chosen by timing at creation; a profiler "
+                         "run that distorts that timing names it)")
     ap.add_argument("--profile-precision", default=None, choices=["fp64", "mixed"],
                     help="only run this precision's steps (for profiler captures)")
     if len(sys.argv) > 1 and sys.argv[1] == "--cpu-worker":
