@@ -214,7 +214,7 @@ struct OpP {
     /* assembled operator (k_apply_asm): this step's coupling values
        A[pair][W][B] and the coupled block of every (block row, block) pair;
        a piece's order range is then a pair range */
-    const double *A;
+    const void *A;                 /* double, or float for the complex64 instance */
     const int *pair_c;
 };
 
@@ -934,9 +934,10 @@ __global__ void k_build_K(double *__restrict__ K, const R4<double>::T *__restric
    imaginary part of the step's coefficient of order parity par(pair) and
    factor ia (coef[lpar * 3 + ia], lpar the first order of that parity).
    grid (element blocks of a pair, pairs); two values per thread */
-__global__ void k_assemble(double2 *__restrict__ A, const double2 *__restrict__ K, int WB2,
+__global__ void k_assemble(double2 *__restrict__ A, float2 *__restrict__ A32, const double2 *__restrict__ K, int WB2,
                            const int *__restrict__ pair_par, const double2 *__restrict__ coef, int2 lpar)
 {
+    /* A32 (NULL: none): the values rounded to float, for mixed precision */
     const int p = blockIdx.y;
     const int par = pair_par[p];
     const int cb = 3 * (par ? lpar.y : lpar.x);
@@ -949,6 +950,7 @@ __global__ void k_assemble(double2 *__restrict__ A, const double2 *__restrict__ 
         v.x = fma(w2, k2.x, fma(w1, k1.x, w0 * k0.x));
         v.y = fma(w2, k2.y, fma(w1, k1.y, w0 * k0.y));
         Ap[e] = v;
+        if (A32) A32[(size_t)p * WB2 + e] = make_float2((float)v.x, (float)v.y);
     }
 }
 
@@ -956,11 +958,11 @@ __global__ void k_assemble(double2 *__restrict__ A, const double2 *__restrict__ 
 
 /* shared memory of k_apply_asm: x slices (x_r, x_n, delta), the staged
    windows of ASM_GB coupled blocks, the slot map, the reduction buffer */
-__host__ __device__ __forceinline__ unsigned asm_smem(int CS, int W, int RM, int nt, unsigned *o_xw, unsigned *o_lcs,
-                                                      unsigned *o_red)
+__host__ __device__ __forceinline__ unsigned asm_smem(int CS, int W, int RM, int nt, unsigned elem, unsigned *o_xw,
+                                                      unsigned *o_lcs, unsigned *o_red)
 {
-    unsigned o = up32(3u * 16u * CS);
-    *o_xw = o;  o = up32(o + 16u * ASM_GB * CS);
+    unsigned o = up32(3u * elem * CS);
+    *o_xw = o;  o = up32(o + elem * ASM_GB * CS);
     *o_lcs = o; o = up32(o + 4u * W * RM);
     *o_red = o; o = up32(o + 8u * NRED * nt);
     return o;
@@ -974,16 +976,18 @@ __host__ __device__ __forceinline__ unsigned asm_smem(int CS, int W, int RM, int
  * the CTA stages the blocks' x windows in shared memory, then every thread
  * streams its rows' values and adds value x window[column].
  */
-template <bool SEP>
+template <typename R, bool SEP>
 __global__ void __launch_bounds__(256, 3)
-    k_apply_asm(OpP P, const double2 *__restrict__ x, int mode, VecP V, RedP red)
+    k_apply_asm(OpP P, const typename Cx<R>::T *__restrict__ x, int mode, VecP V, RedP red)
 {
+    /* R: double (FP64 values and vectors) or float (the complex64 inner solve
+       of mixed precision, with the step's values rounded to float) */
     constexpr int HJ = 15;
-    typedef double2 C;
+    typedef typename Cx<R>::T C;
     extern __shared__ __align__(32) unsigned char smem_raw[];
     const int CS = (P.CM + 2) & ~1;
     unsigned oxw, olcs, ored;
-    asm_smem(CS, P.W, P.RM, blockDim.x, &oxw, &olcs, &ored);
+    asm_smem(CS, P.W, P.RM, blockDim.x, sizeof(C), &oxw, &olcs, &ored);
     C *xr = (C *)smem_raw, *xs = xr + CS, *ds = xs + CS;
     C *xw = (C *)(smem_raw + oxw);
     int *lcs = (int *)(smem_raw + olcs);
@@ -995,7 +999,7 @@ __global__ void __launch_bounds__(256, 3)
     const int tid = threadIdx.x, nt = blockDim.x;
     const int B = P.B, W = P.W, CM = P.CM;
     if (tid == 0) {
-        const C z = make_double2(0, 0);
+        const C z = mk<C>(0, 0);
         xr[CM] = z; xs[CM] = z; ds[CM] = z;
         for (int g = 0; g < ASM_GB; g++) xw[g * CS + CM] = z;
     }
@@ -1033,7 +1037,7 @@ __global__ void __launch_bounds__(256, 3)
     }
 #define LCO(t) ((int)(((t) & 1) ? (lcp[(t) >> 1] >> 16) : (lcp[(t) >> 1] & 0xffffu)))
     const int jB = jb * B;
-    C accS = make_double2(0, 0), accH = accS, accD = accS;
+    C accS = mk<C>(0, 0), accH = accS, accD = accS;
     if (i >= 0 && (pd.w & 0xffff) == 0) {     /* diagonal blocks: the unit's first piece */
         if (SEP && mode == AX_MIX) {
             const C *Se = (const C *)P.S_ell + (size_t)kk * W * B + i + jB;
@@ -1077,7 +1081,7 @@ __global__ void __launch_bounds__(256, 3)
         __syncthreads();
         if (i >= 0) {
             for (int g = 0; g < ng; g++) {
-                const double *Av = P.A + (size_t)(pg + g) * WB + i + jB;
+                const R *Av = (const R *)P.A + (size_t)(pg + g) * WB + i + jB;
                 const C *xg = xw + g * CS;
 #pragma unroll
                 for (int t = 0; t < HJ; t++) {
@@ -1128,7 +1132,7 @@ __global__ void __launch_bounds__(256, 3)
         if (!piece_last) continue;
         __threadfence();
         if (half == 0 && i >= 0) {
-            accS = make_double2(0, 0); accH = accS; accD = accS;
+            accS = mk<C>(0, 0); accH = accS; accD = accS;
             for (int k = 0; k < np; k++) {
                 const size_t pk = (size_t)(pcc - pi + k) * RM3;
                 accH = cadd(accH, __ldcg(&acc[pk + P.RM + trow]));
@@ -1639,8 +1643,10 @@ struct gade_solver {
     int *d_pair_par;            /* [pairs] parity of the orders coupling the pair */
     int lpar[2];                /* first order of each parity (-1: none) */
     std::vector<int> h_pair_ptr, h_pair_r, h_pair_par, h_le_ptr, h_le_l, h_le_e;   /* pairs per block row; (order, term) per pair */
-    PartList part_asm[3];       /* plain, balanced (one accumulator), balanced (S, H apart) */
-    int occ_asm[2];
+    void *d_A32;                /* mixed precision: the values rounded to float */
+    PartList part_asm[1];       /* plain: one piece per unit */
+    PartList part_asm_bal[9];   /* balanced, by resident CTAs per SM */
+    int occ_asm[2][2];          /* resident CTAs per SM [complex64][sep] */
     float asm_ms[2];            /* timed FP64 apply: [0] plain, [1] balanced partition */
     double asm_flops, asm_bytes;          /* one assembled apply: FP64 flops, compulsory DRAM bytes */
     double asmb_flops, asmb_bytes;        /* one step's assembly */
@@ -2203,7 +2209,7 @@ static int solver_create(const gade_problem *p, int npulse, const double *dts, c
     }
     /* block solves: per lane and chunk, bw band terms + 32 inverse terms, 2 sweeps */
     s->precond_flops = 2.0 * 4.0 * (double)s->nblk * 32.0 * s->nch * 2.0 * (s->bwp + 32);
-    if (npulse == 1 && s->rc && precision == GADE_PREC_FP64) {
+    if (npulse == 1 && s->rc) {
         /* (block row, coupled block) pairs and the (order, angular term) list
            of every pair, for the assembled operator */
         s->h_pair_ptr.assign(1, 0);
@@ -2502,8 +2508,11 @@ static int asm_partitions(gade_solver *s)
     }
     auto pcost = [&](int q) { return 2.0 * s->h_chunk_nrows[q] * s->W + 2.0 * s->h_chunk_ncols[q]; };
     auto ufix = [&](int q) { return 4.0 * s->h_chunk_nrows[q] * s->W; };
-    for (int cls = 0; cls < 2; cls++) {
-        const int nseg = s->occ_asm[cls] * s->nsm;
+    for (int cls = 0; cls < 4; cls++) {
+        const int f = cls / 2, o = s->occ_asm[f][cls % 2];
+        if (f == 1 && s->prec != GADE_PREC_MIXED) continue;
+        if (s->part_asm_bal[o].nseg) continue;
+        const int nseg = o * s->nsm;
         double total = 0;
         for (int u = 0; u < nunit; u++) {
             const int r = u / s->nchunk, q = u - r * s->nchunk;
@@ -2537,15 +2546,15 @@ static int asm_partitions(gade_solver *s)
         std::vector<int> seg((size_t)nseg + 1, 0);
         for (int sg : pseg) seg[sg + 1]++;
         for (int k = 0; k < nseg; k++) seg[k + 1] += seg[k];
-        if ((rc = part_upload(s, s->part_asm[1 + cls], seg, pcs))) return rc;
+        if ((rc = part_upload(s, s->part_asm_bal[o], seg, pcs))) return rc;
     }
     return GADE_OK;
 }
 
-static size_t asm_smem_bytes(const gade_solver *s)
+static size_t asm_smem_bytes(const gade_solver *s, size_t elem)
 {
     unsigned a, b, c;
-    return asm_smem((s->CM + 2) & ~1, s->W, s->RM, 256, &a, &b, &c);
+    return asm_smem((s->CM + 2) & ~1, s->W, s->RM, 256, (unsigned)elem, &a, &b, &c);
 }
 
 /* Builds K_a for every pulse factor a that some Bessel order uses: the
@@ -2554,7 +2563,7 @@ static size_t asm_smem_bytes(const gade_solver *s)
    free device memory. */
 static int asm_build(gade_solver *s)
 {
-    if (s->npulse != 1 || !s->rc || s->prec != GADE_PREC_FP64 || s->npairs == 0 || s->asm_ok) return GADE_OK;
+    if (s->npulse != 1 || !s->rc || s->npairs == 0 || s->asm_ok) return GADE_OK;
     for (int par : s->h_pair_par)
         if (par < 0) return GADE_OK;             /* a pair coupled by both parities: stay matrix-free */
     const size_t WB = (size_t)s->W * s->B, per = (size_t)s->npairs * WB;
@@ -2563,10 +2572,16 @@ static int asm_build(gade_solver *s)
     s->lpar[1] = s->lmax > 1 ? 1 : -1;
     size_t fr = 0, tot = 0;
     CK(cudaMemGetInfo(&fr, &tot));
-    if (sizeof(double) * per * 4 > fr / 2) return GADE_OK;
+    const bool mixed = s->prec == GADE_PREC_MIXED;
+    if (sizeof(double) * per * (mixed ? 4.5 : 4.0) > fr / 2) return GADE_OK;
     int rc;
     if ((rc = dev_upload(s, &s->d_K, (const double *)nullptr, per * 3))) return rc;
     if ((rc = dev_upload(s, &s->d_A, (const double *)nullptr, per))) return rc;
+    if (mixed) {
+        float *a32 = nullptr;
+        if ((rc = dev_upload(s, &a32, (const float *)nullptr, per))) return rc;
+        s->d_A32 = a32;
+    }
     if ((rc = dev_upload(s, &s->d_pair_par, s->h_pair_par.data(), s->h_pair_par.size()))) return rc;
     int *d_pr = nullptr, *d_lp = nullptr, *d_ll = nullptr, *d_le = nullptr;
     if ((rc = dev_upload(s, &d_pr, s->h_pair_r.data(), s->h_pair_r.size()))) return rc;
@@ -2603,13 +2618,18 @@ static int asm_build(gade_solver *s)
     s->has_time = 0;             /* the tables held a unit factor */
     dev_release(s, d_pr); dev_release(s, d_lp); dev_release(s, d_ll); dev_release(s, d_le);
     if (rc) return rc;
-    for (int sep = 0; sep < 2; sep++) {
-        int n = 0;
-        cudaError_t e = sep ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_apply_asm<true>, 256, asm_smem_bytes(s))
-                            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_apply_asm<false>, 256, asm_smem_bytes(s));
-        if (e != cudaSuccess || n < 1) { cudaGetLastError(); n = 1; }
-        s->occ_asm[sep] = n > 8 ? 8 : n;
-    }
+    for (int f = 0; f < 2; f++)
+        for (int sep = 0; sep < 2; sep++) {
+            int n = 0;
+            const size_t sm = asm_smem_bytes(s, f ? sizeof(float2) : sizeof(double2));
+            cudaError_t e;
+            if (f) e = sep ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_apply_asm<float, true>, 256, sm)
+                           : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_apply_asm<float, false>, 256, sm);
+            else e = sep ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_apply_asm<double, true>, 256, sm)
+                         : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_apply_asm<double, false>, 256, sm);
+            if (e != cudaSuccess || n < 1) { cudaGetLastError(); n = 1; }
+            s->occ_asm[f][sep] = n > 8 ? 8 : n;
+        }
     if ((rc = asm_partitions(s))) return rc;
     /* costs: 2 FMAs per stored value of the pairs' nonzero slots plus the
        diagonal blocks (complex, 4 FMAs); the values stream once per apply */
@@ -2627,7 +2647,8 @@ static int launch_assemble(gade_solver *s, cudaStream_t st)
     const int WB2 = s->W * s->B / 2;
     prof_begin(s, st);
     k_assemble<<<dim3((unsigned)((WB2 + 255) / 256), (unsigned)s->npairs), 256, 0, st>>>(
-        (double2 *)s->d_A, (const double2 *)s->d_K, WB2, s->d_pair_par, s->d_coef, make_int2(s->lpar[0], s->lpar[1]));
+        (double2 *)s->d_A, (float2 *)s->d_A32, (const double2 *)s->d_K, WB2, s->d_pair_par, s->d_coef,
+        make_int2(s->lpar[0], s->lpar[1]));
     prof_end(s, st, 2);
     CKL();
     s->has_time = 1;
@@ -2640,21 +2661,26 @@ static int launch_step_tables(gade_solver *s, cudaStream_t st)
     return s->use_asm ? launch_assemble(s, st) : launch_table_kernels(s, 1, st);
 }
 
-static int launch_apply_asm(gade_solver *s, const double2 *x, int mode, VecP V, RedP red, cudaStream_t st)
+static OpP op_params32(const gade_solver *s);
+
+/* the assembled operator in FP64 (x double2) or complex64 (x float2) */
+template <typename R>
+static int launch_apply_asm(gade_solver *s, const typename Cx<R>::T *x, int mode, VecP V, RedP red, cudaStream_t st)
 {
-    OpP P = op_params(s);
-    P.A = s->d_A;
+    const bool f32 = sizeof(R) == 4;
+    OpP P = f32 ? op_params32(s) : op_params(s);
+    P.A = f32 ? (const void *)s->d_A32 : (const void *)s->d_A;
     P.pair_c = s->d_pair_c;
     const bool sep = mode == AX_RHS || mode == AX_PARTS || mode == AX_MIX;
-    const PartList &pl = s->asm_part ? s->part_asm[1 + (sep ? 1 : 0)] : s->part_asm[0];
+    const PartList &pl = s->asm_part ? s->part_asm_bal[s->occ_asm[f32][sep]] : s->part_asm[0];
     P.seg_ptr = pl.d_seg_ptr;
     P.pieces = pl.d_pieces;
     dim3 grid(s->nslot, pl.nseg);
-    const size_t smem = asm_smem_bytes(s);
+    const size_t smem = asm_smem_bytes(s, sizeof(typename Cx<R>::T));
     prof_begin(s, st);
-    if (sep) k_apply_asm<true><<<grid, 256, smem, st>>>(P, x, mode, V, red);
-    else k_apply_asm<false><<<grid, 256, smem, st>>>(P, x, mode, V, red);
-    prof_end(s, st, 0);
+    if (sep) k_apply_asm<R, true><<<grid, 256, smem, st>>>(P, x, mode, V, red);
+    else k_apply_asm<R, false><<<grid, 256, smem, st>>>(P, x, mode, V, red);
+    prof_end(s, st, f32 ? 0 : 0);
     CKL();
     return GADE_OK;
 }
@@ -2662,7 +2688,7 @@ static int launch_apply_asm(gade_solver *s, const double2 *x, int mode, VecP V, 
 static int launch_apply(gade_solver *s, const double2 *x, int mode, VecP V, int redkind, cudaStream_t st,
                         int pred = PRED_NONE, DevScal *pb = nullptr)
 {
-    if (s->use_asm) return launch_apply_asm(s, x, mode, V, make_red(s, s->d_sc, redkind, pred, nullptr, pb), st);
+    if (s->use_asm) return launch_apply_asm<double>(s, x, mode, V, make_red(s, s->d_sc, redkind, pred, nullptr, pb), st);
     OpP P = op_params(s);
     RedP red = make_red(s, s->d_sc, redkind, pred, nullptr, pb);
     dim3 grid(s->nslot, op_partition(s, P, false, mode));
@@ -2750,11 +2776,7 @@ static int launch_tables(gade_solver *s, const double *ft, int which = 1)
     int rc = fill_coef(s, 0, ft);
     if (rc) return rc;
     CK(cudaMemcpyAsync(s->d_coef, s->h_coef, sizeof(double2) * (size_t)s->lmax * 3, cudaMemcpyHostToDevice, s->stream));
-    if (s->use_asm && (which & 1)) {
-        if ((rc = launch_assemble(s, s->stream))) return rc;
-        which &= ~1;
-        if (!which) return GADE_OK;
-    }
+    if (s->use_asm && which) return launch_assemble(s, s->stream);   /* FP64 values and their float copy */
     return launch_table_kernels(s, which, s->stream);
 }
 
@@ -2862,6 +2884,7 @@ static OpP op_params32(const gade_solver *s)
 static int launch_apply32(gade_solver *s, const float2 *x, int mode, VecP V, int redkind, DevScal *sc,
                           int pred = PRED_NONE)
 {
+    if (s->use_asm) return launch_apply_asm<float>(s, x, mode, V, make_red(s, sc, redkind, pred), s->stream);
     OpP P = op_params32(s);
     RedP red = make_red(s, sc, redkind, pred);
     dim3 grid(s->nslot, op_partition(s, P, true, mode));
@@ -2963,7 +2986,8 @@ static int choose_split(gade_solver *s)
     return GADE_OK;
 }
 
-/* ms per FP64 apply (R0V) of the current operator and partition */
+/* ms per FP64 apply (R0V) of the current operator and partition, plus two
+   complex64 applies in mixed precision (as choose_split times them) */
 static int time_fp64_apply(gade_solver *s, float *ms)
 {
     cudaEvent_t e0, e1;
@@ -2974,6 +2998,10 @@ static int time_fp64_apply(gade_solver *s, float *ms)
         if (rep == 1 && cudaEventRecord(e0, s->stream) != cudaSuccess) rc = fail(GADE_ERR_CUDA, "event record failed");
         VecP V = {}; V.out0 = s->tmp1; V.in0 = s->r0;
         if (!rc) rc = launch_apply(s, s->x, AX_R0V, V, RED_R0V, s->stream);
+        for (int k = 0; !rc && s->prec == GADE_PREC_MIXED && k < 2; k++) {
+            VecP V32 = {}; V32.out0 = s->v32; V32.in0 = s->r032;
+            rc = launch_apply32(s, s->y32, AX_R0V, V32, RED_R0V, s->d_sc, PRED_NONE);
+        }
     }
     float t = 0;
     if (!rc && (cudaEventRecord(e1, s->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
@@ -2986,7 +3014,7 @@ static int time_fp64_apply(gade_solver *s, float *ms)
 }
 
 /*
- * Matrix-free or assembled operator for one FP64 pulse with real couplings:
+ * Matrix-free or assembled operator for one pulse with real couplings:
  * the assembled values (K_a) are built, both of their partitions timed, and
  * the assembled operator is kept when its apply is clearly faster than the
  * matrix-free one chosen by choose_split (its per-step assembly replaces the
@@ -3021,8 +3049,9 @@ extern "C" int gade_solver_set_operator(gade_solver *s, int32_t assembled)
     if (assembled && !s->asm_ok) {
         if ((rc = asm_build(s))) return rc;
         if (!s->asm_ok)
-            return fail(GADE_ERR_ARG, "gade_solver_set_operator: the assembled operator needs one FP64 pulse with "
-                                      "real couplings and device memory for its values");
+            return fail(GADE_ERR_ARG, "gade_solver_set_operator: the assembled operator needs one pulse with real "
+                                      "couplings, each pair coupled by orders of one parity, and device memory for "
+                                      "its values");
         s->asm_part = 1;
     }
     if (s->engine) batch_drop_graphs(s->engine);
@@ -3290,7 +3319,7 @@ extern "C" int gade_solver_apply_dot_noalloc(gade_solver *s, const void *x_dev, 
         P.pair_c = s->d_pair_c;
         P.seg_ptr = s->part_asm[0].d_seg_ptr;
         P.pieces = s->part_asm[0].d_pieces;
-        k_apply_asm<false><<<dim3(1, s->part_asm[0].nseg), 256, asm_smem_bytes(s), st>>>(
+        k_apply_asm<double, false><<<dim3(1, s->part_asm[0].nseg), 256, asm_smem_bytes(s, sizeof(double2)), st>>>(
             P, (const double2 *)x_dev, AX_R0V, V, red);
         CKL();
         return GADE_OK;
@@ -3412,7 +3441,7 @@ static int batch_seq_first(gade_batch *b, cudaStream_t st)
     gade_solver *s = b->s;
     int rc;
     if (s->prec == GADE_PREC_MIXED) {
-        if ((rc = launch_table_kernels(s, 3, st))) return rc;
+        if ((rc = s->use_asm ? launch_assemble(s, st) : launch_table_kernels(s, 3, st))) return rc;
         const BPred all = {s->d_plist, s->d_sc, s->d_sc2, PRED_NONE};
         k_mixed_prep<<<dim3(s->upd_grid, s->nslot), s->upd_block, 0, st>>>(
             s->n, s->x, s->xprev, s->d_hprev, s->delta64, s->d32, s->tmp0, all, b->use_guess ? b->d_corr : nullptr);

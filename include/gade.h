@@ -168,14 +168,15 @@ int gade_solver_set_split(gade_solver *s, int32_t nsplit);
 int gade_solver_balanced(const gade_solver *s, int32_t *segments, int32_t *pieces, float *ms,
                          double *gather_weight);
 
-/* Operator of a single FP64 pulse with real couplings (no reference
- * counterpart): matrix-free (0) or assembled (1).  The couplings of H(t) are
+/* Operator of a single pulse with real couplings, FP64 or mixed precision
+ * (no reference counterpart): matrix-free (0) or assembled (1).  The couplings of H(t) are
  * linear in the six pulse factors, so the solver can store the coupling
  * values of each unit factor once (K_a, built from the radial tables) and
  * form this step's values as sum_a w_a(t) K_a; an apply then streams the
- * values (2 FMAs each).  gade_solver_create times both and keeps the faster
- * (the assembled one needs 7 x 8 bytes per stored coupling value of device
- * memory).  gade_solver_operator reports the choice and, in ms (3 floats,
+ * values (2 FMAs each); in mixed precision the complex64 inner solve
+ * streams the values rounded to float.  gade_solver_create times both and
+ * keeps the faster (the assembled one needs 32 bytes of device memory per
+ * stored coupling value, 36 in mixed precision).  gade_solver_operator reports the choice and, in ms (3 floats,
  * may be NULL), the timed matrix-free apply and the assembled one with the
  * plain and the balanced partition (0 where not timed).  After
  * gade_solver_set_operator the next gade_solver_set_time or step fills the

@@ -293,26 +293,33 @@ def test_balanced_partition_mixed_precision(workdirs, native_lib):
     assert _rel(out[1], out[0]) < 1e-8
 
 
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
 @pytest.mark.parametrize("name", ["tiny_dipole", "tiny_nondipole"])
-def test_assembled_operator_steps_match_matrix_free(workdirs, native_lib, name):
+def test_assembled_operator_steps_match_matrix_free(workdirs, native_lib, name, prec):
     """CN steps with the assembled couplings (sum of unit-factor values
-    weighted by the step's pulse factors) match the matrix-free ones: same
-    iterations, states within summation-order differences."""
+    weighted by the step's pulse factors) match the matrix-free ones: FP64
+    with the same iterations and states within summation-order differences;
+    mixed precision (complex64 inner solves on the values rounded to float)
+    within its tolerance."""
     d, params, info, T, dt = _setup(workdirs, name)
     prob = Problem(d, info["lmax"])
     psi, _ = prob.psi0()
     fts = [pulse(params["Intensity"], params["Omega"], params["Cycles"], t)
            for _, t in step_times(T, params["Ntime"])[1][:8]]
+    tol = 1e-12 if prec == "fp64" else 1e-10
     out = []
     for op in (0, 1):
-        sol = Solver(prob, dt)
+        sol = Solver(prob, dt, precision=prec)
         sol.set_operator(op)
         sol.set_x(psi)
-        its = [sol.step(ft, maxit=500, tol=1e-12)["iters"] for ft in fts]
+        its = [sol.step(ft, maxit=500, tol=tol)["iters"] for ft in fts]
         out.append((sol.get_x(), its))
         sol.close()
-    assert out[1][1] == out[0][1]
-    assert _rel(out[1][0], out[0][0]) < 1e-12
+    if prec == "fp64":
+        assert out[1][1] == out[0][1]
+        assert _rel(out[1][0], out[0][0]) < 1e-12
+    else:
+        assert _rel(out[1][0], out[0][0]) < 1e-8
 
 
 @pytest.mark.parametrize("name", ["tiny_nondipole", "dipole_small"])
