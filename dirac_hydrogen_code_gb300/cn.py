@@ -88,7 +88,8 @@ def run(workdir: str, maxtime: float, lmax: int, E0: float, omega: float, cycles
 
 
 def run_batch(problem: Problem, pulses: list[dict], tables: np.ndarray | None = None, tol: float = 1e-16,
-              maxit: int = 500, device: int = 0, max_steps: int | None = None, callback=None, **batch_kw):
+              maxit: int = 500, device: int = 0, max_steps: int | None = None, callback=None,
+              operator: int | None = None, **batch_kw):
     """The reference time loop for many pulses at once on one GPU.
 
     ``pulses``: dicts with E0, omega, cycles, ntime and optionally maxtime
@@ -97,8 +98,10 @@ def run_batch(problem: Problem, pulses: list[dict], tables: np.ndarray | None = 
     [npulse, 6, lmax, 4, blk_nnz] (``gen.pulse_tables``) or None when every
     pulse has the Omega and Cycles the problem files were made with.  Each
     pulse keeps its own float-accumulated time grid (Ntime or Ntime+1 steps);
-    a pulse whose grid has ended leaves the batch.  Returns (xs, records,
-    batch): final states (permuted order) and per-pulse step records."""
+    a pulse whose grid has ended leaves the batch.  ``operator``: force the
+    matrix-free (0) or assembled (1) operator instead of the timed choice.
+    Returns (xs, records, batch): final states (permuted order) and per-pulse
+    step records."""
     from .native import Batch
     grids = []
     for p in pulses:
@@ -106,6 +109,8 @@ def run_batch(problem: Problem, pulses: list[dict], tables: np.ndarray | None = 
         grids.append(step_times(maxtime, p["ntime"]))
     dts = [g[0] for g in grids]
     batch = Batch(problem, dts, tables, device=device, **batch_kw)
+    if operator is not None:
+        batch.set_operator(operator)
     nsteps = [len(g[1]) for g in grids]
     total = max(nsteps)
     if max_steps is not None:

@@ -216,6 +216,7 @@ struct OpP {
        a piece's order range is then a pair range */
     const void *A;                 /* double, or float for the complex64 instance */
     const int *pair_c;
+    size_t astride;                /* values per pulse of A */
 };
 
 struct VecP {
@@ -935,9 +936,17 @@ __global__ void k_build_K(double *__restrict__ K, const R4<double>::T *__restric
    factor ia (coef[lpar * 3 + ia], lpar the first order of that parity).
    grid (element blocks of a pair, pairs); two values per thread */
 __global__ void k_assemble(double2 *__restrict__ A, float2 *__restrict__ A32, const double2 *__restrict__ K, int WB2,
-                           const int *__restrict__ pair_par, const double2 *__restrict__ coef, int2 lpar)
+                           const int *__restrict__ pair_par, const double2 *__restrict__ coef, int2 lpar,
+                           const int *__restrict__ plist, size_t astride2, size_t kstride2, int lmax)
 {
-    /* A32 (NULL: none): the values rounded to float, for mixed precision */
+    /* A32 (NULL: none): the values rounded to float, for mixed precision.
+       grid z: pulse slot (plist: slot -> pulse); A per pulse, K per pulse
+       (kstride2 0: shared by pulses with the same radial tables) */
+    const int pulse = plist ? plist[blockIdx.z] : 0;
+    A += (size_t)pulse * astride2;
+    if (A32) A32 += (size_t)pulse * astride2;
+    K += (size_t)pulse * kstride2;
+    coef += (size_t)pulse * lmax * 3;
     const int p = blockIdx.y;
     const int par = pair_par[p];
     const int cb = 3 * (par ? lpar.y : lpar.x);
@@ -1081,7 +1090,7 @@ __global__ void __launch_bounds__(256, 3)
         __syncthreads();
         if (i >= 0) {
             for (int g = 0; g < ng; g++) {
-                const R *Av = (const R *)P.A + (size_t)(pg + g) * WB + i + jB;
+                const R *Av = (const R *)P.A + (size_t)pulse * P.astride + (size_t)(pg + g) * WB + i + jB;
                 const C *xg = xw + g * CS;
 #pragma unroll
                 for (int t = 0; t < HJ; t++) {
@@ -1633,13 +1642,15 @@ struct gade_solver {
     int bal_waves;              /* balanced segments per resident CTA slot (timed at creation) */
     gade_batch *engine;         /* step engine of a single-pulse solver (device control, graphs) */
     int zskip;                  /* the DKB zero blocks hold for every pulse's tables */
+    int g_ext;                  /* the pulses have their own radial tables */
     /* assembled operator (one FP64 pulse, real couplings): A(t) = sum_a w_a(t) K_a */
     int asm_ok;                 /* K_a built */
     int use_asm;                /* applies and steps use it */
     int asm_part;               /* its partition: 0 plain, 1 balanced */
     int npairs;                 /* (block row, coupled block) pairs */
     int *d_pair_c;
-    double *d_K, *d_A;          /* [pairs][3][W][B], [pairs][W][B] */
+    double *d_K, *d_A;          /* [table set][pairs][3][W][B], [pulse][pairs][W][B] */
+    size_t asm_kstride;         /* doubles per pulse of K (0: one set shared by all pulses) */
     int *d_pair_par;            /* [pairs] parity of the orders coupling the pair */
     int lpar[2];                /* first order of each parity (-1: none) */
     std::vector<int> h_pair_ptr, h_pair_r, h_pair_par, h_le_ptr, h_le_l, h_le_e;   /* pairs per block row; (order, term) per pair */
@@ -1651,6 +1662,7 @@ struct gade_solver {
     double asm_flops, asm_bytes;          /* one assembled apply: FP64 flops, compulsory DRAM bytes */
     double asmb_flops, asmb_bytes;        /* one step's assembly */
     float mf_ms;                /* best timed matrix-free apply */
+    float tab_ms[2];            /* timed step tables: matrix-free radial tables, assembly */
 };
 
 static int solver_engine_step(gade_solver *s, const double *ft, int32_t maxit, double tol, gade_step_stats *stats);
@@ -1982,6 +1994,7 @@ static int solver_create(const gade_problem *p, int npulse, const double *dts, c
     s->bw = su->bw; s->Bp = su->Bp; s->nch = su->nch;
     s->dt = dts[0]; s->h = h; s->blk_nnz = p->blk_nnz;
     s->zskip = su->ell_halves && p->dkb_zero;
+    s->g_ext = gext != nullptr;
     if (s->zskip && gext) {
         const size_t per = (size_t)6 * p->lmax * 4 * bn;
         for (int k = 0; k < npulse && s->zskip; k++)
@@ -2209,7 +2222,7 @@ static int solver_create(const gade_problem *p, int npulse, const double *dts, c
     }
     /* block solves: per lane and chunk, bw band terms + 32 inverse terms, 2 sweeps */
     s->precond_flops = 2.0 * 4.0 * (double)s->nblk * 32.0 * s->nch * 2.0 * (s->bwp + 32);
-    if (npulse == 1 && s->rc) {
+    if (s->rc) {
         /* (block row, coupled block) pairs and the (order, angular term) list
            of every pair, for the assembled operator */
         s->h_pair_ptr.assign(1, 0);
@@ -2563,25 +2576,29 @@ static size_t asm_smem_bytes(const gade_solver *s, size_t elem)
    free device memory. */
 static int asm_build(gade_solver *s)
 {
-    if (s->npulse != 1 || !s->rc || s->npairs == 0 || s->asm_ok) return GADE_OK;
+    if (!s->rc || s->npairs == 0 || s->asm_ok) return GADE_OK;
     for (int par : s->h_pair_par)
         if (par < 0) return GADE_OK;             /* a pair coupled by both parities: stay matrix-free */
     const size_t WB = (size_t)s->W * s->B, per = (size_t)s->npairs * WB;
     if (WB % 2) return GADE_OK;
     s->lpar[0] = s->lmax > 0 ? 0 : -1;
     s->lpar[1] = s->lmax > 1 ? 1 : -1;
+    /* K depends only on the radial tables: one set unless the pulses have their own */
+    const int nset = s->g_ext ? s->npulse : 1;
     size_t fr = 0, tot = 0;
     CK(cudaMemGetInfo(&fr, &tot));
     const bool mixed = s->prec == GADE_PREC_MIXED;
-    if (sizeof(double) * per * (mixed ? 4.5 : 4.0) > fr / 2) return GADE_OK;
+    const double need = (double)per * (24.0 * nset + (mixed ? 12.0 : 8.0) * s->npulse);
+    if (need > 0.5 * (double)fr) return GADE_OK;
     int rc;
-    if ((rc = dev_upload(s, &s->d_K, (const double *)nullptr, per * 3))) return rc;
-    if ((rc = dev_upload(s, &s->d_A, (const double *)nullptr, per))) return rc;
+    if ((rc = dev_upload(s, &s->d_K, (const double *)nullptr, per * 3 * nset))) return rc;
+    if ((rc = dev_upload(s, &s->d_A, (const double *)nullptr, per * s->npulse))) return rc;
     if (mixed) {
         float *a32 = nullptr;
-        if ((rc = dev_upload(s, &a32, (const float *)nullptr, per))) return rc;
+        if ((rc = dev_upload(s, &a32, (const float *)nullptr, per * s->npulse))) return rc;
         s->d_A32 = a32;
     }
+    s->asm_kstride = s->g_ext ? 3 * per : 0;
     if ((rc = dev_upload(s, &s->d_pair_par, s->h_pair_par.data(), s->h_pair_par.size()))) return rc;
     int *d_pr = nullptr, *d_lp = nullptr, *d_ll = nullptr, *d_le = nullptr;
     if ((rc = dev_upload(s, &d_pr, s->h_pair_r.data(), s->h_pair_r.size()))) return rc;
@@ -2590,6 +2607,7 @@ static int asm_build(gade_solver *s)
     if ((rc = dev_upload(s, &d_le, s->h_le_e.data(), s->h_le_e.size()))) return rc;
     const int prof = s->profile;
     s->profile = 0;
+    for (int ks = 0; ks < nset && !rc; ks++)
     for (int a = 0; a < 6 && !rc; a++) {
         int l0 = -1;
         for (int l = 0; l < s->lmax && l0 < 0; l++)
@@ -2605,10 +2623,22 @@ static int asm_build(gade_solver *s)
                 s->h_coef[l * 3 + j] = make_double2(0.0, ((l % 2 + 1) % 2 == a % 2 && j == ia) ? 1.0 : 0.0);
         if (cudaMemcpyAsync(s->d_coef, s->h_coef, sizeof(double2) * s->lmax * 3, cudaMemcpyHostToDevice,
                             s->stream) != cudaSuccess) { rc = fail(GADE_ERR_CUDA, "assembled operator: coefficient upload failed"); break; }
-        if ((rc = launch_table_kernels(s, 1, s->stream))) break;
+        {
+            /* the unit factor's tables from table set ks (the radial tables of pulse ks) */
+            TabP T;
+            T.lmax = s->lmax; T.nk = s->nk; T.W = s->W; T.B = s->B; T.kvals = s->d_kvals;
+            T.g = (const double *)s->d_g + (size_t)ks * s->gstride;
+            T.gt = (const double *)s->d_gt + (size_t)ks * s->gstride;
+            T.M = (R4<double>::T *)s->d_M + (size_t)ks * s->mstride;
+            T.M32 = nullptr; T.plist = nullptr; T.gstride = s->gstride; T.mstride = s->mstride;
+            const int per_l = s->W * s->B;
+            k_tables<true, 1><<<dim3((unsigned)((per_l + 255) / 256), s->lmax, 1), 256, 0, s->stream>>>(T, s->d_coef);
+            if (cudaGetLastError() != cudaSuccess) { rc = fail(GADE_ERR_CUDA, "assembled operator: table launch failed"); break; }
+        }
         dim3 grid((unsigned)((WB + 255) / 256), (unsigned)s->npairs);
-        k_build_K<<<grid, 256, 0, s->stream>>>(s->d_K, (const R4<double>::T *)s->d_M, s->nk, (int)WB, a, d_pr,
-                                               s->d_pair_par, s->d_row_kidx, d_lp, d_ll, d_le,
+        k_build_K<<<grid, 256, 0, s->stream>>>(s->d_K + (size_t)ks * 3 * per,
+                                               (const R4<double>::T *)s->d_M + (size_t)ks * s->mstride, s->nk,
+                                               (int)WB, a, d_pr, s->d_pair_par, s->d_row_kidx, d_lp, d_ll, d_le,
                                                (const double *)s->d_ang_a0, (const double *)s->d_ang_a0k,
                                                (const double *)s->d_ang_a1, (const double *)s->d_ang_a1k);
         if (cudaGetLastError() != cudaSuccess) { rc = fail(GADE_ERR_CUDA, "assembled operator: K build launch failed"); break; }
@@ -2645,20 +2675,15 @@ static int asm_build(gade_solver *s)
 static int launch_assemble(gade_solver *s, cudaStream_t st)
 {
     const int WB2 = s->W * s->B / 2;
+    const size_t per2 = (size_t)s->npairs * WB2;
     prof_begin(s, st);
-    k_assemble<<<dim3((unsigned)((WB2 + 255) / 256), (unsigned)s->npairs), 256, 0, st>>>(
+    k_assemble<<<dim3((unsigned)((WB2 + 255) / 256), (unsigned)s->npairs, (unsigned)s->nslot), 256, 0, st>>>(
         (double2 *)s->d_A, (float2 *)s->d_A32, (const double2 *)s->d_K, WB2, s->d_pair_par, s->d_coef,
-        make_int2(s->lpar[0], s->lpar[1]));
+        make_int2(s->lpar[0], s->lpar[1]), s->d_plist, per2, s->asm_kstride / 2, s->lmax);
     prof_end(s, st, 2);
     CKL();
     s->has_time = 1;
     return GADE_OK;
-}
-
-/* the step's FP64 tables: assembled couplings or the matrix-free radial tables */
-static int launch_step_tables(gade_solver *s, cudaStream_t st)
-{
-    return s->use_asm ? launch_assemble(s, st) : launch_table_kernels(s, 1, st);
 }
 
 static OpP op_params32(const gade_solver *s);
@@ -2671,8 +2696,10 @@ static int launch_apply_asm(gade_solver *s, const typename Cx<R>::T *x, int mode
     OpP P = f32 ? op_params32(s) : op_params(s);
     P.A = f32 ? (const void *)s->d_A32 : (const void *)s->d_A;
     P.pair_c = s->d_pair_c;
+    P.astride = (size_t)s->npairs * s->W * s->B;
     const bool sep = mode == AX_RHS || mode == AX_PARTS || mode == AX_MIX;
-    const PartList &pl = s->asm_part ? s->part_asm_bal[s->occ_asm[f32][sep]] : s->part_asm[0];
+    /* batches run the plain partition (their pulses fill the SMs) */
+    const PartList &pl = (s->asm_part && s->nslot == 1) ? s->part_asm_bal[s->occ_asm[f32][sep]] : s->part_asm[0];
     P.seg_ptr = pl.d_seg_ptr;
     P.pieces = pl.d_pieces;
     dim3 grid(s->nslot, pl.nseg);
@@ -3020,21 +3047,61 @@ static int time_fp64_apply(gade_solver *s, float *ms)
  * matrix-free one chosen by choose_split (its per-step assembly replaces the
  * radial tables).
  */
+/* ms of the step's tables of the current operator: the matrix-free radial
+   tables or the assembly of the coupling values (float copies included in
+   mixed precision) */
+static int time_step_tables(gade_solver *s, float *ms)
+{
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    const int which = s->prec == GADE_PREC_MIXED ? 3 : 1;
+    int rc = s->use_asm ? launch_assemble(s, s->stream) : launch_table_kernels(s, which, s->stream);
+    if (!rc && cudaEventRecord(e0, s->stream) != cudaSuccess) rc = fail(GADE_ERR_CUDA, "event record failed");
+    for (int rep = 0; rep < 3 && !rc; rep++)
+        rc = s->use_asm ? launch_assemble(s, s->stream) : launch_table_kernels(s, which, s->stream);
+    float t = 0;
+    if (!rc && (cudaEventRecord(e1, s->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+                cudaEventElapsedTime(&t, e0, e1) != cudaSuccess))
+        rc = fail(GADE_ERR_CUDA, "table timing failed");
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms = t / 3;
+    s->has_time = 0;
+    return rc;
+}
+
+/* A step's operator cost: its tables plus three operator applies (the
+   right-hand side and one BiCGSTAB iteration; in mixed precision the timed
+   apply is the FP64 residual pass plus one inner iteration's two complex64
+   applies, so it counts once) */
+static float step_cost(const gade_solver *s, float tables_ms, float apply_ms)
+{
+    return tables_ms + (s->prec == GADE_PREC_MIXED ? 1.0f : 3.0f) * apply_ms;
+}
+
 static int choose_operator(gade_solver *s)
 {
     s->mf_ms = s->split_ms[s->nsplit >= 1 && s->nsplit <= 4 ? s->nsplit : 0];
     s->asm_ms[0] = s->asm_ms[1] = 0.f;
     int rc = asm_build(s);
     if (rc || !s->asm_ok) return rc;
+    float tab_mf = 0.f, tab_asm = 0.f;
+    s->use_asm = 0;
+    if ((rc = time_step_tables(s, &tab_mf))) return rc;
     s->use_asm = 1;
     for (int part = 0; part < 2 && !rc; part++) {
         s->asm_part = part;
         rc = time_fp64_apply(s, &s->asm_ms[part]);
     }
+    if (!rc) rc = time_step_tables(s, &tab_asm);
     if (rc) { s->use_asm = 0; return rc; }
     s->asm_part = s->asm_ms[1] < s->asm_ms[0] ? 1 : 0;
     const float best = s->asm_ms[s->asm_part];
-    s->use_asm = (s->mf_ms <= 0.f || best < 0.98f * s->mf_ms) ? 1 : 0;
+    s->tab_ms[0] = tab_mf;
+    s->tab_ms[1] = tab_asm;
+    s->use_asm = (s->mf_ms <= 0.f ||
+                  step_cost(s, tab_asm, best) < 0.98f * step_cost(s, tab_mf, s->mf_ms)) ? 1 : 0;
     return GADE_OK;
 }
 
@@ -3049,9 +3116,8 @@ extern "C" int gade_solver_set_operator(gade_solver *s, int32_t assembled)
     if (assembled && !s->asm_ok) {
         if ((rc = asm_build(s))) return rc;
         if (!s->asm_ok)
-            return fail(GADE_ERR_ARG, "gade_solver_set_operator: the assembled operator needs one pulse with real "
-                                      "couplings, each pair coupled by orders of one parity, and device memory for "
-                                      "its values");
+            return fail(GADE_ERR_ARG, "gade_solver_set_operator: the assembled operator needs real couplings, "
+                                      "each pair coupled by orders of one parity, and device memory for its values");
         s->asm_part = 1;
     }
     if (s->engine) batch_drop_graphs(s->engine);
@@ -3064,7 +3130,10 @@ extern "C" int gade_solver_operator(const gade_solver *s, int32_t *assembled, fl
 {
     if (!s) return fail(GADE_ERR_ARG, "gade_solver_operator: NULL solver");
     if (assembled) *assembled = s->use_asm;
-    if (ms) { ms[0] = s->mf_ms; ms[1] = s->asm_ms[0]; ms[2] = s->asm_ms[1]; }
+    if (ms) {
+        ms[0] = s->mf_ms; ms[1] = s->asm_ms[0]; ms[2] = s->asm_ms[1];
+        ms[3] = s->tab_ms[0]; ms[4] = s->tab_ms[1];
+    }
     return GADE_OK;
 }
 
@@ -3317,6 +3386,7 @@ extern "C" int gade_solver_apply_dot_noalloc(gade_solver *s, const void *x_dev, 
         /* the assembled operator, one piece per unit */
         P.A = s->d_A;
         P.pair_c = s->d_pair_c;
+        P.astride = (size_t)s->npairs * s->W * s->B;
         P.seg_ptr = s->part_asm[0].d_seg_ptr;
         P.pieces = s->part_asm[0].d_pieces;
         k_apply_asm<double, false><<<dim3(1, s->part_asm[0].nseg), 256, asm_smem_bytes(s, sizeof(double2)), st>>>(
@@ -3448,7 +3518,8 @@ static int batch_seq_first(gade_batch *b, cudaStream_t st)
         CKL();
         return batch_seq_sweep(b, b->kiter, st);
     }
-    if ((rc = launch_step_tables(s, st))) return rc;
+    /* the step's FP64 tables: assembled couplings or the matrix-free radial tables */
+    if ((rc = s->use_asm ? launch_assemble(s, st) : launch_table_kernels(s, 1, st))) return rc;
     VecP V = {};
     V.out0 = s->rhs; V.out1 = s->r; V.out2 = s->r0;
     if ((rc = launch_apply(s, s->x, AX_RHS, V, RED_RHS, st, PRED_NONE))) return rc;
@@ -3563,6 +3634,46 @@ static int batch_autotune(gade_batch *b, const gade_problem *p)
     return rc;
 }
 
+/* Matrix-free or assembled operator for a batch: the assembled values of
+   every pulse (K shared when the pulses share their radial tables) against
+   the matrix-free operator, both timed as one apply of all pulses */
+static int batch_choose_operator(gade_batch *b)
+{
+    gade_solver *s = b->s;
+    int rc = asm_build(s);
+    if (rc || !s->asm_ok) return rc;
+    if ((rc = batch_set_list(b, b->list))) return rc;
+    float mf = 0.f, am = 0.f, tmf = 0.f, tam = 0.f;
+    s->use_asm = 0;
+    if ((rc = time_fp64_apply(s, &mf)) || (rc = time_step_tables(s, &tmf))) return rc;
+    s->use_asm = 1;
+    s->asm_part = 0;
+    if ((rc = time_fp64_apply(s, &am)) || (rc = time_step_tables(s, &tam))) { s->use_asm = 0; return rc; }
+    s->mf_ms = mf;
+    s->asm_ms[0] = am;
+    s->asm_ms[1] = 0.f;
+    s->tab_ms[0] = tmf;
+    s->tab_ms[1] = tam;
+    s->use_asm = step_cost(s, tam, am) < 0.98f * step_cost(s, tmf, mf) ? 1 : 0;
+    s->has_time = 0;
+    return GADE_OK;
+}
+
+extern "C" int gade_batch_operator(const gade_batch *b, int32_t *assembled, float *ms)
+{
+    if (!b) return fail(GADE_ERR_ARG, "gade_batch_operator: NULL batch");
+    return gade_solver_operator(b->s, assembled, ms);
+}
+
+extern "C" int gade_batch_set_operator(gade_batch *b, int32_t assembled)
+{
+    if (!b) return fail(GADE_ERR_ARG, "gade_batch_set_operator: NULL batch");
+    int rc = gade_solver_set_operator(b->s, assembled);
+    if (rc) return rc;
+    batch_drop_graphs(b);
+    return GADE_OK;
+}
+
 extern "C" int gade_batch_create(const gade_problem *p, int32_t npulse, const double *dt, const double *g,
                                  double h, int32_t precision, int32_t device, const gade_batch_options *opt,
                                  gade_batch **out)
@@ -3593,6 +3704,7 @@ extern "C" int gade_batch_create(const gade_problem *p, int32_t npulse, const do
     for (int k = 0; k < npulse; k++) b->list.push_back(k);
     s->nslot = npulse;
     if (o.chunk_splines == 0 && (rc = batch_autotune(b, p))) { gade_batch_free(b); return rc; }
+    if ((rc = batch_choose_operator(b))) { gade_batch_free(b); return rc; }
     *out = b;
     return GADE_OK;
 }

@@ -87,6 +87,8 @@ _SIGS = {
     "gade_solver_set_split": (C.c_int, [C.c_void_p, C.c_int32]),
     "gade_solver_apply_bytes": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "gade_solver_set_operator": (C.c_int, [C.c_void_p, C.c_int32]),
+    "gade_batch_operator": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.c_void_p]),
+    "gade_batch_set_operator": (C.c_int, [C.c_void_p, C.c_int32]),
     "gade_solver_assembly_cost": (C.c_int, [C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "gade_solver_operator": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.c_void_p]),
     "gade_solver_balanced": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
@@ -315,10 +317,11 @@ class Solver:
         """Operator in use (0 matrix-free, 1 assembled) and the timed FP64
         applies: matrix-free, assembled with the plain and the balanced partition."""
         a = C.c_int32()
-        ms = (C.c_float * 3)()
+        ms = (C.c_float * 5)()
         _check(load_library().gade_solver_operator(self._h, C.byref(a), ms))
         return {"assembled": int(a.value), "matrix_free_ms": float(ms[0]),
-                "assembled_plain_ms": float(ms[1]), "assembled_balanced_ms": float(ms[2])}
+                "assembled_plain_ms": float(ms[1]), "assembled_balanced_ms": float(ms[2]),
+                "tables_ms": float(ms[3]), "assembly_ms": float(ms[4])}
 
     def set_operator(self, assembled: int):
         _check(load_library().gade_solver_set_operator(self._h, int(assembled)))
@@ -426,6 +429,18 @@ class Batch:
 
     def stream(self) -> int:
         return int(load_library().gade_batch_stream(self._h) or 0)
+
+    def operator(self) -> dict:
+        """Operator in use (0 matrix-free, 1 assembled) and the timed batch
+        applies (matrix-free, assembled)."""
+        a = C.c_int32()
+        ms = (C.c_float * 5)()
+        _check(load_library().gade_batch_operator(self._h, C.byref(a), ms))
+        return {"assembled": int(a.value), "matrix_free_ms": float(ms[0]), "assembled_ms": float(ms[1]),
+                "tables_ms": float(ms[3]), "assembly_ms": float(ms[4])}
+
+    def set_operator(self, assembled: int):
+        _check(load_library().gade_batch_set_operator(self._h, int(assembled)))
 
     def state_device(self) -> tuple[int, int]:
         """(device address of the pulse states, per-pulse stride in complex elements)."""

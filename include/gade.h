@@ -174,11 +174,13 @@ int gade_solver_balanced(const gade_solver *s, int32_t *segments, int32_t *piece
  * values of each unit factor once (K_a, built from the radial tables) and
  * form this step's values as sum_a w_a(t) K_a; an apply then streams the
  * values (2 FMAs each); in mixed precision the complex64 inner solve
- * streams the values rounded to float.  gade_solver_create times both and
- * keeps the faster (the assembled one needs 32 bytes of device memory per
- * stored coupling value, 36 in mixed precision).  gade_solver_operator reports the choice and, in ms (3 floats,
- * may be NULL), the timed matrix-free apply and the assembled one with the
- * plain and the balanced partition (0 where not timed).  After
+ * streams the values rounded to float.  gade_solver_create times both (the
+ * step's tables and three applies) and keeps the faster (the assembled one
+ * needs 32 bytes of device memory per stored coupling value, 36 in mixed
+ * precision).  gade_solver_operator reports the choice and, in ms (5
+ * floats, may be NULL), the timed matrix-free apply, the assembled one with
+ * the plain and the balanced partition, and the step's matrix-free radial
+ * tables and assembly (0 where not timed).  After
  * gade_solver_set_operator the next gade_solver_set_time or step fills the
  * chosen operator's tables. */
 int gade_solver_set_operator(gade_solver *s, int32_t assembled);
@@ -258,6 +260,13 @@ typedef struct {
  * graphs).  Every pulse starts from psi0. */
 int gade_batch_create(const gade_problem *p, int32_t npulse, const double *dt, const double *g, double h,
                       int32_t precision, int32_t device, const gade_batch_options *opt, gade_batch **out);
+/* The operator of a batch (no reference counterpart): chosen by timing at
+ * creation like gade_solver_operator, ms as there (the assembled values take 8 bytes per
+ * stored coupling value and pulse, 12 in mixed precision, plus 24 per value
+ * for each distinct set of radial tables); gade_batch_set_operator forces it
+ * (the next step fills the chosen operator's tables). */
+int gade_batch_operator(const gade_batch *b, int32_t *assembled, float *ms);
+int gade_batch_set_operator(gade_batch *b, int32_t assembled);
 void gade_batch_free(gade_batch *b);
 int gade_batch_set_x(gade_batch *b, int32_t pulse, const double *x, int64_t n);
 int gade_batch_get_x(gade_batch *b, int32_t pulse, double *x, int64_t n);

@@ -62,14 +62,17 @@ def test_batch_matches_oracle_per_pulse(batch_case, native_lib):
     assert inf["chunk_splines"] in inf["tune_cs"]
 
 
+@pytest.mark.parametrize("op", [0, 1])
 @pytest.mark.parametrize("graphs", [True, False])
-def test_batch_bit_identical_to_single_pulse_batches(batch_case, native_lib, graphs):
+def test_batch_bit_identical_to_single_pulse_batches(batch_case, native_lib, graphs, op):
+    """With the same operator (matrix-free 0, assembled 1) a pulse's bits do
+    not depend on the other pulses of its batch."""
     d, params, info, prob, tables, dirs = batch_case
     cs = 16
-    xs, recs, _ = run_batch(prob, PULSES, tables, tol=1e-12, chunk_splines=cs, use_graphs=graphs)
+    xs, recs, _ = run_batch(prob, PULSES, tables, tol=1e-12, chunk_splines=cs, use_graphs=graphs, operator=op)
     for k in range(len(PULSES)):
         x1, r1, _ = run_batch(prob, [PULSES[k]], tables[k:k + 1], tol=1e-12, chunk_splines=cs,
-                              use_graphs=True, iters_per_launch=2)
+                              use_graphs=True, iters_per_launch=2, operator=op)
         assert np.array_equal(xs[k], x1[0]), k
         assert [r["iters"] for r in recs[k]] == [r["iters"] for r in r1[0]]
 
@@ -161,11 +164,33 @@ def test_mixed_batch_matches_single_pulse_mixed(batch_case, native_lib):
         assert sum(abs(a["inner_iters"] - r["inner_iters"]) for a, r in zip(rm[k], rs)) <= 4
 
 
-def test_mixed_batch_bit_identical_to_single_pulse_batches(batch_case, native_lib):
+@pytest.mark.parametrize("op", [0, 1])
+def test_mixed_batch_bit_identical_to_single_pulse_batches(batch_case, native_lib, op):
     d, params, info, prob, tables, dirs = batch_case
-    xs, recs, _ = run_batch(prob, PULSES, tables, tol=1e-10, precision="mixed", chunk_splines=16)
+    xs, recs, _ = run_batch(prob, PULSES, tables, tol=1e-10, precision="mixed", chunk_splines=16, operator=op)
     for k in range(len(PULSES)):
         x1, r1, _ = run_batch(prob, [PULSES[k]], tables[k:k + 1], tol=1e-10, precision="mixed", chunk_splines=16,
-                              iters_per_launch=3)
+                              iters_per_launch=3, operator=op)
         assert np.array_equal(xs[k], x1[0]), k
         assert [r["inner_iters"] for r in recs[k]] == [r["inner_iters"] for r in r1[0]]
+
+
+@pytest.mark.parametrize("shared_tables", [False, True])
+def test_batch_operators_agree(batch_case, native_lib, shared_tables):
+    """The assembled operator of a batch (per-pulse values; one set of
+    unit-factor values when the pulses share their radial tables) gives the
+    matrix-free batch's iterations and states."""
+    d, params, info, prob, tables, dirs = batch_case
+    pulses = PULSES
+    if shared_tables:
+        pulses = [dict(p, omega=params["Omega"], cycles=params["Cycles"]) for p in PULSES]
+    tab = None if shared_tables else tables
+    out = []
+    for op in (0, 1):
+        xs, recs, b = run_batch(prob, pulses, tab, tol=1e-12, maxit=500, operator=op)
+        assert b.operator()["assembled"] == op
+        out.append((xs, [[r["iters"] for r in rk] for rk in recs]))
+        b.close()
+    assert out[1][1] == out[0][1]
+    for k in range(len(pulses)):
+        assert _rel(out[1][0][k], out[0][0][k]) < 1e-12, k
