@@ -1089,13 +1089,38 @@ __global__ void __launch_bounds__(256, 3)
         }
         __syncthreads();
         if (i >= 0) {
-            for (int g = 0; g < ng; g++) {
-                const R *Av = (const R *)P.A + (size_t)pulse * P.astride + (size_t)(pg + g) * WB + i + jB;
-                const C *xg = xw + g * CS;
+            const R *A0 = (const R *)P.A + (size_t)pulse * P.astride + (size_t)pg * WB + i + jB;
+            if constexpr (sizeof(R) == 4) {
+                /* complex64: latency-bound, so the next block's values are
+                   loaded while this block's are used (two sets in flight) */
+                R cur[HJ];
+                {
+                    const R *Av = A0;
 #pragma unroll
-                for (int t = 0; t < HJ; t++) {
-                    rfma(accH, __ldcs(Av), xg[LCO(t)]);
-                    if (t + 1 < nj) Av += B;
+                    for (int t = 0; t < HJ; t++) { cur[t] = __ldcs(Av); if (t + 1 < nj) Av += B; }
+                }
+                for (int g = 0; g < ng; g++) {
+                    R nxt[HJ];
+                    if (g + 1 < ng) {
+                        const R *Av = A0 + (size_t)(g + 1) * WB;
+#pragma unroll
+                        for (int t = 0; t < HJ; t++) { nxt[t] = __ldcs(Av); if (t + 1 < nj) Av += B; }
+                    }
+                    const C *xg = xw + g * CS;
+#pragma unroll
+                    for (int t = 0; t < HJ; t++) rfma(accH, cur[t], xg[LCO(t)]);
+#pragma unroll
+                    for (int t = 0; t < HJ; t++) cur[t] = nxt[t];
+                }
+            } else {
+                for (int g = 0; g < ng; g++) {
+                    const R *Av = A0 + (size_t)g * WB;
+                    const C *xg = xw + g * CS;
+#pragma unroll
+                    for (int t = 0; t < HJ; t++) {
+                        rfma(accH, __ldcs(Av), xg[LCO(t)]);
+                        if (t + 1 < nj) Av += B;
+                    }
                 }
             }
         }
