@@ -1191,17 +1191,25 @@ __global__ void __launch_bounds__(256, 3)
 /* ------------------------------------------------------------------ */
 /* block-LU preconditioner, TMA-staged factors                          */
 /* ------------------------------------------------------------------ */
-/* Factor data of one 32-row chunk is contiguous in HBM:
- *   [Linv (32x32, column-major [j][lane])][band: BWP rows [d][lane] holding
- *   -L(o, o-d-1) (negated) only where that source row lies before the chunk, else 0]
- * (and the same for U with the sources after the chunk).  One elected lane
- * streams chunk k+1 into shared memory with cp.async.bulk on an mbarrier
- * while the warp computes chunk k.  Every wait is bounded: on timeout the
+/* Each sweep (L forward, then U backward) over the 32-row chunks c of a
+ * block row is split into a part without dependences and a short chain:
+ *   L:  x_c = Linv_c b_c + G_c  x_{c-1}[32-BWP .. 31],  G_c  = -Linv_c Lband_c
+ *   U:  z_c = Uinv_c x_c + GU_c z_{c+1}[0 .. BWP-1],    GU_c = -Uinv_c Uband_c
+ * (Lband_c / Uband_c: the band entries whose source row lies in the
+ * neighbouring chunk; the band is at most BWP <= 32 wide).  Factor data of
+ * one (pulse, kappa) and sweep is contiguous in HBM:
+ *   [triangles: npair x 33 x 32][chain blocks: nch x BWP x 32]  (complex)
+ * A triangle pair packs two chunks' inverse blocks so that lane i runs
+ * 33 products with no zeros: for L, row i of chunk 2p (i+1 entries) then
+ * row 31-i of chunk 2p+1 (32-i entries); for U, row i of chunk 2p (32-i
+ * entries) then row 31-i of chunk 2p+1 (i+1 entries).  One elected lane
+ * streams stage s+1 into shared memory with cp.async.bulk on an mbarrier
+ * while the CTA computes stage s; every wait is bounded: on timeout the
  * kernel sets sc->err, drains its copies (bounded) and returns. */
 struct PcT {
     int nblk, B, Bp, nch;
     const int *row_kidx, *ord;
-    const void *FL, *FU;           /* [pulse][nk][nch][CH] complex of the kernel's precision */
+    const void *FL, *FU;           /* [pulse][nk][sweep layout] complex of the kernel's precision */
     const int *plist;              /* grid x -> pulse (NULL: pulse 0) */
     long long vstride;             /* complex elements per pulse of every vector */
     size_t fstride;                /* complex elements per pulse of FL / FU */
@@ -1243,13 +1251,24 @@ __device__ __forceinline__ void tma_bulk_load(void *dst, const void *src, unsign
 
 #define MBAR_SPIN_LIMIT (1u << 22)
 
+/* complex elements of one triangle pair and of one chunk's chain block */
+#define PC_TP (33 * 32)
+__host__ __device__ __forceinline__ size_t pc_sweep_elems(int nch, int bwp)
+{
+    return (size_t)((nch + 1) / 2) * PC_TP + (size_t)nch * 32 * bwp;
+}
+/* staging buffer of one stage: up to 4 triangle pairs or PC_GCH chain blocks */
+#define PC_GCH 4
+__host__ __device__ __forceinline__ int pc_stage_elems(int bwp)
+{
+    return 4 * PC_TP > PC_GCH * 32 * bwp ? 4 * PC_TP : PC_GCH * 32 * bwp;
+}
+
 /* 4 warps per block row, one per SM sub-partition (each has its own FP64
- * unit): in every 32-row step warp w applies band terms d = 4w+1..4w+4 and
- * the inverse-block columns j = 8w..8w+7.  Partial sums meet in shared
- * memory and are combined once per row, spread over all four warps (two
- * adds per lane); the inverse-block products read the combined values as
- * broadcasts.  The sweeps are bound by the FP64 instructions each warp
- * issues (54 per step): fewer partial sums and no negations. */
+ * unit).  Triangle stages: warp w takes the stage's pair w.  Chain steps:
+ * warp w applies chain columns w BWP/4 .. (w+1) BWP/4 - 1 to every row; the
+ * partial sums meet in shared memory and are combined once per row, spread
+ * over all four warps (two adds per lane). */
 template <typename R, int BWP>
 __global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const typename Cx<R>::T *__restrict__ in0,
                                                      const typename Cx<R>::T *__restrict__ in1,
@@ -1257,13 +1276,13 @@ __global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const type
                                                      DevScal *sc)
 {
     typedef typename Cx<R>::T C;
-    constexpr int CH = 1024 + 32 * BWP;
-    constexpr int DPW = BWP / 4;                 /* band terms per warp */
+    constexpr int GC = 32 * BWP;                 /* complex elements of one chain block */
+    constexpr int CPW = BWP / 4;                 /* chain columns per warp */
+    const int SB = pc_stage_elems(BWP);
     extern __shared__ __align__(128) unsigned char smem_tma[];
-    C *fac = (C *)smem_tma;          /* [2][CH]  */
-    C *buf = fac + 2 * CH;                 /* [Bp]     */
-    C *pt = buf + Q.Bp;                    /* [4][32] partial t, then t in pt[0..31] */
-    C *py = pt + 128;                      /* [4][32] partial y */
+    C *stg = (C *)smem_tma;                /* [2][SB] */
+    C *buf = stg + 2 * SB;                 /* [Bp]    */
+    C *pt = buf + Q.Bp;                    /* [4][32] partial sums */
     __shared__ __align__(8) uint64_t bar[2];
     __shared__ int all_ok;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -1285,17 +1304,37 @@ __global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const type
         out += vo;
     }
     const int B = Q.B, Bp = Q.Bp, nch = Q.nch;
+    const int npair = (nch + 1) / 2;
+    const int nsa = (npair + 3) / 4, nsg = (nch + PC_GCH - 1) / PC_GCH, nps = nsa + nsg;
+    const int ns = 2 * nps;                 /* stages: L triangles, L chain, U triangles, U chain */
     const int kk = Q.row_kidx[r];
     const size_t off = (size_t)r * B;
-    const C *FL = (const C *)Q.FL + (size_t)pulse * Q.fstride + (size_t)kk * nch * CH;
-    const C *FU = (const C *)Q.FU + (size_t)pulse * Q.fstride + (size_t)kk * nch * CH;
-    const unsigned bytes = CH * sizeof(C);
+    const size_t per = pc_sweep_elems(nch, BWP);
+    const C *FL = (const C *)Q.FL + (size_t)pulse * Q.fstride + (size_t)kk * per;
+    const C *FU = (const C *)Q.FU + (size_t)pulse * Q.fstride + (size_t)kk * per;
+    /* source and size of stage k; the U chain runs its groups last to first */
+    auto stage = [&](int k, const C **src, int *cnt) {
+        const C *F = k < nps ? FL : FU;
+        const int j = k < nps ? k : k - nps;
+        if (j < nsa) {
+            *cnt = min(4, npair - 4 * j);
+            *src = F + (size_t)4 * j * PC_TP;
+            return (unsigned)(*cnt * PC_TP * sizeof(C));
+        }
+        const int g = k < nps ? j - nsa : nsg - 1 - (j - nsa);
+        *cnt = min(PC_GCH, nch - g * PC_GCH);
+        *src = F + (size_t)npair * PC_TP + (size_t)g * PC_GCH * GC;
+        return (unsigned)(*cnt * GC * sizeof(C));
+    };
 
     if (tid == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        tma_bulk_load(fac, FL, bytes, &bar[0]);          /* first forward chunk */
+        const C *src;
+        int cnt;
+        const unsigned bytes = stage(0, &src, &cnt);
+        tma_bulk_load(stg, src, bytes, &bar[0]);
         all_ok = 1;
     }
 
@@ -1332,16 +1371,13 @@ __global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const type
     }
     __syncthreads();
 
-    const int nk = 2 * nch;           /* chunk steps: forward then backward */
     int k = 0;
-    for (; k < nk; k++) {
-        const int fwd = k < nch;
-        const int c = fwd ? k : nch - 1 - (k - nch);
-        if (tid == 0 && k + 1 < nk) {
-            const int k1 = k + 1;
-            const int c1 = k1 < nch ? k1 : nch - 1 - (k1 - nch);
-            const C *src = (k1 < nch ? FL : FU) + (size_t)c1 * CH;
-            tma_bulk_load(fac + (k1 & 1) * CH, src, bytes, &bar[k1 & 1]);
+    for (; k < ns; k++) {
+        if (tid == 0 && k + 1 < ns) {
+            const C *src;
+            int cnt;
+            const unsigned bytes = stage(k + 1, &src, &cnt);
+            tma_bulk_load(stg + ((k + 1) & 1) * SB, src, bytes, &bar[(k + 1) & 1]);
         }
         unsigned spins = 0;
         bool ok = true;
@@ -1351,52 +1387,65 @@ __global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const type
         if (!ok) all_ok = 0;
         __syncthreads();
         if (!all_ok) break;
-        const C *F = fac + (k & 1) * CH;
-        const int o = 32 * c + lane;
-        /* band terms of this warp */
-        C t = (wid == 0) ? buf[o] : mk<C>(0, 0);
+        const C *S = stg + (k & 1) * SB;
+        const int up = k >= nps;                   /* U sweep */
+        const int j = up ? k - nps : k;
+        if (j < nsa) {
+            /* triangle pair 4 j + wid: chunks c0 = 2p, c1 = 2p + 1 */
+            const int p = 4 * j + wid;
+            if (p < npair) {
+                const C *T = S + wid * PC_TP;
+                const int c0 = 2 * p, c1 = 2 * p + 1;
+                const bool has1 = c1 < nch;
+                const int sw = up ? 31 - lane : lane;  /* last product of the first row */
+                C acc = mk<C>(0, 0), sav = acc;
 #pragma unroll
-        for (int q = 0; q < DPW; q++) {
-            const int d = wid * DPW + q + 1;
-            const C bv = F[1024 + (d - 1) * 32 + lane];     /* stored negated */
-            const int src = fwd ? (o - d >= 0 ? o - d : 0) : (o + d < Bp ? o + d : Bp - 1);
-            cfma(t, bv, buf[src]);
-        }
-        pt[wid * 32 + lane] = t;
-        __syncthreads();
-        {
-            /* the row's t = (p0 + p1) + (p2 + p3), once: warp w sums rows
-               8w..8w+7, a lane one pair of one component, a shuffle the pairs */
-            R *pr = (R *)pt;
-            R sum = pr[((2 * ch) * 32 + crow) * 2 + ccomp] + pr[((2 * ch + 1) * 32 + crow) * 2 + ccomp];
-            sum += __shfl_xor_sync(0xffffffffu, sum, 1);
-            if (ch == 0) pr[crow * 2 + ccomp] = sum;
-        }
-        __syncthreads();
-        /* this warp's 8 columns of the inverse block */
-        /* one accumulator: the sweeps are bound by the FP64 instructions a
-           warp issues, not by the length of the DFMA chain (measured) */
-        C a0 = mk<C>(0, 0);
+                for (int q = 0; q < 33; q++) {
+                    int src;
+                    if (!up) src = q <= lane ? 32 * c0 + q : (has1 ? 32 * c1 + q - lane - 1 : 0);
+                    else src = q <= 31 - lane ? 32 * c0 + lane + q : (has1 ? 32 * c1 + q - 1 : 0);
+                    cfma(acc, T[q * 32 + lane], buf[src]);
+                    if (q == sw) { sav = acc; acc = mk<C>(0, 0); }
+                }
+                __syncwarp();
+                buf[32 * c0 + lane] = sav;
+                if (has1) buf[32 * c1 + 31 - lane] = acc;
+            }
+            __syncthreads();
+        } else {
+            const int g = up ? nsg - 1 - (j - nsa) : j - nsa;
+            const int cnt = min(PC_GCH, nch - g * PC_GCH);
+            for (int e = 0; e < cnt; e++) {
+                const int ci = up ? cnt - 1 - e : e;     /* U: last chunk first */
+                const int c = g * PC_GCH + ci;
+                if (up ? c == nch - 1 : c == 0) continue;  /* no neighbour: the triangle result stands */
+                const C *G = S + ci * GC;
+                const int base = up ? 32 * (c + 1) : 32 * c - BWP;
+                C t = (wid == 0) ? buf[32 * c + lane] : mk<C>(0, 0);
 #pragma unroll
-        for (int q = 0; q < 8; q++) {
-            const int j0 = wid * 8 + q;
-            cfma(a0, F[j0 * 32 + lane], pt[j0]);
+                for (int q = 0; q < CPW; q++) {
+                    const int col = wid * CPW + q;
+                    cfma(t, G[col * 32 + lane], buf[base + col]);
+                }
+                pt[wid * 32 + lane] = t;
+                __syncthreads();
+                {
+                    /* the row's sum (p0 + p1) + (p2 + p3), once: warp w sums rows
+                       8w..8w+7, a lane one pair of one component, a shuffle the pairs */
+                    const R *pr = (const R *)pt;
+                    R sum = pr[((2 * ch) * 32 + crow) * 2 + ccomp] + pr[((2 * ch + 1) * 32 + crow) * 2 + ccomp];
+                    sum += __shfl_xor_sync(0xffffffffu, sum, 1);
+                    if (ch == 0) ((R *)buf)[(32 * c + crow) * 2 + ccomp] = sum;
+                }
+                __syncthreads();
+            }
         }
-        py[wid * 32 + lane] = a0;
-        __syncthreads();
-        {
-            const R *pr = (const R *)py;
-            R sum = pr[((2 * ch) * 32 + crow) * 2 + ccomp] + pr[((2 * ch + 1) * 32 + crow) * 2 + ccomp];
-            sum += __shfl_xor_sync(0xffffffffu, sum, 1);
-            if (ch == 0) ((R *)buf)[(32 * c + crow) * 2 + ccomp] = sum;
-        }
-        __syncthreads();
     }
     if (!all_ok) {
         if (tid == 0) {
             atomicOr(&sc->err, 1u);
             /* drain the copies still in flight (bounded) before exiting */
-            for (int k2 = k; k2 < k + 2 && k2 < nk; k2++) {
+            for (int k2 = k; k2 < k + 2 && k2 < ns; k2++) {
                 unsigned spins = 0;
                 while (!mbar_try_wait(&bar[k2 & 1], (k2 >> 1) & 1) && ++spins < MBAR_SPIN_LIMIT) {
                 }
@@ -1901,34 +1950,56 @@ static int set_chunking(gade_solver *s, const gade_setup *su)
     return part_reset(s);
 }
 
-/* chunk-packed block-LU factors of one pulse: [nk][nch][Linv | masked band],
-   the band stored negated (the sweep adds -L(o, o-d) y(o-d)) */
+/* block-LU factors of one pulse in the sweep layout of k_precond_tma:
+   per kappa and sweep [triangle pairs][chain blocks]; the chain blocks
+   G_c = -Linv_c Lband_c and GU_c = -Uinv_c Uband_c are formed here in FP64 */
 static void pack_factors(const gade_setup *su, int nk, int nch, int bw, int bwp, int B, int Bp,
                          double2 *FL, double2 *FU)
 {
-    const int CH = 1024 + 32 * bwp;
-    for (int kk = 0; kk < nk; kk++)
-        for (int c = 0; c < nch; c++) {
-            double2 *fl = FL + ((size_t)kk * nch + c) * CH;
-            double2 *fu = FU + ((size_t)kk * nch + c) * CH;
-            memcpy(fl, su->Linv + ((size_t)kk * nch + c) * 1024, 1024 * sizeof(double2));
-            memcpy(fu, su->Uinv + ((size_t)kk * nch + c) * 1024, 1024 * sizeof(double2));
-            for (int d = 1; d <= bwp; d++)
-                for (int lane = 0; lane < 32; lane++) {
-                    int o = 32 * c + lane;
-                    double2 lv = make_double2(0, 0), uv = make_double2(0, 0);
-                    if (d <= bw && o - d >= 0 && o - d < 32 * c) {
-                        gc64 v = su->Lb[((size_t)kk * bw + d - 1) * Bp + o];
-                        lv = make_double2(v.re, v.im);
-                    }
-                    if (d <= bw && o + d < B && o + d >= 32 * (c + 1)) {
-                        gc64 v = su->Ub[((size_t)kk * bw + d - 1) * Bp + o];
-                        uv = make_double2(v.re, v.im);
-                    }
-                    fl[1024 + (d - 1) * 32 + lane] = make_double2(-lv.x, -lv.y);
-                    fu[1024 + (d - 1) * 32 + lane] = make_double2(-uv.x, -uv.y);
+    const int npair = (nch + 1) / 2;
+    const size_t per = pc_sweep_elems(nch, bwp);
+    auto cmac = [](double2 &acc, gc64 a, gc64 b) {
+        acc.x += a.re * b.re - a.im * b.im;
+        acc.y += a.re * b.im + a.im * b.re;
+    };
+    for (int kk = 0; kk < nk; kk++) {
+        const gc64 *Li = su->Linv + (size_t)kk * nch * 1024, *Ui = su->Uinv + (size_t)kk * nch * 1024;
+        double2 *fl = FL + (size_t)kk * per, *fu = FU + (size_t)kk * per;
+        /* inverse blocks, column-major [j][i]: Linv_c(i, j) = Li[c 1024 + 32 j + i] */
+        for (int p = 0; p < npair; p++) {
+            const int c0 = 2 * p, c1 = 2 * p + 1;
+            for (int q = 0; q < 33; q++)
+                for (int i = 0; i < 32; i++) {
+                    gc64 lv = {0, 0}, uv = {0, 0};
+                    if (q <= i) lv = Li[(size_t)c0 * 1024 + q * 32 + i];
+                    else if (c1 < nch) lv = Li[(size_t)c1 * 1024 + (q - i - 1) * 32 + (31 - i)];
+                    if (q <= 31 - i) uv = Ui[(size_t)c0 * 1024 + (i + q) * 32 + i];
+                    else if (c1 < nch) uv = Ui[(size_t)c1 * 1024 + (q - 1) * 32 + (31 - i)];
+                    fl[(size_t)p * PC_TP + q * 32 + i] = make_double2(lv.re, lv.im);
+                    fu[(size_t)p * PC_TP + q * 32 + i] = make_double2(uv.re, uv.im);
                 }
         }
+        double2 *gl = fl + (size_t)npair * PC_TP, *gu = fu + (size_t)npair * PC_TP;
+        for (int c = 0; c < nch; c++)
+            for (int col = 0; col < bwp; col++)
+                for (int i = 0; i < 32; i++) {
+                    double2 g = make_double2(0, 0), h = make_double2(0, 0);
+                    for (int m = 0; m < 32; m++) {
+                        const int row = 32 * c + m;
+                        if (row >= B) break;
+                        /* L(row, 32 c - bwp + col) */
+                        const int cl = 32 * c - bwp + col, dl = row - cl;
+                        if (c > 0 && dl >= 1 && dl <= bw && cl >= 0 && m <= i)
+                            cmac(g, Li[(size_t)c * 1024 + m * 32 + i], su->Lb[((size_t)kk * bw + dl - 1) * Bp + row]);
+                        /* U(row, 32 (c + 1) + col) */
+                        const int cu = 32 * (c + 1) + col, du = cu - row;
+                        if (c + 1 < nch && du >= 1 && du <= bw && cu < B && m >= i)
+                            cmac(h, Ui[(size_t)c * 1024 + m * 32 + i], su->Ub[((size_t)kk * bw + du - 1) * Bp + row]);
+                    }
+                    gl[((size_t)c * bwp + col) * 32 + i] = make_double2(-g.x, -g.y);
+                    gu[((size_t)c * bwp + col) * 32 + i] = make_double2(-h.x, -h.y);
+                }
+    }
 }
 
 /*
@@ -2046,8 +2117,7 @@ static int solver_create(const gade_problem *p, int npulse, const double *dts, c
     s->gstride = (size_t)s->lmax * 3 * 4 * WB;     /* radial tables in the ELL slot layout */
     s->bwp = s->bw <= 16 ? 16 : 32;
     if (s->bw > 32) { gade_setup_release(su); gade_solver_free(s); return fail(GADE_ERR_ARG, "preconditioner band %d wider than 32 is not supported", s->bw); }
-    const int CH = 1024 + 32 * s->bwp;
-    s->fstride = (size_t)s->nk * s->nch * CH;
+    s->fstride = (size_t)s->nk * pc_sweep_elems(s->nch, s->bwp);
 
     if (npulse > 1) {
         std::vector<int> ident(npulse);
@@ -2120,11 +2190,11 @@ static int solver_create(const gade_problem *p, int npulse, const double *dts, c
         }
     }
     {
-        size_t smem = sizeof(double2) * ((size_t)2 * CH + s->Bp + 256);
+        size_t smem = sizeof(double2) * ((size_t)2 * pc_stage_elems(s->bwp) + s->Bp + 128);
         if (smem > 220 * 1024) { gade_setup_release(su); gade_solver_free(s); return fail(GADE_ERR_ARG, "block dimension too large for the preconditioner"); }
         cudaFuncSetAttribute(k_precond_tma<double, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         cudaFuncSetAttribute(k_precond_tma<double, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        size_t smem32 = sizeof(float2) * ((size_t)2 * CH + s->Bp + 256);
+        size_t smem32 = sizeof(float2) * ((size_t)2 * pc_stage_elems(s->bwp) + s->Bp + 128);
         cudaFuncSetAttribute(k_precond_tma<float, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem32);
         cudaFuncSetAttribute(k_precond_tma<float, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem32);
     }
@@ -2245,8 +2315,10 @@ static int solver_create(const gade_problem *p, int npulse, const double *dts, c
         }
         memset(s->h_sc2, 0, sizeof(DevScal) * NP);
     }
-    /* block solves: per lane and chunk, bw band terms + 32 inverse terms, 2 sweeps */
-    s->precond_flops = 2.0 * 4.0 * (double)s->nblk * 32.0 * s->nch * 2.0 * (s->bwp + 32);
+    /* block solves, 2 sweeps: the triangle pairs (33 products per lane) and
+       the chain blocks of every chunk with a neighbour (BWP products per row) */
+    s->precond_flops = 2.0 * 8.0 * (double)s->nblk *
+                       (32.0 * 33.0 * ((s->nch + 1) / 2) + 32.0 * s->bwp * (s->nch - 1));
     if (s->rc) {
         /* (block row, coupled block) pairs and the (order, angular term) list
            of every pair, for the assembled operator */
@@ -2767,8 +2839,7 @@ static int launch_precond(gade_solver *s, int mode, const double2 *in0, const do
                           double2 *out, cudaStream_t st, int pred = PRED_NONE)
 {
     PcT Q = pc_params(s, s->d_FL, s->d_FU, pred);
-    const int CH = 1024 + 32 * s->bwp;
-    size_t smem = sizeof(double2) * ((size_t)2 * CH + s->Bp + 256);
+    size_t smem = sizeof(double2) * ((size_t)2 * pc_stage_elems(s->bwp) + s->Bp + 128);
     dim3 grid(s->nslot, s->nblk);
     prof_begin(s, st);
     if (s->bwp == 16) k_precond_tma<double, 16><<<grid, 128, smem, st>>>(Q, mode, in0, in1, io, out, s->d_sc);
@@ -2954,8 +3025,7 @@ static int launch_precond32(gade_solver *s, int mode, const float2 *in0, const f
                             float2 *out, DevScal *sc, int pred = PRED_NONE)
 {
     PcT Q = pc_params(s, s->d_FL32, s->d_FU32, pred);
-    const int CH = 1024 + 32 * s->bwp;
-    size_t smem = sizeof(float2) * ((size_t)2 * CH + s->Bp + 256);
+    size_t smem = sizeof(float2) * ((size_t)2 * pc_stage_elems(s->bwp) + s->Bp + 128);
     dim3 grid(s->nslot, s->nblk);
     prof_begin(s, s->stream);
     if (s->bwp == 16) k_precond_tma<float, 16><<<grid, 128, smem, s->stream>>>(Q, mode, in0, in1, io, out, sc);
