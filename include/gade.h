@@ -92,8 +92,9 @@ int gade_solver_set_x(gade_solver *s, const double *x, int64_t n);
 int gade_solver_get_x(gade_solver *s, double *x, int64_t n);
 
 /* One Crank-Nicolson step at time t with pulse factors ft (6 complex, i.e.
- * 12 doubles, beoyndDipolePulse_axialPart at t): assembles nothing — the
- * operator S + H(t) is applied matrix-free — then forms
+ * 12 doubles, beoyndDipolePulse_axialPart at t): fills this step's operator
+ * (the assembled real coupling values, or the matrix-free radial tables,
+ * whichever was chosen at creation), then forms
  * rhs = S x - H(t) x and solves (S + H(t)) x' = rhs with right-block-LU-
  * preconditioned BiCGSTAB warm-started at x.  Replaces the loop body
  * tools/dirac_solver.c:503-551 (gpu_compute_timedep_matrices, gpu_spmv,
@@ -102,6 +103,15 @@ int gade_solver_get_x(gade_solver *s, double *x, int64_t n);
  * stats may be NULL. */
 int gade_solver_step(gade_solver *s, const double *ft, int32_t maxit, double tol,
                      gade_step_stats *stats);
+/* The same step with the state in host memory (no reference counterpart;
+ * the reference keeps psi on the device between steps): x_in (2n doubles,
+ * solver order, may be NULL to continue from the device state) is copied in
+ * as by gade_solver_set_x, the step runs, and the new state is copied to
+ * x_out (may be NULL, may equal x_in).  The copy-out is queued with the
+ * step's convergence read-back, so a step that converges in one graph
+ * replay waits for the device once.  x_out is undefined on error. */
+int gade_solver_step_host(gade_solver *s, const double *x_in, const double *ft, int32_t maxit, double tol,
+                          double *x_out, gade_step_stats *stats);
 
 /* Sets the time-dependent radial tables for pulse factors ft without solving
  * (the pgsum part of gpu_compute_timedep_matrices, tools/gpu_solver.cu:50-82). */

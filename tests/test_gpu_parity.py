@@ -346,3 +346,35 @@ def test_partitions_give_deterministic_applies(workdirs, native_lib, name):
             assert np.array_equal(y, y3), (op, ns)
             assert _rel(y, sx + hx) < 1e-14, (op, ns)
     sol.close()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_step_host_matches_step_sequence(workdirs, native_lib, prec):
+    """gade_solver_step_host (state in and out through host memory, one
+    wait in the common case) gives the same bits as set_x + step + get_x,
+    also with the output aliasing the input and when continuing from the
+    device state (x_in NULL)."""
+    d, params, info, T, dt = _setup(workdirs, "tiny_nondipole")
+    prob = Problem(d, info["lmax"])
+    psi, _ = prob.psi0()
+    fts = [pulse(params["Intensity"], params["Omega"], params["Cycles"], t)
+           for _, t in step_times(T, params["Ntime"])[1][:6]]
+    tol = 1e-12 if prec == "fp64" else 1e-10
+    a = Solver(prob, dt, precision=prec)
+    b = Solver(prob, dt, precision=prec)
+    xa = psi.copy()
+    xb = psi.copy()
+    for k, ft in enumerate(fts):
+        if k < 3:
+            a.set_x(xa)
+            sb = b.step_host(xb, ft, maxit=500, tol=tol, x_out=xb)      # aliased in/out
+        else:
+            out = np.empty_like(xb)
+            sb = b.step_host(None, ft, maxit=500, tol=tol, x_out=out)   # continue on the device
+            xb = out
+        sa = a.step(ft, maxit=500, tol=tol)
+        xa = a.get_x()
+        assert sa["iters"] == sb["iters"], k
+        assert np.array_equal(xa, xb), k
+    a.close()
+    b.close()
