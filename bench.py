@@ -632,6 +632,8 @@ def profile_only(args):
         prob = native.Problem(d, info["lmax"])
         dt, steps = step_times(T, params["Ntime"])
         sol = native.Solver(prob, dt, 1.0, precision=args.profile_precision, device=0)
+        if args.operator != "auto":
+            sol.set_operator(1 if args.operator == "assembled" else 0)
         tol = TOL if args.profile_precision == "fp64" else 1e-10
         for k in range(args.warmup + args.steps):
             sol.step(pulse(params["Intensity"], params["Omega"], params["Cycles"], steps[k][1]), MAXIT, tol)
