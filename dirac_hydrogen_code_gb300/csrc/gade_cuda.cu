@@ -2182,13 +2182,13 @@ static int solver_create(const gade_problem *p, int npulse, const double *dts, c
         UP(s->d_FU, (const double2 *)nullptr, NP * s->fstride);
         if (s->rc) { double *g; UP(g, (const double *)nullptr, NP * s->gstride); s->d_g = g; UP(g, (const double *)nullptr, NP * s->gstride); s->d_gt = g; }
         else { double2 *g; UP(g, (const double2 *)nullptr, NP * s->gstride); s->d_g = g; UP(g, (const double2 *)nullptr, NP * s->gstride); s->d_gt = g; }
-        if (s->rc) { R4d *m; UP(m, (const R4d *)nullptr, NP * s->mstride); s->d_M = m; }
-        else { C4<double2> *m; UP(m, (const C4<double2> *)nullptr, NP * s->mstride); s->d_M = m; }
+        if (s->rc) { R4d *m = nullptr; UP(m, (const R4d *)nullptr, NP * s->mstride); s->d_M = m; }
+        else { C4<double2> *m = nullptr; UP(m, (const C4<double2> *)nullptr, NP * s->mstride); s->d_M = m; }
     }
     const bool mixed = precision == GADE_PREC_MIXED;
     if (mixed) {
-        if (s->rc) { R4f *m; UP(m, (const R4f *)nullptr, NP * s->mstride); s->d_M32 = m; }
-        else { C4<float2> *m; UP(m, (const C4<float2> *)nullptr, NP * s->mstride); s->d_M32 = m; }
+        if (s->rc) { R4f *m = nullptr; UP(m, (const R4f *)nullptr, NP * s->mstride); s->d_M32 = m; }
+        else { C4<float2> *m = nullptr; UP(m, (const C4<float2> *)nullptr, NP * s->mstride); s->d_M32 = m; }
         std::vector<float2> Sf((size_t)s->nk * WB);
         for (size_t e = 0; e < Sf.size(); e++) Sf[e] = make_float2((float)su->S_ell[e].re, (float)su->S_ell[e].im);
         float2 *d;
