@@ -4,9 +4,15 @@ Workload (N=1): the nondipole medium configuration — Z=1, rBox=30,
 NSplines=250, NKappa=8, NMu=4, Nl=0 (lmax 17), 3-cycle pulse Omega=50,
 E0=10, Ntime=1500, complex128, BiCGSTAB tolerance 1e-12; inputs generated
 in the reference file formats (synthetic: there is no dataset).  One "step"
-is one full CN step: per-step radial tables, rhs, preconditioned BiCGSTAB to
-tolerance.  Inputs stay resident in HBM for ``value``; ``e2e`` goes through
-the C ABI with the state copied from pinned host memory and back every step.
+is one full CN step: per-step operator (assembly or radial tables), rhs,
+preconditioned BiCGSTAB to tolerance.  The pulse is run whole (1501 steps);
+the K timed steps are sampled evenly across it after the W warm-up steps,
+so that they follow the envelope through its peak, and each is timed from
+the state the pulse reaches there (the steps between run untimed).  Inputs
+stay resident in HBM for ``value``; ``e2e`` goes through the C ABI with the
+state copied from pinned host memory and back every step.  The reference
+arm and the CPU baseline time the CPU restatement of the reference build on
+the same sampled steps, each from the pulse's own state there.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -117,33 +123,70 @@ def _gen(workdir: str):
     return params, info, T
 
 
-def cpu_reference_time(workdir, params, info, T, nsteps: int, warmup: int = 0):
-    """Per-step wall time of the CPU restatement of the reference build
-    (oracle port: the reference assembly, scipy CSR SpMV and SuperLU ILU
-    solves, BiCGSTAB of tools/bicgstab.c; one rank) over nsteps steps after
-    `warmup` untimed steps; set-up (reads, ILU factorisation) is excluded as
-    in the reference's own per-step timer.  Returns s/step."""
+def sample_positions(nsteps_pulse: int, k: int, warmup: int) -> list[int]:
+    """0-based indices of the k timed steps in the pulse's step order: the
+    steps after the `warmup` first ones cut into k equal strata, the middle
+    step of each, so that the sample follows the pulse envelope through its
+    peak."""
+    span = nsteps_pulse - warmup
+    if k < 1 or k > span:
+        raise ValueError(f"cannot sample {k} steps from {span} steps after {warmup} warm-up steps")
+    return [warmup + int((i + 0.5) * span / k) for i in range(k)]
+
+
+def timed_steps_text(k: int, m: int, w: int) -> str:
+    return (f"{k} CN steps sampled evenly across the {m}-step pulse after {w} warm-up steps (the middle step "
+            f"of each stratum of {(m - w) / k:.1f} steps), each from the state the pulse reaches there")
+
+
+def bench_config(info: dict, ws: int, k: int, m: int, w: int) -> dict:
+    """The workload description, identical in both arms."""
+    return {"workload": WORKLOAD, "N": info["n"], "nnz_equiv": info["nnz_full"], "lmax": info["lmax"], "tol": TOL,
+            "timed_steps": timed_steps_text(k, m, w),
+            "l2": "GPU arm: flushed (256 MB write) before every timed step, outside its events",
+            "parallelism": f"replicas x{ws}",
+            "iters_counting": "tools/bicgstab.c: the iteration that meets the tolerance is not counted"}
+
+
+def cpu_port_time(workdir, lmax: int, sample_file: str) -> float:
+    """Mean wall time of one CN step of the CPU restatement of the reference
+    build (oracle port: the reference assembly, scipy CSR SpMV and SuperLU
+    ILU solves, BiCGSTAB of tools/bicgstab.c; one rank) over the sampled
+    steps in sample_file (positions and the state each step starts from),
+    after one untimed warm-up step.  Set-up (reads, ILU factorisation) is
+    excluded, as in the reference's own per-step timer.  Returns s/step."""
+    import numpy as np
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
-    p = O.load_problem(workdir, info["lmax"])
-    _, recs, _ = O.run(workdir, T, info["lmax"], params["Intensity"], params["Omega"], params["Cycles"],
-                       params["Ntime"], tol=TOL, maxit=MAXIT, precond="ilu", max_steps=nsteps + warmup,
-                       problem=p)
-    timed = recs[warmup:]
-    return sum(r.elapsed for r in timed) / len(timed), T / params["Ntime"]
+    from dirac_hydrogen_code_gb300.gen import CONFIGS
+    params = CONFIGS[WORKLOAD]
+    T = params["Cycles"] * 2 * math.pi / params["Omega"]
+    p = O.load_problem(workdir, lmax)
+    S, Hst = O.stationary(p, T / params["Ntime"])
+    M = O.IluPrecond(S, Hst)
+    data = np.load(sample_file)
+    pos, states = data["positions"], data["states"]
+
+    def one(j, x):
+        _, recs, _ = O.run(workdir, T, lmax, params["Intensity"], params["Omega"], params["Cycles"],
+                           params["Ntime"], tol=TOL, maxit=MAXIT, start_iter=int(j) + 1, precond=M,
+                           max_steps=1, psi=x, problem=p)
+        return recs[0].elapsed
+    one(pos[0], states[0])
+    return sum(one(j, x) for j, x in zip(pos, states)) / len(pos)
 
 
 # one thread per CPU process (the throughput comparison runs one process per core)
 CPU_THREAD_ENV = {"OMP_NUM_THREADS": "1", "OPENBLAS_NUM_THREADS": "1", "MKL_NUM_THREADS": "1"}
 
 
-def cpu_processes(workdir, lmax: int, nsteps: int, warmup: int, nproc: int, one_thread: bool) -> list[float]:
-    """s/step of nproc concurrent oracle-port processes, each stepping its own
-    copy of the pulse in workdir (started together).  one_thread: BLAS and
-    OpenMP limited to one thread per process; else every host thread is
-    available to the port (its BLAS-threaded parts use them)."""
+def cpu_processes(workdir, lmax: int, sample_file: str, nproc: int, one_thread: bool) -> list[float]:
+    """s/step of nproc concurrent oracle-port processes, each timing the
+    sampled steps of sample_file on its own (started together).  one_thread:
+    BLAS and OpenMP limited to one thread per process; else every host thread
+    is available to the port (its BLAS-threaded parts use them)."""
     env = dict(os.environ, **CPU_THREAD_ENV) if one_thread else dict(os.environ)
-    cmd = [sys.executable, os.path.abspath(__file__), "--cpu-worker", workdir, str(lmax), str(nsteps), str(warmup)]
+    cmd = [sys.executable, os.path.abspath(__file__), "--cpu-worker", workdir, str(lmax), sample_file]
     procs = [subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.PIPE, env=env) for _ in range(nproc)]
     out = []
     for p in procs:
@@ -155,33 +198,80 @@ def cpu_processes(workdir, lmax: int, nsteps: int, warmup: int, nproc: int, one_
 
 
 def cpu_worker(argv) -> int:
-    workdir, lmax, nsteps, warmup = argv
-    from dirac_hydrogen_code_gb300.gen import CONFIGS
-    params = CONFIGS[WORKLOAD]
-    T = params["Cycles"] * 2 * math.pi / params["Omega"]
-    s, _ = cpu_reference_time(workdir, params, {"lmax": int(lmax)}, T, int(nsteps), warmup=int(warmup))
-    print(s)
+    workdir, lmax, sample_file = argv
+    print(cpu_port_time(workdir, int(lmax), sample_file))
     return 0
 
 
+def write_sample(path: str, positions, states) -> str:
+    import numpy as np
+    np.savez(path, positions=np.asarray(positions, np.int64), states=np.stack(states))
+    return path
+
+
+def gpu_states(workdir, info, fts, dt, positions, device=0):
+    """The state at the start of each listed step of the pulse, from the
+    plain FP64 GPU path (used only to give the CPU steps their starting
+    states; nothing of it is timed)."""
+    from dirac_hydrogen_code_gb300 import native
+    prob = native.Problem(workdir, info["lmax"])
+    sol = native.Solver(prob, dt, 1.0, precision="fp64", device=device)
+    psi, _ = prob.psi0()
+    sol.set_x(psi)
+    want, out = set(positions), {}
+    for j in range(max(positions) + 1):
+        if j in want:
+            out[j] = sol.get_x()
+        sol.step(fts[j], MAXIT, TOL)
+    sol.close()
+    prob.close()
+    return [out[j] for j in positions]
+
+
 def run_reference(args):
+    """The reference arm: the CPU restatement of the reference build (oracle
+    port) on the host cores, on the GPU arm's workload, config and sampled
+    steps; each timed step starts from the state the pulse reaches there
+    (from the FP64 GPU path when a GPU is present, else psi0)."""
     ws, rank, local = _dist()
     if rank != 0:
         return 0
+    import numpy as np
+    from dirac_hydrogen_code_gb300.cn import pulse, step_times
     with tempfile.TemporaryDirectory() as d:
         params, info, T = _gen(d)
-        s_per_step = cpu_processes(d, info["lmax"], args.steps, args.warmup, 1, False)[0]
+        dt, steps = step_times(T, params["Ntime"])
+        fts = [pulse(params["Intensity"], params["Omega"], params["Cycles"], t) for _, t in steps]
+        pos = sample_positions(len(fts), args.steps, args.warmup)
+        have_gpu = False
+        try:
+            import torch
+            have_gpu = torch.cuda.is_available()
+        except Exception:
+            pass
+        if have_gpu:
+            states = gpu_states(d, info, fts, dt, pos, device=local)
+            start = "the state the FP64 GPU path reaches there (computed beforehand, not timed)"
+        else:
+            from dirac_hydrogen_code_gb300.formats import vec_read
+            psi, _ = vec_read(os.path.join(d, "psi0.vec"))
+            states = [psi] * len(pos)
+            start = "psi0 (no GPU present to give the pulse's own states)"
+        sample = write_sample(os.path.join(d, "sample.npz"), pos, states)
+        s_per_step = cpu_processes(d, info["lmax"], sample, 1, False)[0]
+        cfg = bench_config(info, ws, args.steps, len(fts), args.warmup)
     v = 1.0 / s_per_step
     line = {
         "impl": "reference", "metric": METRIC, "value": v, "unit": "steps/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": s_per_step * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
         "data": "synthetic (generated dumpCouplings inputs)",
-        "config": {"workload": WORKLOAD, "N": info["n"], "nnz_equiv": info["nnz_full"], "tol": TOL},
+        "config": cfg,
         "cpu_baseline": {"value": v, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
-                         "sample": f"{args.steps} CN steps of {WORKLOAD} after {args.warmup} warm-up steps; "
-                                   "one process (one reference rank) with every host thread available "
-                                   "to its BLAS-threaded parts; SpMV and SuperLU solves single-threaded"},
+                         "sample": f"{timed_steps_text(args.steps, len(fts), args.warmup)}; each step starts from "
+                                   f"{start}; one untimed warm-up step; one process (one reference rank) with "
+                                   "every host thread available to its BLAS-threaded parts; SpMV and SuperLU "
+                                   "solves single-threaded"},
         "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -196,6 +286,68 @@ def max_over_ranks(t_local: float, dist, device: str) -> float:
     tt = torch.tensor([t_local], dtype=torch.float64, device=device if dist.get_backend() == "nccl" else "cpu")
     dist.all_reduce(tt, op=dist.ReduceOp.MAX)
     return float(tt.item())
+
+
+def walk(sol, fts, positions, tol, stream, l2_flush, torch, states=False, kernel_times=False, quality_at=None):
+    """One whole pulse on `sol` (restarted from psi0 by the caller): every
+    step's device time with CUDA events on the solver's stream, the L2
+    flushed before each step listed in `positions` (outside its events).
+    states: keep the state each listed step starts from.  kernel_times: the
+    solver's per-kernel event times (direct launches) summed over the listed
+    steps.  quality_at: a step after which the true residual of the step is
+    measured (outside every timed region).  Returns a dict."""
+    import numpy as np
+    want = set(positions)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in fts]
+    out = {"iters": [], "records": [], "states": {}, "launches": 0, "quality": None}
+    kt_sum = {}
+    if kernel_times:
+        sol.profile(True)
+    for j, ft in enumerate(fts):
+        if j in want:
+            if states:
+                out["states"][j] = sol.get_x()
+            with torch.cuda.stream(stream):
+                l2_flush.add_(1.0)
+            if kernel_times:
+                sol.kernel_times()                     # waits for the device and resets the sums
+            l0 = sol.launch_count()
+        x_prev = sol.get_x() if j == quality_at else None
+        with torch.cuda.stream(stream):
+            ev[j][0].record(stream)
+        st = sol.step(ft, MAXIT, tol)
+        with torch.cuda.stream(stream):
+            ev[j][1].record(stream)
+        if j in want:
+            out["launches"] += sol.launch_count() - l0
+            if kernel_times:
+                for k, v in sol.kernel_times().items():
+                    kt_sum[k] = kt_sum.get(k, 0) + v
+        if x_prev is not None:
+            x_new = sol.get_x()
+            _, sxp, hxp = sol.apply(x_prev, parts=True)
+            b_rhs = sxp - hxp
+            out["quality"] = {"step": j + 1, "true_residual": float(np.linalg.norm(b_rhs - sol.apply(x_new))
+                                                                     / np.linalg.norm(b_rhs)),
+                              "recursive_residual": float(st["tol_error"]), "iters": int(st["iters"])}
+        out["iters"].append(int(st["iters"]))
+        out["records"].append(st)
+    torch.cuda.synchronize()
+    if kernel_times:
+        sol.profile(False)
+    ms = [a.elapsed_time(b) for a, b in ev]
+    out["ms"] = ms
+    out["ms_timed"] = sum(ms[j] for j in positions)
+    out["ms_pulse"] = sum(ms)
+    out["kt"] = kt_sum
+    return out
+
+
+def iteration_histogram(iters) -> dict:
+    h = {}
+    for v in iters:
+        h[str(v)] = h.get(str(v), 0) + 1
+    return dict(sorted(h.items(), key=lambda kv: int(kv[0])))
 
 
 def run_ours(args):
@@ -227,95 +379,87 @@ def run_ours(args):
                  "balanced_ctas": bal["segments"], "balanced_pieces": bal["pieces"],
                  "balanced_gather_weight": bal["gather_weight"]}
     psi, _ = prob.psi0()
-    sol.set_x(psi)
     stream = torch.cuda.ExternalStream(sol.stream(), device=device)
     l2_flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{device}")
     fts = [pulse(params["Intensity"], params["Omega"], params["Cycles"], t) for _, t in steps]
+    M = len(fts)
+    pos = sample_positions(M, args.steps, args.warmup)
 
     def barrier():
         if dist is not None:
             dist.barrier()
         torch.cuda.synchronize(device)
 
-    # warm-up
-    idx = 0
-    for _ in range(args.warmup):
-        sol.step(fts[idx % len(fts)], MAXIT, TOL)
-        idx += 1
-    # timed region: device time of each step with events on the solver stream;
-    # L2 flushed between steps outside the events
+    # timed region: the sampled steps of one whole pulse (the warm-up steps
+    # and the steps between the samples run untimed), device time of each
+    # with CUDA events on the solver's stream
     hbm_peak, peak_kind = _peaks()
     clocks = Clocks(device)
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    iters = []
+    sol.restart(psi)
     barrier()
     clocks.start()
-    launches0 = sol.launch_count()
-    for k in range(args.steps):
-        with torch.cuda.stream(stream):
-            l2_flush.add_(1.0)
-            ev[k][0].record(stream)
-        st = sol.step(fts[idx % len(fts)], MAXIT, TOL)
-        with torch.cuda.stream(stream):
-            ev[k][1].record(stream)
-        iters.append(st["iters"])
-        idx += 1
+    w1 = walk(sol, fts, pos, TOL, stream, l2_flush, torch, states=True)
     barrier()
-    launches = sol.launch_count() - launches0
     clk = clocks.stop()
-    # per-kernel device times: a separate pass with event pairs around every
-    # launch (direct launches; the timed steps above replay captured graphs)
-    sol.profile(True)
-    for k in range(args.steps):
-        with torch.cuda.stream(stream):
-            l2_flush.add_(1.0)
-        sol.step(fts[idx % len(fts)], MAXIT, TOL)
-        idx += 1
-    barrier()
-    kt = sol.kernel_times()
-    sol.profile(False)
-    ms = sum(a.elapsed_time(b) for a, b in ev)
-    t_local = max_over_ranks(ms / 1e3, dist, f"cuda:{device}")
+    launches = w1["launches"]
+    t_local = max_over_ranks(w1["ms_timed"] / 1e3, dist, f"cuda:{device}")
     value = ws * args.steps / t_local
+    x_end = sol.get_x()
 
-    # e2e through the C ABI with pinned host buffers
+    # per-kernel device times of the sampled steps: a second pulse with event
+    # pairs around every launch (direct launches; the timed steps above replay
+    # captured graphs), and the step quality near the pulse peak
+    sol.restart(psi)
+    mid = pos[len(pos) // 2]
+    w2 = walk(sol, fts, pos, TOL, stream, l2_flush, torch, kernel_times=True, quality_at=mid)
+    kt = w2["kt"]
+
+    # e2e through the C ABI with pinned host buffers: one gade_solver_step_host
+    # call per step, the state in from and out to the pinned host buffer, the
+    # pulse factors from host memory; the sampled steps timed on the host
     n = prob.n
     hx = torch.empty(2 * n, dtype=torch.float64, pin_memory=True)
-    hx.numpy()[:] = sol.get_x().view(np.float64)
+    hx.numpy()[:] = psi.view(np.float64)
     lib = native.load_library()
     h = sol._h
     ptr = hx.data_ptr()
-    # one C-ABI call per step: the state in from and out to the pinned host
-    # buffer (gade_solver_step_host), the pulse factors from host memory
-    fts_host = [np.ascontiguousarray(fts[(idx + k) % len(fts)], dtype=np.complex128) for k in range(args.steps)]
+    fts_host = [np.ascontiguousarray(f, dtype=np.complex128) for f in fts]
     st_host = native.StepStats()
+    sol.restart(psi)
+    want = set(pos)
+    te = 0.0
     barrier()
-    t0 = time.perf_counter()
-    for k in range(args.steps):
-        native._check(lib.gade_solver_step_host(h, ptr, fts_host[k].ctypes.data, MAXIT, TOL, ptr,
-                                                native.C.byref(st_host)))
-    idx += args.steps
+    for j in range(M):
+        if j in want:
+            with torch.cuda.stream(stream):
+                l2_flush.add_(1.0)
+            torch.cuda.synchronize(device)
+            t0 = time.perf_counter()
+            native._check(lib.gade_solver_step_host(h, ptr, fts_host[j].ctypes.data, MAXIT, TOL, ptr,
+                                                    native.C.byref(st_host)))
+            te += time.perf_counter() - t0
+        else:
+            native._check(lib.gade_solver_step_host(h, ptr, fts_host[j].ctypes.data, MAXIT, TOL, ptr,
+                                                    native.C.byref(st_host)))
     barrier()
-    te = max_over_ranks(time.perf_counter() - t0, dist, f"cuda:{device}")
+    te = max_over_ranks(te, dist, f"cuda:{device}")
     e2e = ws * args.steps / te
 
-    # step quality after the timed steps (outside every timed region): the
-    # true residual |b - A x_{n+1}| / |b| of one more step, its recursive
-    # residual, and the drift of the S-norm psi^H S psi from psi0's
-    x_prev = sol.get_x()
-    st_q = sol.step(fts[idx % len(fts)], MAXIT, TOL)
-    idx += 1
-    x_new = sol.get_x()
-    _, sxp, hxp = sol.apply(x_prev, parts=True)
-    b_rhs = sxp - hxp
-    true_res = float(np.linalg.norm(b_rhs - sol.apply(x_new)) / np.linalg.norm(b_rhs))
-    _, sx_new, _ = sol.apply(x_new, parts=True)
+    # S-norm drift of the whole pulse: psi^H S psi at the end against psi0's
+    _, sx_end, _ = sol.apply(x_end, parts=True)
     _, s_psi0, _ = sol.apply(psi, parts=True)
     sn0 = float(np.vdot(psi, s_psi0).real)
-    quality = {"true_residual": true_res, "recursive_residual": float(st_q["tol_error"]),
-               "steps_taken": idx, "snorm_drift_rel": abs(float(np.vdot(x_new, sx_new).real) - sn0) / sn0}
+    pulse_info = {
+        "steps": M, "iters_histogram": iteration_histogram(w1["iters"]),
+        "timed_positions": [j + 1 for j in pos], "timed_iters": [w1["iters"][j] for j in pos],
+        "whole_pulse_device_s": w1["ms_pulse"] / 1e3, "whole_pulse_steps_per_s": M / (w1["ms_pulse"] / 1e3),
+        "whole_pulse_note": "device time of every step of the pulse, L2 flushed only before the sampled steps",
+        "snorm_drift_rel_at_end": abs(float(np.vdot(x_end, sx_end).real) - sn0) / sn0,
+        "step_quality_near_peak": w2["quality"],
+        "operator_partition": partition,
+    }
 
-    # roofline of the dominant kernel (matrix-free operator)
+    # roofline of the dominant kernel (the operator apply)
     apply_ms = kt["apply_ms"] / max(kt["apply_launches"], 1)
     nnz = info["nnz_full"]
     N = info["n"]
@@ -333,11 +477,11 @@ def run_ours(args):
         "kernel": ("k_apply_asm (S + H(t) apply with this step's assembled real coupling values)" if assembled
                    else "k_apply (matrix-free S + H(t) apply)"),
         "note": ("achieved = CSR-equivalent bytes of the reference assembled complex128 SpMV "
-                 "(20 nnz + 4(N+1) + 32N) / average operator apply time; the kernel stores real coupling "
-                 "values (8 B) and is bound by the FP64 pipe, see fp64" if assembled else
+                 "(20 nnz + 4(N+1) + 32N) / average operator apply time over the sampled steps; the kernel "
+                 "stores real coupling values (8 B) and is bound by the FP64 pipe, see fp64" if assembled else
                  "achieved = CSR-equivalent bytes of the reference assembled complex128 SpMV "
-                 "(20 nnz + 4(N+1) + 32N) / average k_apply time; the matrix-free kernel moves far "
-                 "fewer bytes and is bound by the FP64 pipe, see fp64"),
+                 "(20 nnz + 4(N+1) + 32N) / average k_apply time over the sampled steps; the matrix-free "
+                 "kernel moves far fewer bytes and is bound by the FP64 pipe, see fp64"),
         "operator": opinfo,
         "assembly_per_step": {"kernel": "k_assemble", "flops": asm_flops, "bytes": asm_bytes} if assembled else None,
         "fp64": {"achieved_tflops": mf_flops / (apply_ms * 1e-3) / 1e12, "peak_tflops": fp64_peak,
@@ -358,29 +502,33 @@ def run_ours(args):
     variants = None
     if rank == 0 and not args.no_variants:
         variants = {"single_pulse_precision": mixed_variant(prob, params, info, T, args, device, torch, native,
-                                                            psi, fts, l2_flush)}
+                                                            psi, fts, pos, l2_flush)}
         if not args.no_batch:
             variants["batch64"] = batch_variant(prob, params, args, torch)
         if not args.no_learned:
             variants["learned_nkappa16"] = learned_variant(args, torch)
 
-    # CPU baseline on a bounded sample (rank 0, N=1)
+    # CPU baseline on a bounded sample of the same sampled steps (rank 0, N=1),
+    # each from the state the GPU pulse reached there
     cpu = None
     if rank == 0 and ws == 1 and not args.no_cpu:
-        s_per_step = cpu_processes(tmp.name, info["lmax"], args.cpu_steps, 1, 1, False)[0]
+        every = max(1, len(pos) // args.cpu_steps)
+        cpos = pos[every // 2::every][:args.cpu_steps]
+        sample = write_sample(os.path.join(tmp.name, "cpu_sample.npz"), cpos, [w1["states"][j] for j in cpos])
+        s_per_step = cpu_processes(tmp.name, info["lmax"], sample, 1, False)[0]
         cpu = {"value": 1.0 / s_per_step, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": f"{args.cpu_steps} CN steps of {WORKLOAD} after 1 warm-up step (oracle port: "
-                         "reference assembly, scipy CSR SpMV, SuperLU ILU, BiCGSTAB at tol 1e-12; one "
-                         "process (one reference rank) with every host thread available to its "
-                         "BLAS-threaded parts)"}
+               "sample": f"{len(cpos)} of the timed steps (pulse steps {[j + 1 for j in cpos]}), each from the "
+                         "state the GPU pulse reached there, after one untimed warm-up step (oracle port: "
+                         "reference assembly, scipy CSR SpMV, SuperLU ILU, BiCGSTAB at tol 1e-12; one process "
+                         "(one reference rank) with every host thread available to its BLAS-threaded parts)"}
         if variants is not None and "batch64" in variants:
             # throughput comparison for the batch: one single-threaded process per host core
             nproc = os.cpu_count() or 1
-            per = cpu_processes(tmp.name, info["lmax"], args.cpu_steps, 1, nproc, True)
+            per = cpu_processes(tmp.name, info["lmax"], sample, nproc, True)
             variants["batch64"]["cpu_aggregate"] = {
                 "value": sum(1.0 / x for x in per), "unit": "pulse-steps/s", "processes": nproc, "cores": nproc,
-                "kind": "port", "sample": f"{nproc} concurrent single-threaded processes, each {args.cpu_steps} "
-                                          f"CN steps of one {WORKLOAD} pulse after 1 warm-up step"}
+                "kind": "port", "sample": f"{nproc} concurrent single-threaded processes, each timing the "
+                                          f"{len(cpos)} CN steps of the CPU baseline's sample"}
 
     if rank == 0:
         line = {
@@ -388,17 +536,13 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": t_local * 1e3 / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c128",
             "data": "synthetic (generated dumpCouplings inputs)",
-            "config": {"workload": WORKLOAD, "N": N, "nnz_equiv": nnz, "lmax": info["lmax"], "tol": TOL,
-                       "l2": "flushed (256 MB write) between timed steps", "parallelism": f"replicas x{ws}",
-                       "iters_per_step": sorted(set(iters)),
-                       "iters_counting": "tools/bicgstab.c: the iteration that meets the tolerance is not counted",
-                       "step_quality": quality,
-                       "operator_partition": partition},
+            "config": bench_config(info, ws, args.steps, M, args.warmup),
             "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": 16 * N, "d2h_bytes_per_step": 16 * N},
             "gpu_launches": launches,
             "roofline": roof,
             "cpu_baseline": cpu,
             "clocks": clk,
+            "pulse": pulse_info,
             "variants": variants,
         }
         print(json.dumps(line))
@@ -410,57 +554,32 @@ def run_ours(args):
     return 0
 
 
-def _timed_steps(sol, fts, idx, steps, warmup, tol, stream, l2_flush, torch):
-    """Warm-up then `steps` CN steps timed with CUDA events on the solver's
-    stream (L2 flushed between steps, outside the events), then `steps` more
-    with per-kernel event timing.  Returns (ms_total, records, next index,
-    kernel times)."""
-    for _ in range(warmup):
-        sol.step(fts[idx % len(fts)], MAXIT, tol)
-        idx += 1
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
-    recs = []
-    torch.cuda.synchronize()
-    for k in range(steps):
-        with torch.cuda.stream(stream):
-            l2_flush.add_(1.0)
-            ev[k][0].record(stream)
-        recs.append(sol.step(fts[idx % len(fts)], MAXIT, tol))
-        with torch.cuda.stream(stream):
-            ev[k][1].record(stream)
-        idx += 1
-    torch.cuda.synchronize()
-    # per-kernel times from a separate pass (event pairs around direct launches)
-    sol.profile(True)
-    for k in range(steps):
-        sol.step(fts[idx % len(fts)], MAXIT, tol)
-        idx += 1
-    torch.cuda.synchronize()
-    kt = sol.kernel_times()
-    sol.profile(False)
-    return sum(a.elapsed_time(b) for a, b in ev), recs, idx, kt
-
-
-def mixed_variant(prob, params, info, T, args, device, torch, native, psi, fts, l2_flush):
+def mixed_variant(prob, params, info, T, args, device, torch, native, psi, fts, positions, l2_flush):
     """Mixed precision (complex64 inner BiCGSTAB in FP64 refinement) against
-    plain FP64, both from psi0 over the same warm-up + timed steps at the
-    refinement tolerance 1e-10; error = relative S-norm and L2 of the final
-    state against the plain FP64 run at the configuration's tolerance."""
+    plain FP64, each over the whole pulse from psi0, timed on the sampled
+    steps like the headline, at the refinement tolerance 1e-10; errors of the
+    final state (relative S-norm and L2, populations) against the plain FP64
+    run at the configuration's tolerance."""
     import numpy as np
     from dirac_hydrogen_code_gb300.cn import step_times
     dt, _ = step_times(T, params["Ntime"])
-    out = {}
+    out = {"timed_steps": timed_steps_text(len(positions), len(fts), args.warmup)}
     finals = {}
     for tag, prec, tol in (("fp64", "fp64", TOL), ("fp64_tol1e-10", "fp64", 1e-10), ("mixed_tol1e-10", "mixed", 1e-10)):
         sol = native.Solver(prob, dt, 1.0, precision=prec, device=device)
-        sol.set_x(psi)
+        sol.restart(psi)
         stream = torch.cuda.ExternalStream(sol.stream(), device=device)
-        ms, recs, _, kt = _timed_steps(sol, fts, 0, args.steps, args.warmup, tol, stream, l2_flush, torch)
+        w = walk(sol, fts, positions, tol, stream, l2_flush, torch)
         finals[tag] = sol.get_x()
-        out[tag] = {"steps_per_s": args.steps / (ms / 1e3), "ms_per_step": ms / args.steps,
+        sol.restart(psi)
+        kt = walk(sol, fts, positions, tol, stream, l2_flush, torch, kernel_times=True)["kt"]
+        recs = [w["records"][j] for j in positions]
+        k = len(positions)
+        out[tag] = {"steps_per_s": k / (w["ms_timed"] / 1e3), "ms_per_step": w["ms_timed"] / k,
+                    "whole_pulse_steps_per_s": len(fts) / (w["ms_pulse"] / 1e3),
                     "inner_iters_per_step": float(np.mean([r["inner_iters"] for r in recs])),
                     "fp64_residual_passes_per_step": float(np.mean([r["refinements"] for r in recs])),
-                    "kernel_ms_per_step": {k: round(v / args.steps, 4) for k, v in kt.items() if k.endswith("_ms")}}
+                    "kernel_ms_per_step": {kk: round(v / k, 4) for kk, v in kt.items() if kk.endswith("_ms")}}
         sol.close()
     ref = finals["fp64"]
     eb = _eigenbasis(prob)
@@ -474,8 +593,9 @@ def mixed_variant(prob, params, info, T, args, device, torch, native, psi, fts, 
     for tag in ("fp64_tol1e-10", "mixed_tol1e-10"):
         e = finals[tag] - ref
         _, se, _ = chk.apply(e, parts=True)
-        out[tag]["err_vs_fp64"] = {"s_norm_rel": float(np.sqrt(abs(np.vdot(e, se).real) / abs(np.vdot(ref, sref).real))),
-                                   "l2_rel": float(np.linalg.norm(e) / np.linalg.norm(ref))}
+        out[tag]["err_vs_fp64_whole_pulse"] = {
+            "s_norm_rel": float(np.sqrt(abs(np.vdot(e, se).real) / abs(np.vdot(ref, sref).real))),
+            "l2_rel": float(np.linalg.norm(e) / np.linalg.norm(ref))}
     chk.close()
     out["speedup_mixed_vs_fp64_at_1e-10"] = out["mixed_tol1e-10"]["steps_per_s"] / out["fp64_tol1e-10"]["steps_per_s"]
     return out
@@ -648,7 +768,7 @@ def profile_only(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-steps", type=int, default=4)

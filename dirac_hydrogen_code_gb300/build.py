@@ -57,6 +57,18 @@ def solver_path() -> str:
     return os.path.join(LIB, "dirac_solver")
 
 
+def is_stale() -> bool:
+    """True when the library or the executable is missing or older than a
+    source file or header."""
+    outs = [library_path(), solver_path()]
+    if not all(os.path.exists(o) for o in outs):
+        return True
+    built = min(os.path.getmtime(o) for o in outs)
+    srcs = [os.path.join(CSRC, f) for f in os.listdir(CSRC)] + \
+        [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]
+    return any(os.path.getmtime(f) > built for f in srcs)
+
+
 def build(verbose: bool = False) -> str:
     os.makedirs(LIB, exist_ok=True)
     nvcc = _nvcc()

@@ -21,7 +21,7 @@ from .native import Problem, Solver
 
 
 def pulse(E0: float, omega: float, cycles: float, t: float) -> np.ndarray:
-    """beoyndDipolePulse_axialPart (tools/solver_common.c:103-122)."""
+    """beoyndDipolePulse_axialPart (tools/solver_common.c:53-65)."""
     T = cycles * 2 * math.pi / omega
     phi = -math.pi / 2
     a, b = E0 / (4 * omega), E0 / (2 * omega)
@@ -52,11 +52,15 @@ def run(workdir: str, maxtime: float, lmax: int, E0: float, omega: float, cycles
         ntime: float, tol: float = 1e-16, maxit: int = 500, start_iter: int = 1,
         precision: str = "fp64", device: int = 0, max_steps: int | None = None,
         write_outputs: bool = True, problem: Problem | None = None, x0: np.ndarray | None = None,
-        callback=None):
-    """Returns (x, records, solver) with x in the solver (permuted) order."""
+        callback=None, operator: int | None = None):
+    """Returns (x, records, solver) with x in the solver (permuted) order.
+    ``operator``: force the matrix-free (0) or assembled (1) operator
+    instead of the one chosen by timing at creation."""
     prob = problem if problem is not None else Problem(workdir, lmax)
     dt, steps = step_times(maxtime, ntime, start_iter)
     solver = Solver(prob, dt, 1.0, precision=precision, device=device)
+    if operator is not None:
+        solver.set_operator(operator)
     psi, xperm = prob.psi0()
     solver.set_x(psi if x0 is None else x0)
     nslots = int(ntime) + 4

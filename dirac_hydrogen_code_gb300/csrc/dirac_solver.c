@@ -38,7 +38,7 @@ static double now_us(void)
     return tv.tv_sec * 1e6 + tv.tv_usec;
 }
 
-/* beoyndDipolePulse_axialPart, tools/solver_common.c:110-122 */
+/* beoyndDipolePulse_axialPart, tools/solver_common.c:53-65 */
 static void pulse(double E0, double omega, double T, double t, double *ft)
 {
     const double phi = -M_PI / 2;

@@ -1232,6 +1232,8 @@ struct PcT {
     long long vstride;             /* complex elements per pulse of every vector */
     size_t fstride;                /* complex elements per pulse of FL / FU */
     int pred;                      /* PRED_* */
+    unsigned spin_limit;           /* polls of a stage wait before the kernel gives up */
+    int withhold;                  /* failure injection: stage whose copy is not issued (-1: none) */
 };
 
 __device__ __forceinline__ unsigned smem_u32(const void *p)
@@ -1353,7 +1355,7 @@ __global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const type
         const C *src;
         int cnt;
         const unsigned bytes = stage(0, &src, &cnt);
-        tma_bulk_load(stg, src, bytes, &bar[0]);
+        if (Q.withhold != 0) tma_bulk_load(stg, src, bytes, &bar[0]);
         all_ok = 1;
     }
 
@@ -1392,7 +1394,7 @@ __global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const type
 
     int k = 0;
     for (; k < ns; k++) {
-        if (tid == 0 && k + 1 < ns) {
+        if (tid == 0 && k + 1 < ns && k + 1 != Q.withhold) {
             const C *src;
             int cnt;
             const unsigned bytes = stage(k + 1, &src, &cnt);
@@ -1401,7 +1403,7 @@ __global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const type
         unsigned spins = 0;
         bool ok = true;
         while (!mbar_try_wait(&bar[k & 1], (k >> 1) & 1)) {
-            if (++spins > MBAR_SPIN_LIMIT) { ok = false; break; }
+            if (++spins > Q.spin_limit) { ok = false; break; }
         }
         if (!ok) all_ok = 0;
         __syncthreads();
@@ -1463,8 +1465,10 @@ __global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const type
     if (!all_ok) {
         if (tid == 0) {
             atomicOr(&sc->err, 1u);
-            /* drain the copies still in flight (bounded) before exiting */
+            /* drain the copies still in flight (bounded) before exiting: the
+               stage that timed out and the next one, both issued unless withheld */
             for (int k2 = k; k2 < k + 2 && k2 < ns; k2++) {
+                if (k2 == Q.withhold) continue;
                 unsigned spins = 0;
                 while (!mbar_try_wait(&bar[k2 & 1], (k2 >> 1) & 1) && ++spins < MBAR_SPIN_LIMIT) {
                 }
@@ -1757,6 +1761,8 @@ struct gade_solver {
     double asmb_flops, asmb_bytes;        /* one step's assembly */
     float mf_ms;                /* best timed matrix-free apply */
     float tab_ms[2];            /* timed step tables: matrix-free radial tables, assembly */
+    unsigned pc_wait;           /* polls of a preconditioner stage wait (0: MBAR_SPIN_LIMIT) */
+    int pc_withhold;            /* failure injection: preconditioner stage whose copy is withheld (-1: none) */
 };
 
 static int solver_engine_step(gade_solver *s, const double *ft, int32_t maxit, double tol, gade_step_stats *stats,
@@ -2096,6 +2102,7 @@ static int solver_create(const gade_problem *p, int npulse, const double *dts, c
     }
 
     gade_solver *s = new gade_solver();
+    s->pc_withhold = -1;
     s->device = device;
     s->prec = precision;
     s->rc = p->real_coupling;
@@ -2877,6 +2884,8 @@ static PcT pc_params(const gade_solver *s, const void *FL, const void *FU, int p
     Q.nblk = s->nblk; Q.B = s->B; Q.Bp = s->Bp; Q.nch = s->nch;
     Q.row_kidx = s->d_row_kidx; Q.ord = s->d_ord; Q.FL = FL; Q.FU = FU;
     Q.plist = s->d_plist; Q.vstride = s->n; Q.fstride = s->fstride; Q.pred = pred;
+    Q.spin_limit = s->pc_wait ? s->pc_wait : MBAR_SPIN_LIMIT;
+    Q.withhold = s->pc_withhold;
     return Q;
 }
 
@@ -3924,6 +3933,8 @@ static void batch_adapt(gade_batch *b, int kmax)
 
 /* Mixed-precision step of the listed pulses: the refinement of the
    single-pulse mixed step, with its tests in the reduction epilogues. */
+static int clear_workspace(gade_solver *s, int k);
+
 static int batch_step_mixed(gade_batch *b, const std::vector<int> &list, int32_t maxit, double tol,
                             gade_step_stats *stats)
 {
@@ -3959,6 +3970,7 @@ static int batch_step_mixed(gade_batch *b, const std::vector<int> &list, int32_t
             if (a.err | in.err) {
                 CK(cudaMemsetAsync(&s->d_sc[k].err, 0, sizeof(unsigned), s->stream));
                 CK(cudaMemsetAsync(&s->d_sc2[k].err, 0, sizeof(unsigned), s->stream));
+                if ((rc = clear_workspace(s, k))) return rc;
                 return fail(GADE_ERR_CUDA, "pulse %d: device wait timed out (flags %u): TMA copy did not complete",
                             k, a.err | in.err);
             }
@@ -4012,6 +4024,52 @@ static int batch_step_mixed(gade_batch *b, const std::vector<int> &list, int32_t
 
 static int batch_step_fp64(gade_batch *b, const std::vector<int> &list, int32_t maxit, double tol,
                            gade_step_stats *stats);
+
+/* After a step that ended on a device wait limit the vectors of pulse k are
+   partial; BiCGSTAB's p and v, which carry over from one step to the next
+   (tools/bicgstab.c:28-31), are cleared as after creation so that the next
+   step from a state set by the caller is that of a new solver. */
+static int clear_workspace(gade_solver *s, int k)
+{
+    const size_t off = (size_t)k * s->n, bytes = sizeof(double2) * (size_t)s->n;
+    if (s->p) CK(cudaMemsetAsync(s->p + off, 0, bytes, s->stream));
+    if (s->v) CK(cudaMemsetAsync(s->v + off, 0, bytes, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
+    return GADE_OK;
+}
+
+extern "C" int gade_solver_restart(gade_solver *s, const double *x, int64_t n)
+{
+    int rc = gade_solver_set_x(s, x, n);
+    if (rc) return rc;
+    if (s->xprev) CK(cudaMemsetAsync(s->xprev, 0, sizeof(double2) * (size_t)s->n, s->stream));
+    return clear_workspace(s, 0);
+}
+
+extern "C" int gade_solver_set_wait_limit(gade_solver *s, uint32_t polls)
+{
+    if (!s) return fail(GADE_ERR_ARG, "gade_solver_set_wait_limit: NULL solver");
+    s->pc_wait = polls;
+    if (s->engine) batch_drop_graphs(s->engine);   /* the graphs hold the old kernel parameters */
+    return GADE_OK;
+}
+
+extern "C" int gade_solver_inject_wait_timeout(gade_solver *s, int32_t stage)
+{
+    if (!s) return fail(GADE_ERR_ARG, "gade_solver_inject_wait_timeout: NULL solver");
+    if (stage < -1) return fail(GADE_ERR_ARG, "gade_solver_inject_wait_timeout: stage must be >= -1");
+    s->pc_withhold = stage;
+    if (s->engine) batch_drop_graphs(s->engine);
+    return GADE_OK;
+}
+
+extern "C" int gade_batch_set_wait_limit(gade_batch *b, uint32_t polls)
+{
+    if (!b) return fail(GADE_ERR_ARG, "gade_batch_set_wait_limit: NULL batch");
+    b->s->pc_wait = polls;
+    batch_drop_graphs(b);
+    return GADE_OK;
+}
 
 extern "C" int gade_batch_step(gade_batch *b, const int32_t *active, const double *ft, int32_t maxit, double tol,
                                gade_step_stats *stats)
@@ -4073,6 +4131,7 @@ static int batch_step_fp64(gade_batch *b, const std::vector<int> &list, int32_t 
             const DevScal &d = s->h_sc[k];
             if (d.err) {
                 CK(cudaMemsetAsync(&s->d_sc[k].err, 0, sizeof(unsigned), s->stream));
+                if ((rc = clear_workspace(s, k))) return rc;
                 return fail(GADE_ERR_CUDA, "pulse %d: device wait timed out (flags %u): TMA copy did not complete", k, d.err);
             }
             if (d.state == ST_BAD) return fail(GADE_ERR_NUMERIC, "pulse %d: BiCGSTAB residual became non-finite at iteration %d", k, d.iter);

@@ -89,7 +89,7 @@ int gade_problem_transpose_map(const gade_problem *p, int32_t *tpos);
 /* 1 when the radial tables g (loader layout) have the DKB zero blocks */
 int gade_dkb_zero(const gade_problem *p, const gc64 *g);
 
-/* kappa of an angular index, tools/solver_common.c:87-94 */
+/* kappa of an angular index, tools/solver_common.c:30-37 */
 int gade_ik(int i);
 
 #ifdef __cplusplus

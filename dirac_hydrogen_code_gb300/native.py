@@ -109,6 +109,10 @@ _SIGS = {
     "gade_batch_state_device": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_int64)]),
     "gade_batch_guess_buffer": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_int64)]),
     "gade_batch_use_guess": (C.c_int, [C.c_void_p, C.c_int32]),
+    "gade_solver_set_wait_limit": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "gade_solver_restart": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),
+    "gade_solver_inject_wait_timeout": (C.c_int, [C.c_void_p, C.c_int32]),
+    "gade_batch_set_wait_limit": (C.c_int, [C.c_void_p, C.c_uint32]),
 }
 
 # include/gade_learned.h (device pointers as integers)
@@ -230,6 +234,14 @@ class Solver:
         _check(load_library().gade_solver_get_x(self._h, x.ctypes.data, self.n))
         return x
 
+    def restart(self, x: np.ndarray):
+        """New pulse on this solver: state x, nothing carried over from the
+        previous steps (BiCGSTAB's p and v, the extrapolation history)."""
+        x = _cbuf(x)
+        if x.shape != (self.n,):
+            raise ValueError(f"state must have {self.n} entries")
+        _check(load_library().gade_solver_restart(self._h, x.ctypes.data, self.n))
+
     # pgsum part of gpu_compute_timedep_matrices
     def set_time(self, ft: np.ndarray):
         ft = _cbuf(ft)
@@ -347,6 +359,16 @@ class Solver:
     def set_operator(self, assembled: int):
         _check(load_library().gade_solver_set_operator(self._h, int(assembled)))
 
+    def set_wait_limit(self, polls: int = 0):
+        """Polls of each preconditioner stage wait before the step gives up
+        with GADE_ERR_CUDA (0: the default)."""
+        _check(load_library().gade_solver_set_wait_limit(self._h, int(polls)))
+
+    def inject_wait_timeout(self, stage: int = -1):
+        """Tests of the failure path: the preconditioner kernel withholds the
+        copy of this stage so that its wait runs out (-1: off)."""
+        _check(load_library().gade_solver_inject_wait_timeout(self._h, int(stage)))
+
     def assembly_cost(self) -> tuple[float, float]:
         """(FP64 flops, compulsory DRAM bytes) of one step's coupling assembly."""
         f, b = C.c_double(), C.c_double()
@@ -462,6 +484,9 @@ class Batch:
 
     def set_operator(self, assembled: int):
         _check(load_library().gade_batch_set_operator(self._h, int(assembled)))
+
+    def set_wait_limit(self, polls: int = 0):
+        _check(load_library().gade_batch_set_wait_limit(self._h, int(polls)))
 
     def state_device(self) -> tuple[int, int]:
         """(device address of the pulse states, per-pulse stride in complex elements)."""

@@ -69,7 +69,7 @@ int gade_problem_get_psi0(const gade_problem *p, double *psi, int32_t *perm);
 /* kappa[r] and the original angular index ang[r] of every block row r
  * (nblk entries each; either may be NULL): the rows of H.csr map to angular
  * indices through its perm array, kappa = ik(index) (tools/dirac_solver.c:
- * 396-431, tools/solver_common.c:87-94). */
+ * 396-431, tools/solver_common.c:30-37). */
 int gade_problem_get_blocks(const gade_problem *p, int32_t *kappa, int32_t *ang);
 void gade_problem_free(gade_problem *p);
 
@@ -90,6 +90,13 @@ void gade_solver_free(gade_solver *s);
  * Replaces gpu_put_vec / gpu_get_vec (tools/gpu_sparse.c:120-152). */
 int gade_solver_set_x(gade_solver *s, const double *x, int64_t n);
 int gade_solver_get_x(gade_solver *s, double *x, int64_t n);
+/* Starts a new pulse on the same solver (no reference counterpart: the
+ * reference runs one pulse per process): sets the state like
+ * gade_solver_set_x and clears what carries over from one step to the next
+ * (BiCGSTAB's p and v, tools/bicgstab.c:28-31, and the previous state that
+ * mixed precision extrapolates from), so the following steps are those of a
+ * new solver with the same operator choice and partition. */
+int gade_solver_restart(gade_solver *s, const double *x, int64_t n);
 
 /* One Crank-Nicolson step at time t with pulse factors ft (6 complex, i.e.
  * 12 doubles, beoyndDipolePulse_axialPart at t): fills this step's operator
@@ -223,12 +230,34 @@ int gade_solver_assembly_cost(const gade_solver *s, double *flops, double *bytes
  * array inside the library (16384 partial-sum slots), which every GPU that
  * loads the library keeps until exit.  Problems that need more than 16384
  * row-chunk x block work units are rejected with GADE_ERR_ARG.  The first call
- * on each device looks up that array's device address; make that first call
- * before any stream capture.  All calls share the array, so calls whose
- * kernels overlap on the GPU race: order them on one stream.  Asynchronous on
- * `stream` (NULL: the solver's stream). */
+ * on each device looks up that array's device address and keeps it for the
+ * life of the process; make that first call before any stream capture, and
+ * do not call cudaDeviceReset (or otherwise tear down the device's primary
+ * context) after it.  All calls share the array, so calls whose kernels
+ * overlap on the GPU race: order them on one stream.  The call reads the
+ * operator (radial tables or assembled values) that set_time and step write
+ * asynchronously on the solver's stream (gade_solver_stream): on another
+ * stream, order it after them with an event.  Asynchronous on `stream`
+ * (NULL: the solver's stream). */
 int gade_solver_apply_dot_noalloc(gade_solver *s, const void *x_dev, const void *r0_dev, void *y_dev,
                                   void *dot_dev, void *stream);
+
+/* Polls of each shared-memory stage wait of the block-LU preconditioner
+ * kernel before it gives up (no reference counterpart: the reference's
+ * cuSPARSE solves have no waits of their own).  0 restores the default,
+ * 2^22.  A wait that runs out sets an error bit, the kernel lets its copies
+ * in flight land (with the default limit) and returns; the step then
+ * returns GADE_ERR_CUDA, clears BiCGSTAB's carried vectors p and v
+ * (tools/bicgstab.c:28-31) and leaves the state undefined: set it again
+ * before the next step.  The device stays usable.  Takes effect at the next
+ * step (captured graphs are rebuilt). */
+int gade_solver_set_wait_limit(gade_solver *s, uint32_t polls);
+/* Failure injection for tests of that path (no reference counterpart): the
+ * preconditioner kernel does not issue the copy of stage `stage` (0 is the
+ * first; -1 turns the injection off), so the wait for it runs out after the
+ * wait limit and the step returns GADE_ERR_CUDA.  Nothing is read or written
+ * out of place: the kernel only skips that copy and the wait for it. */
+int gade_solver_inject_wait_timeout(gade_solver *s, int32_t stage);
 
 /* Measured FP64 FMA throughput of a device in TFLOP/s (2 flops per DFMA),
  * from a dependent-chain-free FMA kernel timed with CUDA events. */
@@ -305,6 +334,8 @@ int gade_batch_guess_buffer(gade_batch *b, void **corr_dev, int64_t *ld);
 int gade_batch_use_guess(gade_batch *b, int32_t enable);
 /* The cudaStream_t (as void*) on which the batch's work is ordered. */
 void *gade_batch_stream(const gade_batch *b);
+/* gade_solver_set_wait_limit for the pulses of a batch. */
+int gade_batch_set_wait_limit(gade_batch *b, uint32_t polls);
 
 #ifdef __cplusplus
 }

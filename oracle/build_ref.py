@@ -1,6 +1,8 @@
 """Recipe: compile the reference CPU solver (tools/ with USE_MPI, one rank)
-from its own sources, in place under /root/reference/tools, into
-oracle/_ref/dirac_solver_ref.  Test infrastructure only.
+from its own sources, in place under <reference>/tools, into
+oracle/_ref/dirac_solver_ref.  Test infrastructure only.  The reference
+checkout is taken from the GADE_REFERENCE environment variable or the first
+command-line argument (default /root/reference).
 
 The reference needs MPI, SuperLU and a Fortran-ABI BLAS, none of which is
 installed, plus an x86-only SSE header.  The shims under oracle/shim/ stand
@@ -21,12 +23,22 @@ import sys
 import sysconfig
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = "/root/reference/tools"
+
+
+def reference_tools(root: str | None = None) -> str:
+    """tools/ directory of the reference checkout: the argument, else
+    $GADE_REFERENCE, else /root/reference."""
+    root = root or os.environ.get("GADE_REFERENCE") or "/root/reference"
+    return os.path.join(root, "tools")
+
+
+REF = reference_tools()
 OUT = os.path.join(HERE, "_ref")
 SRCS = ["dirac_solver.c", "solver.c", "csr.c", "bicgstab.c", "solver_common.c", "utils.c", "sorted_list.c"]
 
 
-def build() -> str:
+def build(ref: str | None = None) -> str:
+    REF = reference_tools(ref) if ref else globals()["REF"]
     if not os.path.isdir(REF):
         raise FileNotFoundError(f"{REF} not present: the pinned reference oracle cannot be built here")
     os.makedirs(OUT, exist_ok=True)
@@ -50,4 +62,4 @@ def build() -> str:
 
 
 if __name__ == "__main__":
-    print(build())
+    print(build(sys.argv[1] if len(sys.argv) > 1 else None))

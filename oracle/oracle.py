@@ -12,8 +12,8 @@ themselves, compiled in place with single-rank MPI/BLAS/SuperLU shims by
 the comparison outputs are committed under ``tests/golden/``.
 
 Functions follow, line by line:
-  * f(t) pulse factors      tools/solver_common.c:103-122
-  * kappa of an index       tools/solver_common.c:87-94
+  * f(t) pulse factors      tools/solver_common.c:53-65
+  * kappa of an index       tools/solver_common.c:30-37
   * set-up                  tools/dirac_solver.c:223-431
   * unblocked CSR + map     tools/csr.c:653-743
   * stationary matrices     tools/solver.c:409-458
@@ -43,7 +43,7 @@ SOL = 137.035999084
 
 
 def ik(i: int) -> int:
-    """tools/solver_common.c:87-94."""
+    """tools/solver_common.c:30-37."""
     ii = i // 4
     abskappa = int(0.5 * (math.sqrt(8.0 * ii + 1.0) - 1.0)) + 1
     sgnmod = max(4, abskappa * 4)
@@ -53,7 +53,7 @@ def ik(i: int) -> int:
 
 
 def pulse(E0: float, omega: float, cycles: float, t: float) -> np.ndarray:
-    """beoyndDipolePulse_axialPart, tools/solver_common.c:110-122 (phi=-pi/2)."""
+    """beoyndDipolePulse_axialPart, tools/solver_common.c:53-65 (phi=-pi/2)."""
     T = cycles * 2 * math.pi / omega
     phi = -math.pi / 2
     a = E0 / (4 * omega)
@@ -118,8 +118,11 @@ def _conj_transpose_on_pattern(Ap, Ai, Ax):
     return out
 
 
-def load_problem(workdir: str, lmax: int) -> Problem:
-    """Reads every input like tools/dirac_solver.c:223-388."""
+def load_problem(workdir: str, lmax: int, unblock: bool = True) -> Problem:
+    """Reads every input like tools/dirac_solver.c:223-388.  unblock=False
+    skips the unblocked CSR of the whole operator (tools/csr.c:653-743),
+    which only ``timedep``/``stationary``/``run`` need; ``apply_block_rows``
+    works without it."""
     j = lambda f: os.path.join(workdir, f)
     Hall = csr_read(j("H.csr"))
     if Hall.perm is None:
@@ -155,7 +158,8 @@ def load_problem(workdir: str, lmax: int) -> Problem:
         H1[:, l] = np.asarray(H[l][1][orig_r, orig_c]).ravel()
     p = Problem(lmax, nblk, blkdim, blk_nnz, hall, perm, kappa, H0, H1, g, gt, h0, s0,
                 g0.Ap, g0.Ai, psi, xperm)
-    _unblock(p)
+    if unblock:
+        _unblock(p)
     return p
 
 
@@ -253,6 +257,61 @@ def timedep(p: Problem, dt: float, ft: np.ndarray, h: float = 1.0) -> sp.csr_mat
     data = np.empty(int(p.A_indptr[-1]), complex)
     data[p.sub_map.ravel()] = sub.ravel()
     return sp.csr_matrix((data, p.A_indices, p.A_indptr), shape=(p.n, p.n))
+
+
+def apply_block_rows(p: Problem, dt: float, ft: np.ndarray, x: np.ndarray, rows, h: float = 1.0):
+    """S x and Hfull x on the listed block rows only, with the block values
+    of ``timedep`` (tools/solver.c:196-407) and ``stationary``
+    (tools/solver.c:409-458): for block row r, Hx_r = sum over the coupled
+    blocks c of block(r, c) @ x_c, block(r, c) on the base pattern.  Needs no
+    unblocked CSR, so it serves the largest configurations.  Returns two
+    arrays [len(rows), blkdim]."""
+    ihdt = 1j * h * dt / 2
+    pg, pgt = pgsums(p, dt, ft, h)
+    tab = np.concatenate([pg, pgt], axis=1).reshape(p.lmax * 8, p.blk_nnz)
+    Ap, Ai = p.Hall.indptr, p.Hall.indices
+    bd = p.blkdim
+    base_rows = np.repeat(np.arange(bd), np.diff(p.sub_Ap))
+    X = x.reshape(p.nblk, bd)
+    Hx = np.zeros((len(rows), bd), complex)
+    Sx = np.zeros((len(rows), bd), complex)
+    for j, r in enumerate(rows):
+        kr = float(p.kappa[r])
+        for e in range(Ap[r], Ap[r + 1]):
+            c = Ai[e]
+            kc = float(p.kappa[c])
+            coef = np.concatenate([p.H0[e][:, None] * np.array([1.0, kr, kc, kr * kc])[None, :],
+                                   p.H1[e][:, None] * np.array([1.0, kc, kr, kr * kc])[None, :]], axis=1)
+            vals = coef.reshape(p.lmax * 8) @ tab
+            if p.perm[r] == p.perm[c]:
+                vals = vals + ihdt * (p.h0[0] + p.h0[1] * kr + p.h0[2] * kr * kr + p.h0[3] * kr * kr * kr)
+                svals = p.s0[0] + p.s0[1] * kr + p.s0[2] * kr * kr
+                Sx[j] += _rowsum(base_rows, svals * X[c][p.sub_Ai], bd)
+            Hx[j] += _rowsum(base_rows, vals * X[c][p.sub_Ai], bd)
+    return Sx, Hx
+
+
+def _rowsum(rows, v, n):
+    out = np.zeros(n, complex)
+    np.add.at(out, rows, v)
+    return out
+
+
+def overlap_from_files(workdir: str) -> sp.csr_matrix:
+    """S in the solver order from the input files alone: block r is
+    s0 + k s1 + k^2 s2 with k the kappa of block row r (tools/solver.c:428-432,
+    block diagonal)."""
+    from dirac_hydrogen_code_gb300.formats import csr_read as _read
+    hall = _read(os.path.join(workdir, "H.csr"))
+    s = [_read(os.path.join(workdir, f"s{i}.csr")).to_scipy() for i in range(3)]
+    blocks = {}
+    out = []
+    for orig in hall.perm:
+        k = ik(int(orig))
+        if k not in blocks:
+            blocks[k] = (s[0] + k * s[1] + k * k * s[2]).tocsr()
+        out.append(blocks[k])
+    return sp.block_diag(out, format="csr")
 
 
 class IluPrecond:
@@ -374,7 +433,10 @@ def run(workdir: str, maxtime: float, lmax: int, E0: float, omega: float, cycles
     p = problem if problem is not None else load_problem(workdir, lmax)
     dt = maxtime / ntime
     S, Hst = stationary(p, dt, h)
-    M = IluPrecond(S, Hst) if precond == "ilu" else BlockLuPrecond(p, S, Hst)
+    if not isinstance(precond, str):
+        M = precond                      # a preconditioner built beforehand (same dt)
+    else:
+        M = IluPrecond(S, Hst) if precond == "ilu" else BlockLuPrecond(p, S, Hst)
     x = (p.psi0 if psi is None else psi).astype(complex).copy()
     wsp = Workspace(p.n)
     it = start_iter

@@ -4,8 +4,9 @@
  *    iteration cap (tools/dirac_solver.c:506-507; env GADE_REF_TOL,
  *    GADE_REF_MAXIT), records iterations and tolerance of every step
  *    (GADE_REF_LOG), writes the state after every step (GADE_REF_XOUT; the
- *    reference itself writes only every 2000 steps) and can stop after a
- *    number of steps (GADE_REF_MAXSTEPS).
+ *    reference itself writes only every 2000 steps), keeps a copy of the
+ *    state every k steps in <GADE_REF_XOUT>.<step> (GADE_REF_XSNAP_EVERY=k)
+ *    and can stop after a number of steps (GADE_REF_MAXSTEPS).
  *  - --wrap=calloc: pads allocations; the reference indexes
  *    itersarr/tolsarr/timearr[iter] one or two past their calloc'd length
  *    (tools/dirac_solver.c:498-500, 575-577).
@@ -47,6 +48,15 @@ void __wrap_bicgstab(spmv_fun spmv, const void *mat, const cdouble_t *rhs, cdoub
         if (f) {
             fwrite(x + local_col_beg, sizeof(cdouble_t), (size_t)nrow, f);
             fclose(f);
+        }
+        const char *every = getenv("GADE_REF_XSNAP_EVERY");
+        if (every && atoi(every) > 0 && step % atoi(every) == 0) {
+            char path[4096];
+            snprintf(path, sizeof path, "%s.%d", e, step);
+            if ((f = fopen(path, "wb"))) {
+                fwrite(x + local_col_beg, sizeof(cdouble_t), (size_t)nrow, f);
+                fclose(f);
+            }
         }
     }
     if ((e = getenv("GADE_REF_MAXSTEPS")) && step >= atoi(e)) exit(0);

@@ -35,6 +35,6 @@ def workdirs(tmp_path_factory):
 @pytest.fixture(scope="session")
 def native_lib():
     from dirac_hydrogen_code_gb300 import build, native
-    if not os.path.exists(build.library_path()):
+    if build.is_stale():
         build.build()
     return native.load_library()

@@ -4,7 +4,16 @@
 * CPU: the oracle restatement reproduces the reference exactly in iteration
   counts and to 1e-12 in the final state (this pins the oracle).
 * GPU: the CUDA path (C ABI) reproduces the reference to 1e-10 in the final
-  state with iteration counts within +-1 on every step.
+  state with iteration counts within +-1 on every step: on the small cases,
+  over the whole 1500-step pulse of the nondipole medium configuration (the
+  benchmark workload) and over the first 20 steps of the NKappa=16
+  configuration (N = 244,000), with the operator chosen at creation and with
+  each operator forced.  Along the way the state and its S-norm x^H S x are
+  checked every 150 (5) steps: the S-norm drift must match the
+  reference's.  Where the fixture keeps a sketch R x of the state (a
+  seeded Gaussian R with E|R e|^2 = |e|^2, tests/golden/cases.py), the L2
+  error is estimated as |R x - R x_ref|; its relative spread is
+  1/sqrt(128), under 9%.
 """
 import math
 import os
@@ -14,7 +23,7 @@ import pytest
 
 import oracle as O
 from dirac_hydrogen_code_gb300.gen import generate
-from tests.golden.cases import CASES, fingerprint
+from tests.golden.cases import CASES, fingerprint, sketch
 
 HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
@@ -79,3 +88,97 @@ def test_gpu_matches_reference_build(golden_inputs, native_lib, name):
     assert len(its) == len(g["iters"])
     assert np.max(np.abs(its - g["iters"])) <= 1
     _check_state(x, g, 1e-10)
+
+
+# whole-pulse cases: (case, operator forced: None = chosen at creation,
+# 0 = matrix-free, 1 = assembled).  At the nondipole medium size the
+# creation-time choice is the assembled operator, at NKappa=16 the
+# matrix-free one.
+WHOLE = [("nondipole_medium_full", None), ("nondipole_medium_full", 0), ("nondipole_medium_full", 1),
+         ("nondipole_large_20", None), ("nondipole_large_20", 1)]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name,op", WHOLE)
+def test_gpu_whole_pulse_matches_reference_build(golden_inputs, native_lib, name, op):
+    from dirac_hydrogen_code_gb300.cn import run
+    d, info, spec, g = golden_inputs(name)
+    S = O.overlap_from_files(d)
+    want = set(g["snap_steps"].tolist())
+    snaps = {}
+
+    def grab(it, t, solver):
+        if it in want:
+            snaps[it] = solver.get_x()
+    x, recs, sol = run(*_args(d, info, spec["params"]), tol=spec["tol"], maxit=spec["maxit"],
+                       max_steps=spec.get("max_steps"), write_outputs=False, callback=grab, operator=op)
+    if op is not None:
+        assert sol.operator()["assembled"] == op
+    its = np.array([r["iters"] for r in recs])
+    assert len(its) == len(g["iters"])
+    assert np.max(np.abs(its - g["iters"])) <= 1, np.nonzero(its != g["iters"])
+    sn0 = float(g["snorm0"])
+    for k, step in enumerate(g["snap_steps"]):
+        v = snaps[int(step)]
+        err = np.linalg.norm(sketch(v) - g["snap_sketch"][k]) / g["snap_norm"][k]
+        assert err <= 1e-10, (int(step), err)
+        sn = float(np.vdot(v, S @ v).real)
+        # S-norm drift from psi0 equal to the reference's
+        assert abs((sn - sn0) - (g["snap_snorm"][k] - sn0)) <= 1e-10 * sn0, (int(step), sn, g["snap_snorm"][k])
+    if "x" in g:
+        assert np.linalg.norm(x - g["x"]) / np.linalg.norm(g["x"]) <= 1e-10
+    else:
+        assert np.linalg.norm(sketch(x) - g["x_sketch"]) / g["x_norm"] <= 1e-10
+    sn = float(np.vdot(x, S @ x).real)
+    assert abs((sn - sn0) - (g["snorm_final"] - sn0)) <= 1e-10 * sn0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("op", [0, 1])
+def test_gpu_large_operator_rows_match_oracle(golden_inputs, native_lib, op):
+    """The operator at NKappa=16 (lmax 10, N = 244,000): S x and H(t) x of
+    the CUDA path on a seeded subset of block rows against the oracle's
+    block values (tools/solver.c:196-458), near the pulse peak, with the
+    matrix-free (0) and the assembled (1) operator."""
+    from dirac_hydrogen_code_gb300.cn import pulse, step_times
+    from dirac_hydrogen_code_gb300.native import Problem, Solver
+    d, info, spec, g = golden_inputs("nondipole_large_20")
+    params = spec["params"]
+    T = params["Cycles"] * 2 * math.pi / params["Omega"]
+    dt, _ = step_times(T, params["Ntime"])
+    ft = pulse(params["Intensity"], params["Omega"], params["Cycles"], 0.45 * T)
+    prob = Problem(d, info["lmax"])
+    sol = Solver(prob, dt)
+    sol.set_operator(op)
+    sol.set_time(ft)
+    assert sol.operator()["assembled"] == op
+    rng = np.random.default_rng(31)
+    x = rng.standard_normal(prob.n) + 1j * rng.standard_normal(prob.n)
+    y, sx, hx = sol.apply(x, parts=True)
+    p = O.load_problem(d, info["lmax"], unblock=False)
+    rows = sorted(set([0, p.nblk - 1] + rng.choice(p.nblk, 14, replace=False).tolist()))
+    so, ho = O.apply_block_rows(p, dt, ft, x, rows)
+    bd = p.blkdim
+    for j, r in enumerate(rows):
+        blk = slice(r * bd, (r + 1) * bd)
+        assert np.linalg.norm(hx[blk] - ho[j]) / np.linalg.norm(ho[j]) <= 1e-13, r
+        assert np.linalg.norm(sx[blk] - so[j]) / np.linalg.norm(so[j]) <= 1e-13, r
+        assert np.linalg.norm(y[blk] - (so[j] + ho[j])) / np.linalg.norm(so[j] + ho[j]) <= 1e-13, r
+
+
+def test_oracle_block_rows_match_full_assembly(golden_inputs):
+    """apply_block_rows (used at sizes where the full assembly is too large)
+    equals the rows of the oracle's assembled operator."""
+    d, info, spec, g = golden_inputs("tiny_nondipole")
+    params = spec["params"]
+    p = O.load_problem(d, info["lmax"])
+    dt = params["Cycles"] * 2 * math.pi / params["Omega"] / params["Ntime"]
+    ft = O.pulse(params["Intensity"], params["Omega"], params["Cycles"], 17 * dt)
+    H = O.timedep(p, dt, ft)
+    S, Hst = O.stationary(p, dt)
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal(p.n) + 1j * rng.standard_normal(p.n)
+    rows = list(range(p.nblk))
+    so, ho = O.apply_block_rows(p, dt, ft, x, rows)
+    assert np.allclose(so.ravel(), S @ x, rtol=0, atol=1e-14 * np.abs(S @ x).max())
+    assert np.allclose(ho.ravel(), H @ x, rtol=0, atol=1e-14 * np.abs(H @ x).max())
