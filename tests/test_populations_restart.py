@@ -58,6 +58,29 @@ def test_projection_is_complete(workdirs, native_lib):
     assert eb.evals.min() < -2e4 and eb.evals.max() > 0 and ((eb.evals < 0) & (eb.evals > -2e4)).any()
 
 
+def test_host_populations_match_oracle(workdirs, native_lib):
+    """The product's host projection against the oracle restatement of the
+    reference's dumpEigvals + processOutput (oracle/populations.py), on the
+    ground state and on a seeded random state: every block's projections
+    and the class populations."""
+    import populations as OP
+    d, info, prob, eb, kap = _basis(workdirs, "tiny_nondipole")
+    kmax = int(np.abs(kap).max())
+    rng = np.random.default_rng(12)
+    psi, _ = prob.psi0()
+    for x in (psi, rng.standard_normal(prob.n) + 1j * rng.standard_normal(prob.n)):
+        c = eb.project(x)
+        projs, evls = OP.psiev(d, x, kmax)
+        scale = max(np.abs(c).max(), 1e-300)
+        for r in range(len(projs)):
+            assert np.abs(c[r] - projs[r]).max() <= 1e-12 * scale, r
+            assert np.array_equal(eb.evals[eb.block_kidx[r]], evls[r])
+        ref = OP.populations(d, x, kmax)
+        got = eb.populations(x)
+        for key in ref:
+            assert abs(got[key] - ref[key]) <= 1e-12 * ref["norm"], key
+
+
 def test_populations_cli(workdirs, native_lib, tmp_path):
     d, info, prob, eb, kap = _basis(workdirs, "tiny_dipole")
     psi, perm = prob.psi0()
