@@ -8,7 +8,9 @@ Outputs (git-ignored) in ``dirac_hydrogen_code_gb300/lib/``:
   reference tools/dirac_solver).
 
 Translation units are compiled in parallel; a full build takes a few
-seconds.  No cmake, no torch extension machinery.
+seconds.  No cmake, no torch extension machinery.  GADE_NVCC_FLAGS adds
+flags to the CUDA compilation of the solver (tuning builds, e.g.
+-DA32_NST=4 for the stages of the complex64 assembled apply).
 """
 from __future__ import annotations
 
@@ -78,6 +80,7 @@ def build(verbose: bool = False) -> str:
         "gade_host.o": ["gcc", "-O3", "-std=gnu11", "-fPIC", "-Wall", "-Wno-unused-function",
                         "-I", INCLUDE, "-c", os.path.join(CSRC, "gade_host.c")],
         "gade_cuda.o": [nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
+                        *os.environ.get("GADE_NVCC_FLAGS", "").split(),
                         "-I", INCLUDE, "-c", os.path.join(CSRC, "gade_cuda.cu")],
         "gade_learned.o": [nvcc, *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
                            "-I", INCLUDE, "-c", os.path.join(CSRC, "gade_learned.cu")],

@@ -125,6 +125,101 @@ template <typename R> struct R4;
 template <> struct R4<double> { typedef R4d T; };
 template <> struct R4<float> { typedef R4f T; };
 template <typename C> struct alignas(16) C4 { C a, b, c, d; };
+/* cache-global load of a complex value (the partial sums of pieces) */
+template <typename C> __device__ __forceinline__ C ldcg_c(const C *p) { return __ldcg(p); }
+
+/*
+ * Double-float ("dd") arithmetic for the refinement residual of mixed
+ * precision.  A value is hi + lo in two floats, |lo| <= ulp(hi)/2 when
+ * normalised, about 48 significant bits.  A product a b is split exactly
+ * into p = fl(a.hi b.hi) and its error by one FMA (the FMA form of Dekker's
+ * two-product, with the a.hi b.lo + a.lo b.hi terms added to the error);
+ * the high parts of a running sum are added by Knuth's two-sum, which is
+ * exact, and the rounding errors collect in the low part.  The relative
+ * error of a sum of n products is about n 2^-46 of the terms' magnitudes,
+ * against n 2^-53 in FP64: residuals of the refinement are then accurate
+ * to ~1e-13 of |b|, far below the tolerances (>= 1e-12) they decide.  All
+ * of it runs on the FP32 pipes, which GB300 has 64 times as many of as
+ * FP64 units.
+ */
+struct __align__(8) dd { float hi, lo; };
+struct __align__(16) cdd { dd x, y; };
+struct alignas(32) R4dd { dd a, b, c, d; };
+template <> struct Cx<dd> { typedef cdd T; };
+template <> struct R4<dd> { typedef R4dd T; };
+
+__host__ __device__ inline dd dd_from(double v)
+{
+    dd r;
+    r.hi = (float)v;
+    r.lo = (float)(v - (double)r.hi);
+    return r;
+}
+__device__ __forceinline__ double dd_to(dd a) { return (double)a.hi + (double)a.lo; }
+__device__ __forceinline__ dd dd_neg(dd a) { dd r; r.hi = -a.hi; r.lo = -a.lo; return r; }
+/* acc += a b */
+__device__ __forceinline__ void dd_fma(dd &acc, dd a, dd b)
+{
+    const float p = a.hi * b.hi;
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, e);
+    e = __fmaf_rn(a.lo, b.hi, e);
+    const float sum = acc.hi + p;
+    const float bv = sum - acc.hi;
+    const float err = (acc.hi - (sum - bv)) + (p - bv);
+    acc.hi = sum;
+    acc.lo += err + e;
+}
+__device__ __forceinline__ dd dd_add(dd a, dd b)
+{
+    const float sum = a.hi + b.hi;
+    const float bv = sum - a.hi;
+    const float err = (a.hi - (sum - bv)) + (b.hi - bv);
+    dd r;
+    r.hi = sum;
+    r.lo = a.lo + b.lo + err;
+    return r;
+}
+/* renormalise (fast two-sum of hi and lo) */
+__device__ __forceinline__ dd dd_norm(dd a)
+{
+    dd r;
+    r.hi = a.hi + a.lo;
+    r.lo = a.lo - (r.hi - a.hi);
+    return r;
+}
+template <> __device__ __forceinline__ cdd mk<cdd>(double re, double im)
+{
+    cdd c; c.x = dd_from(re); c.y = dd_from(im); return c;
+}
+template <> __device__ __forceinline__ cdd cadd<cdd>(cdd a, cdd b)
+{
+    cdd c; c.x = dd_add(a.x, b.x); c.y = dd_add(a.y, b.y); return c;
+}
+template <> __device__ __forceinline__ cdd csub<cdd>(cdd a, cdd b)
+{
+    cdd c; c.x = dd_add(a.x, dd_neg(b.x)); c.y = dd_add(a.y, dd_neg(b.y)); return c;
+}
+template <> __device__ __forceinline__ void cfma<cdd>(cdd &acc, cdd a, cdd b)
+{
+    dd_fma(acc.x, a.x, b.x); dd_fma(acc.x, dd_neg(a.y), b.y);
+    dd_fma(acc.y, a.x, b.y); dd_fma(acc.y, a.y, b.x);
+}
+__device__ __forceinline__ void rfma(cdd &acc, dd a, cdd b)
+{
+    dd_fma(acc.x, a, b.x); dd_fma(acc.y, a, b.y);
+}
+template <> __device__ __forceinline__ cdd ldcg_c<cdd>(const cdd *p)
+{
+    const float4 v = __ldcg((const float4 *)p);
+    cdd c; c.x.hi = v.x; c.x.lo = v.y; c.y.hi = v.z; c.y.lo = v.w; return c;
+}
+__device__ __forceinline__ cdd cdd_norm(cdd a) { cdd c; c.x = dd_norm(a.x); c.y = dd_norm(a.y); return c; }
+/* a sum about to be used as a factor: renormalised for double-float, as is otherwise */
+template <typename C> __device__ __forceinline__ C norm_c(C a) { return a; }
+template <> __device__ __forceinline__ cdd norm_c<cdd>(cdd a) { return cdd_norm(a); }
+__device__ __forceinline__ double2 cdd_to(cdd a) { return make_double2(dd_to(a.x), dd_to(a.y)); }
+__device__ __forceinline__ cdd cdd_from(double2 v) { cdd c; c.x = dd_from(v.x); c.y = dd_from(v.y); return c; }
 
 /* ------------------------------------------------------------------ */
 /* device scalars of one BiCGSTAB solve                                */
@@ -210,6 +305,7 @@ struct OpP {
     const int *row_kidx, *act_ptr, *act_l, *ang_ptr, *ang_c;
     const void *ang_a0, *ang_a0k, *ang_a1, *ang_a1k;
     const int *chunk_nrows, *chunk_ncols, *chunk_rows, *chunk_cols, *chunk_lcol;
+    const unsigned short *chunk_acol;   /* [nchunk][W][RM] column within the block of each ELL slot (B: empty) */
     const void *M;             /* [pulse][lmax][nk][W][B] */
     const void *S_ell;         /* [nk][W][B], shared by all pulses */
     const void *Hst_ell, *D_ell;   /* [pulse][nk][W][B] (depend on dt) */
@@ -238,6 +334,7 @@ struct OpP {
 struct VecP {
     void *out0, *out1, *out2;      /* outputs by mode */
     const void *in0, *in1;         /* r0 / s / rhs by mode */
+    const void *in0dd, *in1dd;     /* double-float residual pass: x_n and delta as double-float */
 };
 
 struct RedP {
@@ -418,7 +515,7 @@ struct TabP {
     const double *kvals;
     const void *g, *gt;           /* [pulse][lmax][3][4][W][B]: ELL slot layout, zero on empty slots
                                      (a in the l-parity set) */
-    void *M, *M32;                /* [pulse][lmax][nk][W][B]: FP64 tables, complex64 copies */
+    void *M, *M32, *Mdd;          /* [pulse][lmax][nk][W][B]: FP64 tables, complex64 and double-float copies */
     const int *plist;             /* grid z -> pulse (NULL: pulse 0) */
     size_t gstride, mstride;      /* elements per pulse of g / gt and of M */
 };
@@ -430,8 +527,9 @@ struct TabP {
 template <bool RC, int OUT>
 __global__ void k_tables(TabP T, const double2 *__restrict__ coef)
 {
-    /* OUT: 1 the FP64 tables M, 2 the complex64 copies M32 (rounded from the
-       same FP64 values), 3 both from one pass */
+    /* OUT: bit 1 the FP64 tables M, bit 2 the complex64 copies M32 (rounded
+       from the same FP64 values), bit 4 the double-float copies Mdd (real
+       couplings), any combination from one pass */
     const int per_l = T.W * T.B;
     const int l = blockIdx.y;
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;     /* j*B + i: consecutive threads stream g, gt and M */
@@ -466,6 +564,11 @@ __global__ void k_tables(TabP T, const double2 *__restrict__ coef)
                 R4<float>::T f;
                 f.a = (float)m.a; f.b = (float)m.b; f.c = (float)m.c; f.d = (float)m.d;
                 ((R4<float>::T *)T.M32)[e] = f;
+            }
+            if (OUT & 4) {
+                R4dd f;
+                f.a = dd_from(m.a); f.b = dd_from(m.b); f.c = dd_from(m.c); f.d = dd_from(m.d);
+                ((R4dd *)T.Mdd)[e] = f;
             }
         }
     } else {
@@ -695,8 +798,10 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 8 && SEP) ? 2 : 3)
     }
     for (int c = tid; c < ncols; c += nt) xr[c] = xb[cols[c]];
     if (mode == AX_MIX) {
+        /* x_n and delta (double-float instance: their double-float copies) */
+        constexpr bool DD = std::is_same<R, dd>::value;
         const size_t vo = (size_t)pulse * P.vstride + (size_t)r * B;
-        const C *xn = (const C *)V.in0 + vo, *dn = (const C *)V.in1 + vo;
+        const C *xn = (const C *)(DD ? V.in0dd : V.in0) + vo, *dn = (const C *)(DD ? V.in1dd : V.in1) + vo;
         for (int c = tid; c < ncols; c += nt) { xs[c] = xn[cols[c]]; ds[c] = dn[cols[c]]; }
     }
     __syncthreads();
@@ -783,6 +888,7 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 8 && SEP) ? 2 : 3)
                     if (need_d) cfma(uv.d, a.d, xv);
                 }
             }
+            uv.a = norm_c(uv.a); uv.b = norm_c(uv.b); uv.c = norm_c(uv.c); uv.d = norm_c(uv.d);
             ub[g * CS + c] = uv;
         }
         __syncthreads();
@@ -876,20 +982,23 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 8 && SEP) ? 2 : 3)
             accS = mk<C>(0, 0); accH = accS; accD = accS;
             for (int k = 0; k < np; k++) {
                 const size_t pk = (size_t)(pc - pi + k) * RM3;
-                accH = cadd(accH, __ldcg(&acc[pk + P.RM + trow]));
+                accH = cadd(accH, ldcg_c(&acc[pk + P.RM + trow]));
                 if (SEP) {
-                    accS = cadd(accS, __ldcg(&acc[pk + trow]));
-                    accD = cadd(accD, __ldcg(&acc[pk + 2 * P.RM + trow]));
+                    accS = cadd(accS, ldcg_c(&acc[pk + trow]));
+                    accD = cadd(accD, ldcg_c(&acc[pk + 2 * P.RM + trow]));
                 }
             }
         }
         if (tid == 0) P.unit_tick[u] = 0u;
     }
-    /* epilogue */
+    /* epilogue (the double-float instance writes FP64 outputs) */
     double v[NRED] = {0, 0, 0, 0};
     if (half == 0 && i >= 0) {
         const size_t gi = (size_t)pulse * P.vstride + (size_t)r * B + i;
-        apply_epilogue<C, SEP>(mode, V, gi, accS, accH, accD, v);
+        if constexpr (std::is_same<R, dd>::value)
+            apply_epilogue<double2, SEP>(mode, V, gi, cdd_to(accS), cdd_to(accH), cdd_to(accD), v);
+        else
+            apply_epilogue<C, SEP>(mode, V, gi, accS, accH, accD, v);
     }
     /* the unit's dot partials, indexed by unit (not by CTA): the final sum
        has the same order for every partition */
@@ -1515,20 +1624,23 @@ __global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const type
  * it issued and finishes its pieces without the products, so the launch's
  * reductions stay consistent.
  */
+#ifndef A32_NST
 #define A32_NST 3
+#endif
 
 __host__ __device__ __forceinline__ unsigned up128(unsigned o) { return (o + 127u) & ~127u; }
 
 /* shared memory of k_apply_asm32: stages [A32_NST][values | x block], the
    unit's own x block, the reduction buffer */
-__host__ __device__ __forceinline__ unsigned a32_smem(int W, int RMp, int B, int nt, unsigned *o_vb, unsigned *o_sb,
-                                                      unsigned *o_xr, unsigned *o_red)
+__host__ __device__ __forceinline__ unsigned a32_smem(int W, int RMp, int B, int nt, int mp, unsigned *o_vb,
+                                                      unsigned *o_sb, unsigned *o_xr, unsigned *o_red, unsigned *o_pl)
 {
     const unsigned vb = up128(4u * W * RMp), sb = vb + up128(8u * (B + 1));
     *o_vb = vb; *o_sb = sb;
     unsigned o = A32_NST * sb;
     *o_xr = o;  o += up128(8u * (B + 1));
     *o_red = o; o += up128(8u * NRED * nt);
+    *o_pl = o;  o += up128(4u * mp);
     return o;
 }
 
@@ -1549,16 +1661,17 @@ __device__ __forceinline__ void a32_issue(unsigned char *dst, unsigned vb, const
 }
 
 __global__ void __launch_bounds__(256, 3)
-    k_apply_asm32(OpP P, const float2 *__restrict__ x, int mode, VecP V, RedP red, int RMp, int npairs)
+    k_apply_asm32(OpP P, const float2 *__restrict__ x, int mode, VecP V, RedP red, int RMp, int npairs, int mp)
 {
     constexpr int HJ = 15;
     typedef float2 C;
     extern __shared__ __align__(128) unsigned char smem_a32[];
     const int W = P.W, B = P.B;
-    unsigned VB, SB, oxr, ored;
-    a32_smem(W, RMp, B, blockDim.x, &VB, &SB, &oxr, &ored);
+    unsigned VB, SB, oxr, ored, opl;
+    a32_smem(W, RMp, B, blockDim.x, mp, &VB, &SB, &oxr, &ored, &opl);
     C *xr = (C *)(smem_a32 + oxr);
     double *shred = (double *)(smem_a32 + ored);
+    int *pcl = (int *)(smem_a32 + opl);       /* [mp] coupled block of each pair of the piece */
     __shared__ __align__(8) uint64_t bar[A32_NST];
     __shared__ int s_pc, s_pw, s_fail;
 
@@ -1601,20 +1714,20 @@ __global__ void __launch_bounds__(256, 3)
                           x + (size_t)P.pair_c[pp] * B, xbytes, &bar[b]);
             }
     }
-    /* the unit's own x block (diagonal blocks) and the thread's slot columns */
+    /* the piece's coupled blocks (read by the refills), the unit's own x
+       block (diagonal blocks) and the thread's slot columns */
+    for (int k = tid; k < np; k += nt) pcl[k] = P.pair_c[p0 + k];
     {
         const C *xb = x + (size_t)r * B;
         for (int c = tid; c < B; c += nt) xr[c] = xb[c];
     }
     unsigned lcp[(HJ + 1) / 2];
     {
-        const int *gl = P.chunk_lcol + (size_t)q * W * P.RM;
-        const int *cl = P.chunk_cols + (size_t)q * P.CM;
+        const unsigned short *ac = P.chunk_acol + (size_t)q * W * P.RM;
 #pragma unroll
         for (int t = 0; t < HJ; t += 2) {
-            unsigned c0 = B, c1 = B;
-            if (t < nj && trow < P.RM) { const int lc = gl[(jb + t) * P.RM + trow]; if (lc >= 0) c0 = cl[lc]; }
-            if (t + 1 < nj && trow < P.RM) { const int lc = gl[(jb + t + 1) * P.RM + trow]; if (lc >= 0) c1 = cl[lc]; }
+            const unsigned c0 = (t < nj && trow < P.RM) ? ac[(jb + t) * P.RM + trow] : (unsigned)B;
+            const unsigned c1 = (t + 1 < nj && trow < P.RM) ? ac[(jb + t + 1) * P.RM + trow] : (unsigned)B;
             lcp[t / 2] = c0 | (c1 << 16);
         }
     }
@@ -1660,9 +1773,9 @@ __global__ void __launch_bounds__(256, 3)
             break;
         }
         if (tid == 0 && k + A32_NST < np) {     /* refill the freed buffer */
-            const int pp = p0 + k + A32_NST;
-            a32_issue(smem_a32 + b * SB, VB, A + (size_t)q * qstride + (size_t)pp * W * RMp, vbytes,
-                      x + (size_t)P.pair_c[pp] * B, xbytes, &bar[b]);
+            const int kk2 = k + A32_NST;
+            a32_issue(smem_a32 + b * SB, VB, A + (size_t)q * qstride + (size_t)(p0 + kk2) * W * RMp, vbytes,
+                      x + (size_t)pcl[kk2] * B, xbytes, &bar[b]);
         }
     }
     gs += np;
@@ -1767,10 +1880,13 @@ __device__ __forceinline__ int bp_select(BPred &bp)
 /* delta = x - x_prev (linear extrapolation of the state) or 0; FP32 copies.
    hprev[pulse] says whether x_prev exists.
    Under device control the first CTA also opens the step's records. */
+/* double-float copies of the residual pass's inputs (NULL: none) */
+struct DdVec { cdd *x, *d, *w; };
+
 __global__ void k_mixed_prep(long long n, const double2 *__restrict__ x, const double2 *__restrict__ xprev,
                              const int *__restrict__ hprev, double2 *__restrict__ d64,
                              float2 *__restrict__ d32, double2 *__restrict__ w, BPred bp,
-                             const double2 *__restrict__ corr)
+                             const double2 *__restrict__ corr, DdVec Q)
 {
     const int pulse = bp_select(bp);
     if (pulse < 0) return;
@@ -1778,6 +1894,7 @@ __global__ void k_mixed_prep(long long n, const double2 *__restrict__ x, const d
         const long long vo = (long long)pulse * n;
         x += vo; xprev += vo; d64 += vo; d32 += vo; w += vo;
         if (corr) corr += vo;
+        if (Q.x) { Q.x += vo; Q.d += vo; Q.w += vo; }
     }
     const int have_prev = hprev[pulse];
     if (blockIdx.x == 0 && threadIdx.x == 0 && bp.a && bp.a->ctl == 1) {
@@ -1796,7 +1913,9 @@ __global__ void k_mixed_prep(long long n, const double2 *__restrict__ x, const d
         }
         d64[i] = d;
         d32[i] = make_float2((float)d.x, (float)d.y);
-        w[i] = make_double2(2.0 * xv.x + d.x, 2.0 * xv.y + d.y);
+        const double2 wv = make_double2(2.0 * xv.x + d.x, 2.0 * xv.y + d.y);
+        w[i] = wv;
+        if (Q.x) { Q.x[i] = cdd_from(xv); Q.d[i] = cdd_from(d); Q.w[i] = cdd_from(wv); }
     }
 }
 
@@ -1828,13 +1947,14 @@ __global__ void k_inner_init(long long n, const double2 *__restrict__ rin, float
 /* delta += e (FP64), refresh the FP32 copy and w = 2 x_n + delta */
 __global__ void k_delta_add(long long n, double2 *__restrict__ d64, const float2 *__restrict__ e,
                             float2 *__restrict__ d32, const double2 *__restrict__ x, double2 *__restrict__ w,
-                            BPred bp)
+                            BPred bp, DdVec Q)
 {
     const int pulse = bp_select(bp);
     if (pulse < 0) return;
     {
         const long long vo = (long long)pulse * n;
         d64 += vo; e += vo; d32 += vo; x += vo; w += vo;
+        if (Q.x) { Q.d += vo; Q.w += vo; }
     }
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const float2 ev = e[i];
@@ -1843,7 +1963,9 @@ __global__ void k_delta_add(long long n, double2 *__restrict__ d64, const float2
         d64[i] = d;
         d32[i] = make_float2((float)d.x, (float)d.y);
         const double2 xv = x[i];
-        w[i] = make_double2(2.0 * xv.x + d.x, 2.0 * xv.y + d.y);
+        const double2 wv = make_double2(2.0 * xv.x + d.x, 2.0 * xv.y + d.y);
+        w[i] = wv;
+        if (Q.x) { Q.d[i] = cdd_from(d); Q.w[i] = cdd_from(wv); }
     }
 }
 
@@ -1914,6 +2036,7 @@ struct gade_solver {
     int *d_row_kidx, *d_act_ptr, *d_act_l, *d_ang_ptr, *d_ang_c;
     void *d_ang_a0, *d_ang_a0k, *d_ang_a1, *d_ang_a1k;
     int *d_chunk_nrows, *d_chunk_ncols, *d_chunk_rows, *d_chunk_cols, *d_chunk_lcol;
+    unsigned short *d_chunk_acol;
     void *d_M, *d_S_ell, *d_Hst_ell, *d_D_ell;
     double *d_kvals;            /* the distinct kappa values, as doubles for the table kernel */
     void *d_g, *d_gt;
@@ -1984,6 +2107,7 @@ struct gade_solver {
     std::vector<int> h_pair_ptr, h_pair_r, h_pair_par, h_le_ptr, h_le_l, h_le_e;   /* pairs per block row; (order, term) per pair */
     void *d_A32;                /* mixed precision: the values rounded to float, chunk-major (k_apply_asm32) */
     int RMp;                    /* rows per chunk of that layout (RM rounded up to 4) */
+    int max_row_pairs;          /* most coupled blocks of one block row */
     size_t a32_stride;          /* floats per pulse of d_A32 */
     int *d_row_pos;             /* [B] chunk << 16 | row within the chunk */
     PartList part_asm[1];       /* plain: one piece per unit */
@@ -1995,6 +2119,12 @@ struct gade_solver {
     float mf_ms;                /* best timed matrix-free apply */
     float tab_ms[2];            /* timed step tables: matrix-free radial tables, assembly */
     unsigned pc_wait;           /* polls of a preconditioner stage wait (0: MBAR_SPIN_LIMIT) */
+    /* double-float refinement residual (mixed precision, real couplings,
+       matrix-free operator): tables, angular factors, S and i h dt/2 h0 and
+       the pass's inputs as double-float */
+    int mix_dd;                 /* 1: the residual pass runs in double-float on the FP32 pipes */
+    void *d_ang_dd[4], *d_Sdd, *d_Hdd, *d_Mdd;
+    cdd *xdd, *ddd, *wdd;
     int pc_withhold;            /* failure injection: preconditioner stage whose copy is withheld (-1: none) */
 };
 
@@ -2154,6 +2284,20 @@ static int set_chunking(gade_solver *s, const gade_setup *su)
     if ((rc = dev_upload(s, &s->d_chunk_rows, su->chunk_rows, (size_t)s->nchunk * s->RM))) return rc;
     if ((rc = dev_upload(s, &s->d_chunk_cols, su->chunk_cols, (size_t)s->nchunk * s->CM))) return rc;
     if ((rc = dev_upload(s, &s->d_chunk_lcol, su->chunk_lcol, (size_t)s->nchunk * s->W * s->RM))) return rc;
+    if (s->B > 65535) return fail(GADE_ERR_ARG, "block dimension %d exceeds the 16-bit column indices", s->B);
+    {
+        /* every ELL slot's column within the block (B when empty) */
+        std::vector<unsigned short> ac((size_t)s->nchunk * s->W * s->RM);
+        for (int q = 0; q < s->nchunk; q++)
+            for (int j = 0; j < s->W; j++)
+                for (int t = 0; t < s->RM; t++) {
+                    const int lc = su->chunk_lcol[((size_t)q * s->W + j) * s->RM + t];
+                    ac[((size_t)q * s->W + j) * s->RM + t] =
+                        (unsigned short)(lc < 0 ? s->B : su->chunk_cols[(size_t)q * s->CM + lc]);
+                }
+        dev_release(s, s->d_chunk_acol);
+        if ((rc = dev_upload(s, &s->d_chunk_acol, ac.data(), ac.size()))) return rc;
+    }
     {
         /* position of every row in the chunk layout (chunk << 16 | row within the chunk) */
         std::vector<int> pos((size_t)s->B, 0);
@@ -2342,6 +2486,8 @@ static int solver_create(const gade_problem *p, int npulse, const double *dts, c
         cudaFuncSetAttribute(k_apply<float, false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
         cudaFuncSetAttribute(k_apply<float, false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
         cudaFuncSetAttribute(k_apply_asm32, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<dd, true, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
+        cudaFuncSetAttribute(k_apply<dd, true, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim);
     }
 
     gade_solver *s = new gade_solver();
@@ -2459,6 +2605,25 @@ static int solver_create(const gade_problem *p, int npulse, const double *dts, c
                 float2 *dd; UP(dd, v.data(), su->n_ang); s->d_a32[k] = dd;
             }
         }
+        if (s->rc) {
+            /* the double-float residual pass: angular factors, S, tables, inputs */
+            for (int k = 0; k < 4; k++) {
+                std::vector<dd> v((size_t)su->n_ang + 1);
+                for (int64_t e = 0; e < su->n_ang; e++) v[e] = dd_from(src[k][e].im);
+                dd *q; UP(q, v.data(), su->n_ang); s->d_ang_dd[k] = q;
+            }
+            std::vector<cdd> Sd((size_t)s->nk * WB);
+            for (size_t e = 0; e < Sd.size(); e++) { Sd[e].x = dd_from(su->S_ell[e].re); Sd[e].y = dd_from(su->S_ell[e].im); }
+            cdd *c;
+            UP(c, Sd.data(), Sd.size()); s->d_Sdd = c;
+            UP(c, (const cdd *)nullptr, NP * s->dstride); s->d_Hdd = c;
+            R4dd *m = nullptr;
+            UP(m, (const R4dd *)nullptr, NP * s->mstride); s->d_Mdd = m;
+            UP(s->xdd, (const cdd *)nullptr, NP * s->n);
+            UP(s->ddd, (const cdd *)nullptr, NP * s->n);
+            UP(s->wdd, (const cdd *)nullptr, NP * s->n);
+            s->mix_dd = 1;
+        }
     }
     {
         size_t smem = sizeof(double2) * ((size_t)2 * pc_stage_elems(s->bwp) + s->Bp + 128);
@@ -2508,6 +2673,15 @@ static int solver_create(const gade_problem *p, int npulse, const double *dts, c
                     FUf[e] = make_float2((float)FU[e].x, (float)FU[e].y);
                 }
                 ce = cudaMemcpy((float2 *)s->d_H32 + k * s->dstride, Hf.data(), sizeof(float2) * s->dstride, cudaMemcpyHostToDevice);
+                if (ce == cudaSuccess && s->d_Hdd) {
+                    std::vector<cdd> Hd(s->dstride);
+                    for (size_t e = 0; e < s->dstride; e++) {
+                        Hd[e].x = dd_from(sk->Hst_ell[e].re);
+                        Hd[e].y = dd_from(sk->Hst_ell[e].im);
+                    }
+                    ce = cudaMemcpy((cdd *)s->d_Hdd + k * s->dstride, Hd.data(), sizeof(cdd) * s->dstride,
+                                    cudaMemcpyHostToDevice);
+                }
                 if (ce == cudaSuccess) ce = cudaMemcpy((float2 *)s->d_D32 + k * s->dstride, Df.data(), sizeof(float2) * s->dstride, cudaMemcpyHostToDevice);
                 if (ce == cudaSuccess) ce = cudaMemcpy((float2 *)s->d_FL32 + k * s->fstride, FLf.data(), sizeof(float2) * s->fstride, cudaMemcpyHostToDevice);
                 if (ce == cudaSuccess) ce = cudaMemcpy((float2 *)s->d_FU32 + k * s->fstride, FUf.data(), sizeof(float2) * s->fstride, cudaMemcpyHostToDevice);
@@ -2615,6 +2789,8 @@ static int solver_create(const gade_problem *p, int npulse, const double *dts, c
                 s->h_le_e.push_back(ent[k].second.second);
             }
             s->h_pair_ptr.push_back(s->npairs);
+            const int rp = s->h_pair_ptr.back() - s->h_pair_ptr[s->h_pair_ptr.size() - 2];
+            if (rp > s->max_row_pairs) s->max_row_pairs = rp;
         }
         s->h_le_ptr.push_back((int)s->h_le_l.size());
         std::vector<int> pc;
@@ -2645,7 +2821,7 @@ static OpP op_params(const gade_solver *s)
     P.ang_ptr = s->d_ang_ptr; P.ang_c = s->d_ang_c;
     P.ang_a0 = s->d_ang_a0; P.ang_a0k = s->d_ang_a0k; P.ang_a1 = s->d_ang_a1; P.ang_a1k = s->d_ang_a1k;
     P.chunk_nrows = s->d_chunk_nrows; P.chunk_ncols = s->d_chunk_ncols; P.chunk_rows = s->d_chunk_rows;
-    P.chunk_cols = s->d_chunk_cols; P.chunk_lcol = s->d_chunk_lcol;
+    P.chunk_cols = s->d_chunk_cols; P.chunk_lcol = s->d_chunk_lcol; P.chunk_acol = s->d_chunk_acol;
     P.M = s->d_M; P.S_ell = s->d_S_ell; P.Hst_ell = s->d_Hst_ell; P.D_ell = s->d_D_ell;
     P.plist = s->d_plist; P.vstride = s->n; P.mstride = s->mstride; P.dstride = s->dstride;
     P.nchunk = s->nchunk;
@@ -2941,8 +3117,8 @@ static size_t asm_smem_bytes(const gade_solver *s, size_t elem)
 /* dynamic shared memory of k_apply_asm32 */
 static size_t asm32_smem_bytes(const gade_solver *s)
 {
-    unsigned a, b, c, d;
-    return a32_smem(s->W, (s->RM + 3) & ~3, s->B, 256, &a, &b, &c, &d);
+    unsigned a, b, c, d, e;
+    return a32_smem(s->W, (s->RM + 3) & ~3, s->B, 256, s->max_row_pairs, &a, &b, &c, &d, &e);
 }
 
 /* Builds K_a for every pulse factor a that some Bessel order uses: the
@@ -3008,7 +3184,7 @@ static int asm_build(gade_solver *s)
             T.g = (const double *)s->d_g + (size_t)ks * s->gstride;
             T.gt = (const double *)s->d_gt + (size_t)ks * s->gstride;
             T.M = (R4<double>::T *)s->d_M + (size_t)ks * s->mstride;
-            T.M32 = nullptr; T.plist = nullptr; T.gstride = s->gstride; T.mstride = s->mstride;
+            T.M32 = nullptr; T.Mdd = nullptr; T.plist = nullptr; T.gstride = s->gstride; T.mstride = s->mstride;
             const int per_l = s->W * s->B;
             k_tables<true, 1><<<dim3((unsigned)((per_l + 255) / 256), s->lmax, 1), 256, 0, s->stream>>>(T, s->d_coef);
             if (cudaGetLastError() != cudaSuccess) { rc = fail(GADE_ERR_CUDA, "assembled operator: table launch failed"); break; }
@@ -3109,7 +3285,8 @@ static int launch_apply_asm(gade_solver *s, const typename Cx<R>::T *x, int mode
         else launch_pdl(k_apply_asm<R, false>, grid, dim3(256), smem, st, P, x, mode, V, red);
     } else {
         /* the values stream through shared memory by cp.async.bulk */
-        k_apply_asm32<<<grid, 256, asm32_smem_bytes(s), st>>>(P, (const float2 *)x, mode, V, red, s->RMp, s->npairs);
+        k_apply_asm32<<<grid, 256, asm32_smem_bytes(s), st>>>(P, (const float2 *)x, mode, V, red, s->RMp, s->npairs,
+                                                              s->max_row_pairs);
     }
     prof_end(s, st, f32 ? 0 : 0);
     CKL();
@@ -3184,18 +3361,25 @@ static int launch_table_kernels(gade_solver *s, int which, cudaStream_t st)
 {
     TabP T;
     T.lmax = s->lmax; T.nk = s->nk; T.W = s->W; T.B = s->B;
-    T.kvals = s->d_kvals; T.g = s->d_g; T.gt = s->d_gt; T.M = s->d_M; T.M32 = s->d_M32;
+    T.kvals = s->d_kvals; T.g = s->d_g; T.gt = s->d_gt; T.M = s->d_M; T.M32 = s->d_M32; T.Mdd = s->d_Mdd;
     T.plist = s->d_plist; T.gstride = s->gstride; T.mstride = s->mstride;
-    if (!s->d_M32) which &= 1;
+    if (!s->d_M32) which &= ~2;
+    if (!s->d_Mdd || !s->rc) which &= ~4;
     if (!which) return GADE_OK;
     const int per_l = s->W * s->B, nt = 256;
     dim3 grid((unsigned)((per_l + nt - 1) / nt), s->lmax, s->nslot);
     prof_begin(s, st);
 #define KT(OUT_) do { if (s->rc) k_tables<true, OUT_><<<grid, nt, 0, st>>>(T, s->d_coef); \
                       else k_tables<false, OUT_><<<grid, nt, 0, st>>>(T, s->d_coef); } while (0)
-    if (which == 3) KT(3);
-    else if (which == 1) KT(1);
-    else KT(2);
+    switch (which) {
+    case 1: KT(1); break;
+    case 2: KT(2); break;
+    case 3: KT(3); break;
+    case 4: if (s->rc) k_tables<true, 4><<<grid, nt, 0, st>>>(T, s->d_coef); break;
+    case 5: if (s->rc) k_tables<true, 5><<<grid, nt, 0, st>>>(T, s->d_coef); break;
+    case 6: if (s->rc) k_tables<true, 6><<<grid, nt, 0, st>>>(T, s->d_coef); break;
+    default: if (s->rc) k_tables<true, 7><<<grid, nt, 0, st>>>(T, s->d_coef); break;
+    }
 #undef KT
     prof_end(s, st, 2);
     CKL();
@@ -3605,6 +3789,34 @@ extern "C" int gade_solver_time_apply(gade_solver *s, int32_t reps, double *ms)
     return GADE_OK;
 }
 
+extern "C" int gade_solver_time_apply_mixed(gade_solver *s, int32_t reps, double *ms)
+{
+    if (!s || !ms || reps < 1) return fail(GADE_ERR_ARG, "gade_solver_time_apply_mixed: bad argument");
+    if (s->prec != GADE_PREC_MIXED) return fail(GADE_ERR_STATE, "gade_solver_time_apply_mixed: not a mixed-precision solver");
+    if (!s->has_time) return fail(GADE_ERR_STATE, "gade_solver_time_apply_mixed: call gade_solver_set_time first");
+    CK(cudaSetDevice(s->device));
+    int rc;
+    /* this step's complex64 operator: the assembly wrote both copies; the
+       matrix-free tables are refreshed in both precisions */
+    if (!s->use_asm && (rc = launch_table_kernels(s, 3, s->stream))) return rc;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1));
+    VecP V = {}; V.out0 = s->v32; V.in0 = s->r032;
+    /* the inner solve's apply with its <r0, v> reduction (on the inner record,
+       which every refinement sweep re-initialises) */
+    if ((rc = launch_apply32(s, s->y32, AX_R0V, V, RED_R0V, s->d_sc2))) return rc;
+    CK(cudaEventRecord(e0, s->stream));
+    for (int k = 0; k < reps; k++)
+        if ((rc = launch_apply32(s, s->y32, AX_R0V, V, RED_R0V, s->d_sc2))) return rc;
+    CK(cudaEventRecord(e1, s->stream));
+    CK(cudaEventSynchronize(e1));
+    float t = 0;
+    CK(cudaEventElapsedTime(&t, e0, e1));
+    *ms = t / reps;
+    cudaEventDestroy(e0); cudaEventDestroy(e1);
+    return GADE_OK;
+}
+
 extern "C" int gade_solver_time_precond(gade_solver *s, int32_t reps, double *ms)
 {
     if (!s || !ms || reps < 1) return fail(GADE_ERR_ARG, "gade_solver_time_precond: bad argument");
@@ -3892,6 +4104,37 @@ static int batch_seq_iters(gade_batch *b, int K, cudaStream_t st)
    one (FP64 residual pass, inner-solve start), K inner complex64 iterations
    of every pulse whose inner solve runs, then the delta update and the
    certification test of every pulse whose inner solve has ended */
+/* the residual pass of a mixed step runs in double-float when the solver
+   has the double-float tables and the operator is matrix-free */
+static bool use_dd(const gade_solver *s) { return s->mix_dd && s->d_Mdd && !s->use_asm; }
+static DdVec dd_vecs(const gade_solver *s)
+{
+    DdVec q = {nullptr, nullptr, nullptr};
+    if (use_dd(s)) { q.x = s->xdd; q.d = s->ddd; q.w = s->wdd; }
+    return q;
+}
+
+/* r = -S delta - H (2 x_n + delta), |b|^2, x_n^H S x_n (AX_MIX) with the
+   matrix-free operator in double-float */
+static int launch_apply_mix_dd(gade_solver *s, VecP V, cudaStream_t st)
+{
+    OpP P = op_params(s);
+    P.ang_a0 = s->d_ang_dd[0]; P.ang_a0k = s->d_ang_dd[1]; P.ang_a1 = s->d_ang_dd[2]; P.ang_a1k = s->d_ang_dd[3];
+    P.M = s->d_Mdd; P.S_ell = s->d_Sdd; P.Hst_ell = s->d_Hdd; P.D_ell = nullptr;
+    RedP red = make_red(s, s->d_sc, RED_MIX, PRED_MIX, nullptr, s->d_sc2);
+    dim3 grid(s->nslot, op_partition(s, P, false, AX_MIX));
+    int nt;
+    size_t smem;
+    apply_dims(s, sizeof(cdd), &nt, &smem);
+    V.in0dd = s->xdd; V.in1dd = s->ddd;
+    prof_begin(s, st);
+    if (s->zskip) k_apply<dd, true, true, true><<<grid, nt, smem, st>>>(P, s->wdd, AX_MIX, V, red);
+    else k_apply<dd, true, true, false><<<grid, nt, smem, st>>>(P, s->wdd, AX_MIX, V, red);
+    prof_end(s, st, 0);
+    CKL();
+    return GADE_OK;
+}
+
 static int batch_seq_sweep(gade_batch *b, int K, cudaStream_t st)
 {
     gade_solver *s = b->s;
@@ -3902,7 +4145,9 @@ static int batch_seq_sweep(gade_batch *b, int K, cudaStream_t st)
     const size_t rsm = sizeof(double) * NRED * blk;
     VecP R = {};
     R.out0 = s->r; R.in0 = s->x; R.in1 = s->delta64;
-    if ((rc = launch_apply(s, s->tmp0, AX_MIX, R, RED_MIX, st, PRED_MIX, s->d_sc2))) return rc;
+    if (use_dd(s)) rc = launch_apply_mix_dd(s, R, st);
+    else rc = launch_apply(s, s->tmp0, AX_MIX, R, RED_MIX, st, PRED_MIX, s->d_sc2);
+    if (rc) return rc;
     {
         RedP red = make_red(s, s->d_sc2, RED_RHS, PRED_MIX, s->d_sc, nullptr);
         k_inner_init<<<grid, blk, rsm, st>>>(n, s->r, s->e32, s->ri32, s->r032, s->p32, s->v32, red, s->d_plist);
@@ -3921,7 +4166,7 @@ static int batch_seq_sweep(gade_batch *b, int K, cudaStream_t st)
         CKL();
     }
     const BPred fin = {s->d_plist, s->d_sc, s->d_sc2, PRED_FIN};
-    k_delta_add<<<grid, blk, 0, st>>>(n, s->delta64, s->e32, s->d32, s->x, s->tmp0, fin);
+    k_delta_add<<<grid, blk, 0, st>>>(n, s->delta64, s->e32, s->d32, s->x, s->tmp0, fin, dd_vecs(s));
     CKL();
     k_mixed_ctl<<<dim3(1, s->nslot), 32, 0, st>>>(fin);
     CKL();
@@ -3933,10 +4178,11 @@ static int batch_seq_first(gade_batch *b, cudaStream_t st)
     gade_solver *s = b->s;
     int rc;
     if (s->prec == GADE_PREC_MIXED) {
-        if ((rc = s->use_asm ? launch_assemble(s, st) : launch_table_kernels(s, 3, st))) return rc;
+        if ((rc = s->use_asm ? launch_assemble(s, st) : launch_table_kernels(s, use_dd(s) ? 7 : 3, st))) return rc;
         const BPred all = {s->d_plist, s->d_sc, s->d_sc2, PRED_NONE};
         k_mixed_prep<<<dim3(s->upd_grid, s->nslot), s->upd_block, 0, st>>>(
-            s->n, s->x, s->xprev, s->d_hprev, s->delta64, s->d32, s->tmp0, all, b->use_guess ? b->d_corr : nullptr);
+            s->n, s->x, s->xprev, s->d_hprev, s->delta64, s->d32, s->tmp0, all, b->use_guess ? b->d_corr : nullptr,
+            dd_vecs(s));
         CKL();
         return batch_seq_sweep(b, b->kiter, st);
     }
@@ -4315,6 +4561,34 @@ extern "C" int gade_solver_inject_wait_timeout(gade_solver *s, int32_t stage)
     if (stage < -1) return fail(GADE_ERR_ARG, "gade_solver_inject_wait_timeout: stage must be >= -1");
     s->pc_withhold = stage;
     if (s->engine) batch_drop_graphs(s->engine);
+    return GADE_OK;
+}
+
+extern "C" int gade_solver_set_residual_precision(gade_solver *s, int32_t mode)
+{
+    if (!s || (mode != 0 && mode != 1)) return fail(GADE_ERR_ARG, "gade_solver_set_residual_precision: bad argument");
+    if (mode == 1 && !s->d_Mdd)
+        return fail(GADE_ERR_ARG, "gade_solver_set_residual_precision: double-float needs a mixed-precision solver "
+                                  "with real couplings");
+    s->mix_dd = mode;
+    if (s->engine) batch_drop_graphs(s->engine);
+    return GADE_OK;
+}
+
+extern "C" int gade_solver_residual_precision(const gade_solver *s, int32_t *mode, int32_t *in_use)
+{
+    if (!s) return fail(GADE_ERR_ARG, "gade_solver_residual_precision: NULL solver");
+    if (mode) *mode = s->mix_dd;
+    if (in_use) *in_use = (s->prec == GADE_PREC_MIXED && use_dd(s)) ? 1 : 0;
+    return GADE_OK;
+}
+
+extern "C" int gade_batch_set_residual_precision(gade_batch *b, int32_t mode)
+{
+    if (!b) return fail(GADE_ERR_ARG, "gade_batch_set_residual_precision: NULL batch");
+    int rc = gade_solver_set_residual_precision(b->s, mode);
+    if (rc) return rc;
+    batch_drop_graphs(b);
     return GADE_OK;
 }
 

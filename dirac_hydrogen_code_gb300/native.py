@@ -80,6 +80,7 @@ _SIGS = {
     "gade_solver_launch_count": (C.c_int64, [C.c_void_p]),
     "gade_solver_time_apply": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_double)]),
     "gade_solver_time_precond": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_double)]),
+    "gade_solver_time_apply_mixed": (C.c_int, [C.c_void_p, C.c_int32, C.POINTER(C.c_double)]),
     "gade_solver_stream": (C.c_void_p, [C.c_void_p]),
     "gade_solver_profile": (C.c_int, [C.c_void_p, C.c_int32]),
     "gade_solver_kernel_times": (C.c_int, [C.c_void_p, C.POINTER(KernelTimes)]),
@@ -112,6 +113,9 @@ _SIGS = {
     "gade_solver_set_wait_limit": (C.c_int, [C.c_void_p, C.c_uint32]),
     "gade_solver_restart": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),
     "gade_solver_inject_wait_timeout": (C.c_int, [C.c_void_p, C.c_int32]),
+    "gade_solver_set_residual_precision": (C.c_int, [C.c_void_p, C.c_int32]),
+    "gade_solver_residual_precision": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "gade_batch_set_residual_precision": (C.c_int, [C.c_void_p, C.c_int32]),
     "gade_batch_set_wait_limit": (C.c_int, [C.c_void_p, C.c_uint32]),
 }
 
@@ -312,6 +316,12 @@ class Solver:
         _check(load_library().gade_solver_time_apply(self._h, int(reps), C.byref(ms)))
         return ms.value
 
+    def time_apply_mixed(self, reps: int = 20) -> float:
+        """Average ms of the complex64 inner-solve apply (mixed precision)."""
+        ms = C.c_double()
+        _check(load_library().gade_solver_time_apply_mixed(self._h, int(reps), C.byref(ms)))
+        return ms.value
+
     def time_precond(self, reps: int = 20) -> float:
         ms = C.c_double()
         _check(load_library().gade_solver_time_precond(self._h, int(reps), C.byref(ms)))
@@ -363,6 +373,16 @@ class Solver:
         """Polls of each preconditioner stage wait before the step gives up
         with GADE_ERR_CUDA (0: the default)."""
         _check(load_library().gade_solver_set_wait_limit(self._h, int(polls)))
+
+    def set_residual_precision(self, mode: int):
+        """Mixed precision: the refinement residual on the FP64 units (0) or
+        in double-float on the FP32 units (1, the default where available)."""
+        _check(load_library().gade_solver_set_residual_precision(self._h, int(mode)))
+
+    def residual_precision(self) -> dict:
+        m, u = C.c_int32(), C.c_int32()
+        _check(load_library().gade_solver_residual_precision(self._h, C.byref(m), C.byref(u)))
+        return {"mode": int(m.value), "double_float_in_use": bool(u.value)}
 
     def inject_wait_timeout(self, stage: int = -1):
         """Tests of the failure path: the preconditioner kernel withholds the
@@ -487,6 +507,9 @@ class Batch:
 
     def set_wait_limit(self, polls: int = 0):
         _check(load_library().gade_batch_set_wait_limit(self._h, int(polls)))
+
+    def set_residual_precision(self, mode: int):
+        _check(load_library().gade_batch_set_residual_precision(self._h, int(mode)))
 
     def state_device(self) -> tuple[int, int]:
         """(device address of the pulse states, per-pulse stride in complex elements)."""

@@ -149,6 +149,9 @@ int64_t gade_solver_launch_count(const gade_solver *s);
  * the solver's stream; ms receives the average. */
 int gade_solver_time_apply(gade_solver *s, int32_t reps, double *ms);
 int gade_solver_time_precond(gade_solver *s, int32_t reps, double *ms);
+/* The same for the complex64 operator apply of a mixed-precision solver's
+ * inner BiCGSTAB (with its <r0, v> reduction); no reference counterpart. */
+int gade_solver_time_apply_mixed(gade_solver *s, int32_t reps, double *ms);
 
 /* The cudaStream_t (as void*) on which every call of this solver is ordered;
  * callers record their own CUDA events on it. */
@@ -241,6 +244,19 @@ int gade_solver_assembly_cost(const gade_solver *s, double *flops, double *bytes
  * (NULL: the solver's stream). */
 int gade_solver_apply_dot_noalloc(gade_solver *s, const void *x_dev, const void *r0_dev, void *y_dev,
                                   void *dot_dev, void *stream);
+
+/* Arithmetic of the FP64 refinement residual of a mixed-precision step (no
+ * reference counterpart): 0 the FP64 units; 1 (the default where available)
+ * double-float on the FP32 units, each value a pair of floats (about 48
+ * significant bits: products split exactly by FMA, sums by two-sum), which
+ * keeps the residual accurate to ~1e-13 of |b| and runs on GB300's 64-times
+ * larger FP32 rate.  Available for mixed-precision solvers with real
+ * couplings on the matrix-free operator; the assembled operator's residual
+ * stays FP64.  gade_solver_residual_precision reports the setting and
+ * whether the double-float pass is the one steps use.  Takes effect at the
+ * next step. */
+int gade_solver_set_residual_precision(gade_solver *s, int32_t mode);
+int gade_solver_residual_precision(const gade_solver *s, int32_t *mode, int32_t *in_use);
 
 /* Polls of each shared-memory stage wait of the block-LU preconditioner
  * kernel before it gives up (no reference counterpart: the reference's
@@ -336,6 +352,8 @@ int gade_batch_use_guess(gade_batch *b, int32_t enable);
 void *gade_batch_stream(const gade_batch *b);
 /* gade_solver_set_wait_limit for the pulses of a batch. */
 int gade_batch_set_wait_limit(gade_batch *b, uint32_t polls);
+/* gade_solver_set_residual_precision for a batch. */
+int gade_batch_set_residual_precision(gade_batch *b, int32_t mode);
 
 #ifdef __cplusplus
 }
