@@ -2123,6 +2123,7 @@ struct gade_solver {
        matrix-free operator): tables, angular factors, S and i h dt/2 h0 and
        the pass's inputs as double-float */
     int mix_dd;                 /* 1: the residual pass runs in double-float on the FP32 pipes */
+    int m64_stale;              /* the last step wrote no FP64 radial tables (refreshed on the next FP64 apply) */
     void *d_ang_dd[4], *d_Sdd, *d_Hdd, *d_Mdd;
     cdd *xdd, *ddd, *wdd;
     int pc_withhold;            /* failure injection: preconditioner stage whose copy is withheld (-1: none) */
@@ -3383,7 +3384,8 @@ static int launch_table_kernels(gade_solver *s, int which, cudaStream_t st)
 #undef KT
     prof_end(s, st, 2);
     CKL();
-    if (which & 1) s->has_time = 1;
+    if (which & 1) s->m64_stale = 0;
+    s->has_time = 1;
     return GADE_OK;
 }
 
@@ -3406,6 +3408,14 @@ static int sync_scal(gade_solver *s)
         return fail(GADE_ERR_CUDA, "device wait timed out (flags %u): TMA copy did not complete", e);
     }
     return GADE_OK;
+}
+
+/* the FP64 radial tables of the last step, where a mixed step with the
+   double-float residual pass left them out (from its coefficients, d_coef) */
+static int ensure_fp64_tables(gade_solver *s)
+{
+    if (!s->m64_stale || s->use_asm) return GADE_OK;
+    return launch_table_kernels(s, 1, s->stream);
 }
 
 extern "C" int gade_solver_set_time(gade_solver *s, const double *ft)
@@ -3445,6 +3455,10 @@ extern "C" int gade_solver_apply(gade_solver *s, const double *x, double *y, dou
     if (!s || !x) return fail(GADE_ERR_ARG, "gade_solver_apply: NULL argument");
     if (!s->has_time) return fail(GADE_ERR_STATE, "gade_solver_apply: call gade_solver_set_time first");
     CK(cudaSetDevice(s->device));
+    {
+        int rc0 = ensure_fp64_tables(s);
+        if (rc0) return rc0;
+    }
     const size_t bytes = sizeof(double2) * (size_t)s->n;
     CK(cudaMemcpyAsync(s->tmp0, x, bytes, cudaMemcpyHostToDevice, s->stream));
     VecP V = {};
@@ -3469,6 +3483,13 @@ extern "C" int gade_solver_apply_device(gade_solver *s, const void *x_dev, void 
 {
     if (!s || !x_dev || !y_dev) return fail(GADE_ERR_ARG, "gade_solver_apply_device: NULL argument");
     if (!s->has_time) return fail(GADE_ERR_STATE, "gade_solver_apply_device: call gade_solver_set_time first");
+    if (s->m64_stale && !s->use_asm) {
+        /* refreshed on the solver's stream, which the caller's stream may not follow */
+        CK(cudaSetDevice(s->device));
+        int rc0 = ensure_fp64_tables(s);
+        if (rc0) return rc0;
+        CK(cudaStreamSynchronize(s->stream));
+    }
     VecP V = {};
     V.out0 = y_dev;
     return launch_apply(s, (const double2 *)x_dev, AX_PLAIN, V, RED_NONE,
@@ -3772,6 +3793,10 @@ extern "C" int gade_solver_time_apply(gade_solver *s, int32_t reps, double *ms)
     if (!s || !ms || reps < 1) return fail(GADE_ERR_ARG, "gade_solver_time_apply: bad argument");
     if (!s->has_time) return fail(GADE_ERR_STATE, "gade_solver_time_apply: call gade_solver_set_time first");
     CK(cudaSetDevice(s->device));
+    {
+        int rc0 = ensure_fp64_tables(s);
+        if (rc0) return rc0;
+    }
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0)); CK(cudaEventCreate(&e1));
     VecP V = {}; V.out0 = s->tmp1;
@@ -3981,6 +4006,13 @@ extern "C" int gade_solver_apply_dot_noalloc(gade_solver *s, const void *x_dev, 
     if (!s || !x_dev || !r0_dev || !y_dev || !dot_dev)
         return fail(GADE_ERR_ARG, "gade_solver_apply_dot_noalloc: NULL argument");
     if (!s->has_time) return fail(GADE_ERR_STATE, "gade_solver_apply_dot_noalloc: call gade_solver_set_time first");
+    if (s->m64_stale && !s->use_asm) {
+        /* refreshed on the solver's stream, which the caller's stream may not follow */
+        CK(cudaSetDevice(s->device));
+        int rc0 = ensure_fp64_tables(s);
+        if (rc0) return rc0;
+        CK(cudaStreamSynchronize(s->stream));
+    }
     if (s->device < 0 || s->device >= 256) return fail(GADE_ERR_ARG, "gade_solver_apply_dot_noalloc: device ordinal out of range");
     const long long ncta = (long long)s->nchunk * s->nblk;
     if (ncta > GADE_NOALLOC_MAX_CTAS)
@@ -4178,7 +4210,9 @@ static int batch_seq_first(gade_batch *b, cudaStream_t st)
     gade_solver *s = b->s;
     int rc;
     if (s->prec == GADE_PREC_MIXED) {
-        if ((rc = s->use_asm ? launch_assemble(s, st) : launch_table_kernels(s, use_dd(s) ? 7 : 3, st))) return rc;
+        /* the double-float residual pass needs no FP64 tables: they are
+           rebuilt from the step's coefficients by the next FP64 apply */
+        if ((rc = s->use_asm ? launch_assemble(s, st) : launch_table_kernels(s, use_dd(s) ? 6 : 3, st))) return rc;
         const BPred all = {s->d_plist, s->d_sc, s->d_sc2, PRED_NONE};
         k_mixed_prep<<<dim3(s->upd_grid, s->nslot), s->upd_block, 0, st>>>(
             s->n, s->x, s->xprev, s->d_hprev, s->delta64, s->d32, s->tmp0, all, b->use_guess ? b->d_corr : nullptr,
@@ -4513,6 +4547,7 @@ static int batch_step_mixed(gade_batch *b, const std::vector<int> &list, int32_t
         CK(cudaMemcpyAsync(b->xout_host, s->x, sizeof(double2) * (size_t)s->n, cudaMemcpyDeviceToHost, s->stream));
         CK(cudaStreamSynchronize(s->stream));
     }
+    if (use_dd(s)) s->m64_stale = 1;
     b->steps++;
     batch_adapt(b, kmax);
     if (stalled >= 0) {

@@ -124,3 +124,27 @@ def test_double_float_residual_agrees_with_fp64_residual(golden_case, native_lib
     for a, b in zip(r64, rdd):
         assert abs(a["init_residual"] - b["init_residual"]) <= 1e-6 * a["init_residual"] + 1e-15
     assert np.linalg.norm(xdd - x64) / np.linalg.norm(x64) <= 1e-10
+
+
+def test_fp64_apply_after_double_float_steps(golden_case, native_lib):
+    """Mixed steps with the double-float residual pass leave the FP64 radial
+    tables out; the next FP64 apply rebuilds them from the step's pulse
+    factors: the same result as setting the time again."""
+    from dirac_hydrogen_code_gb300.cn import pulse, step_times
+    from dirac_hydrogen_code_gb300.native import Problem, Solver
+    d, info, spec, g = golden_case("tiny_nondipole")
+    params = spec["params"]
+    T = params["Cycles"] * 2 * math.pi / params["Omega"]
+    dt, steps = step_times(T, params["Ntime"])
+    prob = Problem(d, info["lmax"])
+    sol = Solver(prob, dt, precision="mixed")
+    sol.set_operator(0)
+    assert sol.residual_precision()["double_float_in_use"]
+    fts = [pulse(params["Intensity"], params["Omega"], params["Cycles"], t) for _, t in steps[:5]]
+    for ft in fts:
+        sol.step(ft, 500, 1e-12)
+    rng = np.random.default_rng(2)
+    x = rng.standard_normal(prob.n) + 1j * rng.standard_normal(prob.n)
+    y_after_step = sol.apply(x)
+    sol.set_time(fts[-1])
+    assert np.array_equal(y_after_step, sol.apply(x))
