@@ -726,7 +726,10 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 8 && SEP) ? 2 : 3)
     const int CS = (P.CM + 2) & ~1;           /* column stride: CM + the zero column, even */
     const ApplySmem L = apply_smem(CS, P.W, P.RM, P.AM, G, sizeof(C), sizeof(A4), blockDim.x, P.lmax);
     C *xr = (C *)(smem_raw + L.xr);           /* [CS] */
-    C4<C> *ub = (C4<C> *)(smem_raw + L.ub);   /* [G][CS] u, w, u', w' of a column */
+    /* [G][4][CS] u, w, u', w' of a column, one array per vector: a warp
+       reads one vector of neighbouring columns, 16 or 8 bytes apart, free of
+       bank conflicts */
+    C *ub = (C *)(smem_raw + L.ub);
     C *xs = (C *)(smem_raw + L.xs);           /* [CS] AX_MIX: x_n slice   */
     C *ds = (C *)(smem_raw + L.ds);           /* [CS] AX_MIX: delta slice */
     int *lcs = (int *)(smem_raw + L.lcs);     /* [W][RM] local column of each ELL slot (CM: empty) */
@@ -748,7 +751,8 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 8 && SEP) ? 2 : 3)
         const C z = mk<C>(0, 0);
         xr[CM] = z; xs[CM] = z; ds[CM] = z;
         C4<C> z4; z4.a = z; z4.b = z; z4.c = z; z4.d = z;
-        for (int g = 0; g < G; g++) ub[g * CS + CM] = z4;
+        for (int g = 0; g < G; g++)
+            for (int q4 = 0; q4 < 4; q4++) ub[(g * 4 + q4) * CS + CM] = z4.a;
     }
     /* this CTA's segment: pieces (unit, order range) in sequence order.  The
        piece's scalars are kept in shared memory and read back after the
@@ -888,46 +892,46 @@ __global__ void __launch_bounds__(256, (sizeof(R) == 8 && SEP) ? 2 : 3)
                     if (need_d) cfma(uv.d, a.d, xv);
                 }
             }
-            uv.a = norm_c(uv.a); uv.b = norm_c(uv.b); uv.c = norm_c(uv.c); uv.d = norm_c(uv.d);
-            ub[g * CS + c] = uv;
+            C *u4 = ub + (size_t)g * 4 * CS + c;
+            u4[0] = norm_c(uv.a); u4[CS] = norm_c(uv.b); u4[2 * CS] = norm_c(uv.c); u4[3 * CS] = norm_c(uv.d);
         }
         __syncthreads();
         if (i >= 0) {
             for (int g = 0; g < ng; g++) {
                 const int l = oinf[ag - pd.y + g].x;
-                const C4<C> *ug = ub + g * CS;
+                const C *ua = ub + (size_t)g * 4 * CS, *uw = ua + CS, *uc = ua + 2 * CS, *ud = ua + 3 * CS;
+                const bool second = half == 1;
+                const C *u3 = second ? ud : uw;          /* with the DKB zero blocks: the half's third vector */
                 if constexpr (RC) {
                     typedef typename R4<R>::T Q4;
                     const Q4 *Mt = (const Q4 *)P.M + (size_t)pulse * P.mstride + ((size_t)l * P.nk + kk) * W * B + i + jB;
-                    const bool second = half == 1;
 #pragma unroll
                     for (int t = 0; t < HJ; t++) {
                         const Q4 m = *Mt;
-                        const C4<C> uv = ug[LCO(t)];
-                        rfma(accH, m.a, uv.a);
-                        rfma(accH, m.c, uv.c);
+                        const int lc = LCO(t);
+                        rfma(accH, m.a, ua[lc]);
+                        rfma(accH, m.c, uc[lc]);
                         if (Z) {
-                            rfma(accH, second ? m.d : m.b, second ? uv.d : uv.b);
+                            rfma(accH, second ? m.d : m.b, u3[lc]);
                         } else {
-                            rfma(accH, m.b, uv.b);
-                            rfma(accH, m.d, uv.d);
+                            rfma(accH, m.b, uw[lc]);
+                            rfma(accH, m.d, ud[lc]);
                         }
                         if (t + 1 < nj) Mt += B;
                     }
                 } else {
                     const C4<C> *Mt = (const C4<C> *)P.M + (size_t)pulse * P.mstride + ((size_t)l * P.nk + kk) * W * B + i + jB;
-                    const bool second = half == 1;
 #pragma unroll
                     for (int t = 0; t < HJ; t++) {
                         const C4<C> m = *Mt;
-                        const C4<C> uv = ug[LCO(t)];
-                        cfma(accH, m.a, uv.a);
-                        cfma(accH, m.c, uv.c);
+                        const int lc = LCO(t);
+                        cfma(accH, m.a, ua[lc]);
+                        cfma(accH, m.c, uc[lc]);
                         if (Z) {
-                            cfma(accH, second ? m.d : m.b, second ? uv.d : uv.b);
+                            cfma(accH, second ? m.d : m.b, u3[lc]);
                         } else {
-                            cfma(accH, m.b, uv.b);
-                            cfma(accH, m.d, uv.d);
+                            cfma(accH, m.b, uw[lc]);
+                            cfma(accH, m.d, ud[lc]);
                         }
                         if (t + 1 < nj) Mt += B;
                     }

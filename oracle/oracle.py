@@ -91,6 +91,7 @@ class Problem:
     A_indptr: np.ndarray = None
     A_indices: np.ndarray = None
     sub_map: np.ndarray = None     # (nnz(Hall), blk_nnz) -> position in A
+    sub_inv: np.ndarray = None     # position in A -> flat index into (nnz(Hall), blk_nnz)
     S_indptr: np.ndarray = None
     S_indices: np.ndarray = None
     S_map: np.ndarray = None       # (nblk, blk_nnz)
@@ -188,6 +189,11 @@ def _unblock(p: Problem) -> None:
             # block k of this row, base entry e -> dst0 + k*(hi-lo) + (e-lo)
             sub_map[Ap[r]:Ap[r + 1], lo:hi] = dst0 + np.arange(nb)[:, None] * (hi - lo) + np.arange(hi - lo)[None, :]
     p.A_indptr, p.A_indices, p.sub_map = indptr, indices, sub_map
+    # the inverse map (position in A -> flat (pair, base entry)): filling A is
+    # then a gather, split over the host threads like the reference's
+    # OpenMP-parallel assembly
+    p.sub_inv = np.empty(nnz, np.int64)
+    p.sub_inv[sub_map.ravel()] = np.arange(nnz, dtype=np.int64)
     # S: block diagonal
     s_indptr = np.zeros(p.nblk * bd + 1, np.int64)
     np.cumsum(np.tile(srow_nnz, p.nblk), out=s_indptr[1:])
@@ -254,9 +260,30 @@ def timedep(p: Problem, dt: float, ft: np.ndarray, h: float = 1.0) -> sp.csr_mat
     kd = ki[diag]
     sub[diag] += ihdt * (p.h0[0][None] + p.h0[1][None] * kd + p.h0[2][None] * kd * kd
                          + p.h0[3][None] * kd * kd * kd)
-    data = np.empty(int(p.A_indptr[-1]), complex)
-    data[p.sub_map.ravel()] = sub.ravel()
+    data = _gather(sub.ravel(), p.sub_inv)
     return sp.csr_matrix((data, p.A_indices, p.A_indptr), shape=(p.n, p.n))
+
+
+_POOL = None
+
+
+def _gather(src: np.ndarray, idx: np.ndarray) -> np.ndarray:
+    """src[idx], split over the host threads (numpy releases the GIL)."""
+    global _POOL
+    out = np.empty(idx.size, src.dtype)
+    nthr = os.cpu_count() or 1
+    if idx.size < (1 << 20) or nthr == 1:
+        np.take(src, idx, out=out)
+        return out
+    if _POOL is None:
+        from concurrent.futures import ThreadPoolExecutor
+        _POOL = ThreadPoolExecutor(nthr)
+
+    def part(k):
+        lo, hi = k * idx.size // nthr, (k + 1) * idx.size // nthr
+        np.take(src, idx[lo:hi], out=out[lo:hi])
+    list(_POOL.map(part, range(nthr)))
+    return out
 
 
 def apply_block_rows(p: Problem, dt: float, ft: np.ndarray, x: np.ndarray, rows, h: float = 1.0):

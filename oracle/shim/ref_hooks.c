@@ -3,7 +3,9 @@
  *  - --wrap=bicgstab: optionally overrides the hard-coded tolerance and
  *    iteration cap (tools/dirac_solver.c:506-507; env GADE_REF_TOL,
  *    GADE_REF_MAXIT), records iterations and tolerance of every step
- *    (GADE_REF_LOG), writes the state after every step (GADE_REF_XOUT; the
+ *    (GADE_REF_LOG: step, iterations, tolerance, BiCGSTAB microseconds and
+ *    the wall clock at its end, whose differences time whole steps), writes
+ *    the state after every step (GADE_REF_XOUT; the
  *    reference itself writes only every 2000 steps), keeps a copy of the
  *    state every k steps in <GADE_REF_XOUT>.<step> (GADE_REF_XSNAP_EVERY=k)
  *    and can stop after a number of steps (GADE_REF_MAXSTEPS).
@@ -38,8 +40,9 @@ void __wrap_bicgstab(spmv_fun spmv, const void *mat, const cdouble_t *rhs, cdoub
     if ((e = getenv("GADE_REF_LOG"))) {
         FILE *f = fopen(e, step == 1 ? "w" : "a");
         if (f) {
-            fprintf(f, "%d %d %.17e %ld\n", step, *iters, *tol_error,
-                    (long)((t1.tv_sec - t0.tv_sec) * 1000000L + (t1.tv_usec - t0.tv_usec)));
+            fprintf(f, "%d %d %.17e %ld %ld\n", step, *iters, *tol_error,
+                    (long)((t1.tv_sec - t0.tv_sec) * 1000000L + (t1.tv_usec - t0.tv_usec)),
+                    (long)(t1.tv_sec * 1000000L + t1.tv_usec));
             fclose(f);
         }
     }
