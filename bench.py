@@ -505,6 +505,8 @@ def run_ours(args):
                                                             psi, fts, pos, l2_flush)}
         if not args.no_batch:
             variants["batch64"] = batch_variant(prob, params, args, torch)
+        if not args.no_large:
+            variants["nkappa16_whole_pulse"] = nkappa16_variant(args, torch)
         if not args.no_learned:
             variants["learned_nkappa16"] = learned_variant(args, torch)
 
@@ -664,6 +666,7 @@ def batch_variant(prob, params, args, torch):
                     "iters_per_step": float(np.mean([[r["iters"] for r in row] for row in st])),
                     "fp64_residual_passes_per_step": float(np.mean([[r["refinements"] for r in row] for row in st])),
                     "graph_replays_per_step": inf["graph_replays"] / max(inf["steps"], 1),
+                    "operator": "assembled" if b.operator()["assembled"] else "matrix-free",
                     "chunk_splines": inf["chunk_splines"], "autotune_ms": dict(zip(inf["tune_cs"], inf["tune_ms"]))}
         finals[tag] = np.stack([b.get_x(k) for k in range(len(pulses))])
         b.close()
@@ -679,6 +682,63 @@ def batch_variant(prob, params, args, torch):
             "l2_rel_max": float(np.max(np.linalg.norm(mx - ref, axis=1) / np.linalg.norm(ref, axis=1))),
             "bound_abs_max": max(e["bound_abs"] for e in perr),
             "continuum_abs_max": max(e["continuum_abs"] for e in perr)}
+    return out
+
+
+def nkappa16_variant(args, torch):
+    """The NKappa=16 configuration (NMu=8, NSplines=300, Nl=10, 5 cycles,
+    Ntime=4000, N = 244,000; the matrix-free operator): one whole pulse per
+    precision, timed on K steps sampled evenly across it like the headline
+    (L2 flushed before each), plain FP64 at tolerance 1e-12 and 1e-10 and
+    mixed precision (complex64 inner solve, double-float refinement residual)
+    at 1e-10 and 1e-12; final-state errors against the plain FP64 run at
+    1e-12."""
+    import numpy as np
+    from dirac_hydrogen_code_gb300 import native
+    from dirac_hydrogen_code_gb300.cn import pulse, step_times
+    from dirac_hydrogen_code_gb300.gen import CONFIGS, generate
+    params = CONFIGS["nondipole_large"]
+    out = {"workload": "nondipole_large (NKappa=16)", "unit": "steps/s"}
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    with tempfile.TemporaryDirectory() as d:
+        info = generate(params, d)
+        prob = native.Problem(d, info["lmax"])
+        T = params["Cycles"] * 2 * math.pi / params["Omega"]
+        dt, steps = step_times(T, params["Ntime"])
+        fts = [pulse(params["Intensity"], params["Omega"], params["Cycles"], t) for _, t in steps]
+        pos = sample_positions(len(fts), args.steps, args.warmup)
+        out["timed_steps"] = timed_steps_text(len(pos), len(fts), args.warmup)
+        psi, _ = prob.psi0()
+        finals = {}
+        for tag, prec, tol in (("fp64_tol1e-12", "fp64", 1e-12), ("fp64_tol1e-10", "fp64", 1e-10),
+                               ("mixed_tol1e-10", "mixed", 1e-10), ("mixed_tol1e-12", "mixed", 1e-12)):
+            sol = native.Solver(prob, dt, 1.0, precision=prec)
+            sol.restart(psi)
+            stream = torch.cuda.ExternalStream(sol.stream())
+            w = walk(sol, fts, pos, tol, stream, flush, torch)
+            finals[tag] = sol.get_x().copy()
+            recs = [w["records"][j] for j in pos]
+            rec = {"steps_per_s": len(pos) / (w["ms_timed"] / 1e3),
+                   "whole_pulse_steps_per_s": len(fts) / (w["ms_pulse"] / 1e3),
+                   "iters_histogram": iteration_histogram(w["iters"]), "operator": sol.operator()["assembled"]}
+            if prec == "mixed":
+                rec["fp64_residual_passes_per_step"] = float(np.mean([r["refinements"] for r in recs]))
+                rec["inner_iters_per_step"] = float(np.mean([r["inner_iters"] for r in recs]))
+                rec["residual_pass"] = ("double-float" if sol.residual_precision()["double_float_in_use"]
+                                        else "FP64")
+            out[tag] = rec
+            sol.close()
+        eb = _eigenbasis(prob)
+        ref = finals["fp64_tol1e-12"]
+        pref = eb.populations(ref)
+        for tag in ("fp64_tol1e-10", "mixed_tol1e-10", "mixed_tol1e-12"):
+            out[tag]["l2_err_vs_fp64_tol1e-12"] = float(np.linalg.norm(finals[tag] - ref) / np.linalg.norm(ref))
+            out[tag]["population_err_vs_fp64"] = _pop_err(eb.populations(finals[tag]), pref)
+        prob.close()
+    base12, base10 = out["fp64_tol1e-12"]["steps_per_s"], out["fp64_tol1e-10"]["steps_per_s"]
+    out["speedup_mixed_tol1e-10_vs_fp64_tol1e-10"] = out["mixed_tol1e-10"]["steps_per_s"] / base10
+    out["speedup_mixed_tol1e-10_vs_fp64_tol1e-12"] = out["mixed_tol1e-10"]["steps_per_s"] / base12
+    out["speedup_mixed_tol1e-12_vs_fp64_tol1e-12"] = out["mixed_tol1e-12"]["steps_per_s"] / base12
     return out
 
 
@@ -756,15 +816,19 @@ def profile_only(args):
     from dirac_hydrogen_code_gb300 import native
     from dirac_hydrogen_code_gb300.cn import pulse, step_times
     native.load_library()
+    from dirac_hydrogen_code_gb300.gen import CONFIGS, generate
     with tempfile.TemporaryDirectory() as d:
-        params, info, T = _gen(d)
+        params = CONFIGS[args.profile_workload]
+        info = generate(params, d)
+        T = params["Cycles"] * 2 * math.pi / params["Omega"]
         prob = native.Problem(d, info["lmax"])
         dt, steps = step_times(T, params["Ntime"])
         sol = native.Solver(prob, dt, 1.0, precision=args.profile_precision, device=0)
         if args.operator != "auto":
             sol.set_operator(1 if args.operator == "assembled" else 0)
         tol = TOL if args.profile_precision == "fp64" else 1e-10
-        for k in range(args.warmup + args.steps):
+        first = args.profile_from
+        for k in range(first, first + args.warmup + args.steps):
             sol.step(pulse(params["Intensity"], params["Omega"], params["Cycles"], steps[k][1]), MAXIT, tol)
         torch.cuda.synchronize()
         print(json.dumps({"profiled": args.profile_precision, "steps": args.warmup + args.steps,
@@ -785,6 +849,7 @@ def main():
     ap.add_argument("--no-variants", action="store_true", help="skip every variant (precision, batch, learned)")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-pulse batch variant")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-guess variant")
+    ap.add_argument("--no-large", action="store_true", help="skip the NKappa=16 whole-pulse variant")
     ap.add_argument("--batch-steps", type=int, default=10, help="timed batch steps of the batch variant")
     ap.add_argument("--learned-steps", type=int, default=200, help="steps per pulse of the learned variant")
     ap.add_argument("--operator", default="auto", choices=["auto", "assembled", "matrix-free"],
@@ -792,6 +857,11 @@ def main():
                          "run that distorts that timing names it)")
     ap.add_argument("--profile-precision", default=None, choices=["fp64", "mixed"],
                     help="only run this precision's steps (for profiler captures)")
+    ap.add_argument("--profile-workload", default=WORKLOAD, choices=["dipole_small", WORKLOAD, "nondipole_large"],
+                    help="workload of the profile-only run")
+    ap.add_argument("--profile-from", type=int, default=0,
+                    help="profile-only run: first step (0-based) of the pulse to run, from psi0 (e.g. the pulse "
+                         "peak, where BiCGSTAB iterates)")
     if len(sys.argv) > 1 and sys.argv[1] == "--cpu-worker":
         return cpu_worker(sys.argv[2:])
     args = ap.parse_args()

@@ -156,6 +156,27 @@ __host__ __device__ inline dd dd_from(double v)
     return r;
 }
 __device__ __forceinline__ double dd_to(dd a) { return (double)a.hi + (double)a.lo; }
+/* the same split without double -> float conversions (which run at the FP64
+   rate on GB300): hi keeps the sign, exponent and top 23 stored mantissa
+   bits (truncation, exact), lo the remaining 29 bits as a float (one
+   integer -> float conversion and a power-of-two scale), so hi + lo is v
+   within 2^-47 relative.  Below 2^-74 lo is dropped (float precision) and
+   below 2^-126 the value is 0: terms that small do not register in sums of
+   the tables' magnitudes. */
+__device__ __forceinline__ dd dd_from_bits(double v)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const unsigned sign = (unsigned)(b >> 63) << 31;
+    const int e11 = (int)((b >> 52) & 0x7FF);
+    const int e8 = e11 - 1023 + 127;
+    dd r;
+    if (e8 <= 0) { r.hi = 0.f; r.lo = 0.f; return r; }
+    r.hi = __uint_as_float(sign | ((unsigned)e8 << 23) | (unsigned)((b >> 29) & 0x7FFFFF));
+    const unsigned rem = (unsigned)(b & 0x1FFFFFFFull);   /* units of 2^(e11 - 1075) */
+    const int t = e11 - 1075 + 127;
+    r.lo = (t > 0 && rem) ? (float)rem * __uint_as_float(sign | ((unsigned)t << 23)) : 0.f;
+    return r;
+}
 __device__ __forceinline__ dd dd_neg(dd a) { dd r; r.hi = -a.hi; r.lo = -a.lo; return r; }
 /* acc += a b */
 __device__ __forceinline__ void dd_fma(dd &acc, dd a, dd b)
@@ -560,15 +581,21 @@ __global__ void k_tables(TabP T, const double2 *__restrict__ coef)
             m.d = fma(kap, pgt[3], pgt[1]);
             const size_t e = mo + ((size_t)l * T.nk + kk) * per_l + slot;
             if (OUT & 1) ((R4<double>::T *)T.M)[e] = m;
-            if (OUT & 2) {
+            if (OUT & 4) {
+                /* double-float split by bit operations; the complex64 copy is
+                   its high part (truncated rather than rounded to float) */
+                R4dd f;
+                f.a = dd_from_bits(m.a); f.b = dd_from_bits(m.b); f.c = dd_from_bits(m.c); f.d = dd_from_bits(m.d);
+                ((R4dd *)T.Mdd)[e] = f;
+                if (OUT & 2) {
+                    R4<float>::T h;
+                    h.a = f.a.hi; h.b = f.b.hi; h.c = f.c.hi; h.d = f.d.hi;
+                    ((R4<float>::T *)T.M32)[e] = h;
+                }
+            } else if (OUT & 2) {
                 R4<float>::T f;
                 f.a = (float)m.a; f.b = (float)m.b; f.c = (float)m.c; f.d = (float)m.d;
                 ((R4<float>::T *)T.M32)[e] = f;
-            }
-            if (OUT & 4) {
-                R4dd f;
-                f.a = dd_from(m.a); f.b = dd_from(m.b); f.c = dd_from(m.c); f.d = dd_from(m.d);
-                ((R4dd *)T.Mdd)[e] = f;
             }
         }
     } else {
@@ -705,8 +732,11 @@ __host__ __device__ __forceinline__ ApplySmem apply_smem(int CS, int W, int RM, 
  * contracted vectors u, w, u', w' of a column are interleaved (one 32- or
  * 64-byte record) and so are the four angular factors of a term.
  */
+#ifndef GADE_DD_MINB
+#define GADE_DD_MINB 2     /* resident CTAs per SM the double-float instance is compiled for */
+#endif
 template <typename R, bool RC, bool SEP, bool Z>
-__global__ void __launch_bounds__(256, (sizeof(R) == 8 && SEP) ? 2 : 3)
+__global__ void __launch_bounds__(256, std::is_same<R, dd>::value ? GADE_DD_MINB : ((sizeof(R) == 8 && SEP) ? 2 : 3))
     k_apply(OpP P, const typename Cx<R>::T *__restrict__ x, int mode, VecP V, RedP red)
 {
     /* Z: the DKB zero blocks hold (slots laid out by column half): the
