@@ -10,10 +10,12 @@
  * precision step then starts from x_n + (x_n - x_{n-1}) + U c.  Everything
  * here works on device pointers handed in by the host; nothing allocates.
  *
- * Tensor-core path: mma.sync.aligned.m16n8k16 (BF16 in, FP32 accumulate)
- * from shared-memory tiles.  The GEMMs of this network are a few MFLOP per
- * step (M = pulses, N = 256), far from any roofline; the kernels favour
- * exact, checkable arithmetic over peak throughput.
+ * Tensor-core path: tcgen05.mma (BF16 in, FP32 accumulate in tensor
+ * memory) from shared-memory tiles, one elected thread issuing, completion
+ * tracked by mbarriers.  The GEMMs of this network are a few MFLOP per step
+ * (M = pulses, N = 256) and ~1 GFLOP per training epoch, far from any
+ * roofline; the kernels favour exact, checkable arithmetic over peak
+ * throughput.
  */
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -42,23 +44,50 @@ static int lfail(int code, const char *what, cudaError_t e)
 typedef __nv_bfloat16 bf16;
 
 /* ------------------------------------------------------------------ */
-/* GEMM: C = epi(A B + bias)                                           */
+/* GEMM: C = epi(A B + bias) on the 5th-generation tensor cores         */
 /* ------------------------------------------------------------------ */
 /* A(i,k) = A[i*sa0 + k*sa1], B(k,j) = B[k*sb0 + j*sb1] (any transposition),
  * FP32 accumulation.  Epilogue: + bias[j]; times (mask(i,j) > 0) when a
  * mask is given (ReLU backward); ReLU when act = 1; FP32 result to C and/or
- * a BF16 copy to C16. */
-#define GBM 64
-#define GBN 64
-#define GBK 32
-#define GPAD 8
+ * a BF16 copy to C16.
+ *
+ * One CTA computes a 128 x 64 tile of C with tcgen05.mma (kind::f16, BF16
+ * A and B, FP32 accumulator in tensor memory, M = 128, N = 64, K = 16 per
+ * instruction).  The four warps stage 64-wide K blocks of A and B in
+ * shared memory in the no-swizzle K-major layout of 8-row x 16-byte core
+ * matrices (element (r, k) at (r/8)*GSBO + (k/8)*GLBO + (r%8)*16 + (k%8)*2
+ * bytes), two buffers deep: while the tensor core multiplies block k (four
+ * MMAs issued by one thread, completion signalled by tcgen05.commit on the
+ * buffer's mbarrier) the warps stage block k+1.  The accumulator is read
+ * back with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31 = rows of the
+ * tile) for the epilogue.  Every mbarrier wait is bounded: on a timeout the
+ * CTA records it in the library's learned-kernel status word, waits
+ * (bounded) for its MMAs in flight, frees its tensor memory and returns. */
+#define GTM 128
+#define GTN 64
+#define GTK 64
+#define GLBO 128                         /* bytes between K-adjacent core matrices */
+#define GSBO ((GTK / 8) * 128)           /* bytes between 8-row groups */
+#define GSTAGE ((GTM + GTN) * GTK * 2)   /* bytes of one buffer: A then B */
+#define GSPIN (1u << 24)
 
-__device__ __forceinline__ void mma_bf16(float (&c)[4], const uint32_t (&a)[4], const uint32_t (&b)[2])
+static __device__ unsigned g_learned_err;   /* bit 0: a tensor-core wait ran out */
+
+__device__ __forceinline__ unsigned l_smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ bool l_try_wait(uint64_t *bar, unsigned parity)
 {
-    asm volatile("mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
-                 "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};"
-                 : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
-                 : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+    unsigned ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok) : "r"(l_smem_u32(bar)), "r"(parity) : "memory");
+    return ok != 0;
+}
+/* shared-memory matrix descriptor: start address, leading (K) and stride
+   (8-row group) byte offsets, the tcgen05 descriptor version, no swizzle */
+__device__ __forceinline__ uint64_t l_sdesc(unsigned addr)
+{
+    return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)((GLBO >> 4) & 0x3FFF) << 16) |
+           ((uint64_t)((GSBO >> 4) & 0x3FFF) << 32) | (1ull << 46);
 }
 
 __global__ void __launch_bounds__(128) k_gemm_bf16(int M, int N, int K, const bf16 *__restrict__ A, long long sa0,
@@ -68,72 +97,119 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(int M, int N, int K, const bf
                                                    float *__restrict__ C, long long ldc, bf16 *__restrict__ C16,
                                                    long long ldc16)
 {
-    __shared__ __align__(16) bf16 As[GBM][GBK + GPAD];   /* [i][k] */
-    __shared__ __align__(16) bf16 Bs[GBN][GBK + GPAD];   /* [j][k] */
-    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    const int wm = warp >> 1, wn = warp & 1;             /* 2 x 2 warps of 32 x 32 */
-    const int i0 = blockIdx.y * GBM, j0 = blockIdx.x * GBN;
-    float acc[2][4][4];
-#pragma unroll
-    for (int a = 0; a < 2; a++)
-#pragma unroll
-        for (int b = 0; b < 4; b++)
-#pragma unroll
-            for (int c = 0; c < 4; c++) acc[a][b][c] = 0.f;
-    const bf16 zero = __float2bfloat16(0.f);
-    for (int k0 = 0; k0 < K; k0 += GBK) {
-        for (int e = tid; e < GBM * GBK; e += 128) {
-            const int r = e / GBK, k = e % GBK;
-            const int gi = i0 + r, gk = k0 + k;
-            As[r][k] = (gi < M && gk < K) ? A[gi * sa0 + gk * sa1] : zero;
-        }
-        for (int e = tid; e < GBN * GBK; e += 128) {
-            const int c = e / GBK, k = e % GBK;
-            const int gj = j0 + c, gk = k0 + k;
-            Bs[c][k] = (gj < N && gk < K) ? B[gk * sb0 + gj * sb1] : zero;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int kk = 0; kk < GBK; kk += 16) {
-            uint32_t af[2][4], bfr[4][2];
-            const int kc = kk + (lane & 3) * 2;
-#pragma unroll
-            for (int mt = 0; mt < 2; mt++) {
-                const int r = wm * 32 + mt * 16 + (lane >> 2);
-                af[mt][0] = *(const uint32_t *)&As[r][kc];
-                af[mt][1] = *(const uint32_t *)&As[r + 8][kc];
-                af[mt][2] = *(const uint32_t *)&As[r][kc + 8];
-                af[mt][3] = *(const uint32_t *)&As[r + 8][kc + 8];
-            }
-#pragma unroll
-            for (int nt = 0; nt < 4; nt++) {
-                const int c = wn * 32 + nt * 8 + (lane >> 2);
-                bfr[nt][0] = *(const uint32_t *)&Bs[c][kc];
-                bfr[nt][1] = *(const uint32_t *)&Bs[c][kc + 8];
-            }
-#pragma unroll
-            for (int mt = 0; mt < 2; mt++)
-#pragma unroll
-                for (int nt = 0; nt < 4; nt++) mma_bf16(acc[mt][nt], af[mt], bfr[nt]);
-        }
-        __syncthreads();
+    extern __shared__ __align__(1024) unsigned char gsm[];   /* [2][A 128x64 | B 64x64] */
+    __shared__ __align__(8) uint64_t bar[2];
+    __shared__ unsigned tmem_base;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int i0 = blockIdx.y * GTM, j0 = blockIdx.x * GTN;
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(l_smem_u32(&tmem_base)),
+                     "r"(GTN) : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
     }
-#pragma unroll
-    for (int mt = 0; mt < 2; mt++)
-#pragma unroll
-        for (int nt = 0; nt < 4; nt++)
-#pragma unroll
-            for (int h = 0; h < 4; h++) {
-                const int i = i0 + wm * 32 + mt * 16 + (lane >> 2) + (h >= 2 ? 8 : 0);
-                const int j = j0 + wn * 32 + nt * 8 + (lane & 3) * 2 + (h & 1);
-                if (i >= M || j >= N) continue;
-                float v = acc[mt][nt][h];
-                if (bias) v += bias[j];
-                if (mask && !(mask[i * ldm + j] > 0.f)) v = 0.f;
-                if (act == 1) v = v > 0.f ? v : 0.f;
-                if (C) C[i * ldc + j] = v;
-                if (C16) C16[i * ldc16 + j] = __float2bfloat16(v);
+    if (tid == 0) {
+        for (int b = 0; b < 2; b++)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(l_smem_u32(&bar[b])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const unsigned tmem = tmem_base;
+    /* instruction descriptor: FP32 accumulator, BF16 A and B, both K-major, N, M */
+    const unsigned idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(GTN >> 3) << 17) |
+                           ((unsigned)(GTM >> 4) << 24);
+    const bf16 zero = __float2bfloat16(0.f);
+    const int nkb = (K + GTK - 1) / GTK;
+    bool ok = true;
+    int issued = 0;                            /* K blocks whose MMAs were committed */
+    for (int kb = 0; kb < nkb; kb++) {
+        const int b = kb & 1, k0 = kb * GTK;
+        unsigned char *As = gsm + b * GSTAGE, *Bs = As + GTM * GTK * 2;
+        if (kb >= 2) {                         /* the MMAs of block kb-2 are done with this buffer */
+            unsigned spins = 0;
+            while (!l_try_wait(&bar[b], ((kb - 2) >> 1) & 1))
+                if (++spins > GSPIN) { ok = false; break; }
+        }
+        if (__syncthreads_or(!ok)) break;
+        for (int e = tid; e < GTM * GTK; e += 128) {
+            const int r = e / GTK, k = e % GTK;
+            const int gi = i0 + r, gk = k0 + k;
+            *(bf16 *)(As + (r >> 3) * GSBO + (k >> 3) * GLBO + (r & 7) * 16 + (k & 7) * 2) =
+                (gi < M && gk < K) ? A[gi * sa0 + gk * sa1] : zero;
+        }
+        for (int e = tid; e < GTN * GTK; e += 128) {
+            const int c = e / GTK, k = e % GTK;
+            const int gj = j0 + c, gk = k0 + k;
+            *(bf16 *)(Bs + (c >> 3) * GSBO + (k >> 3) * GLBO + (c & 7) * 16 + (k & 7) * 2) =
+                (gj < N && gk < K) ? B[gk * sb0 + gj * sb1] : zero;
+        }
+        /* the generic-proxy stores become visible to the tensor core */
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        if (tid == 0) {
+            for (int kk = 0; kk < GTK / 16; kk++) {
+                const uint64_t ad = l_sdesc(l_smem_u32(As) + kk * 2 * GLBO);
+                const uint64_t bd = l_sdesc(l_smem_u32(Bs) + kk * 2 * GLBO);
+                const unsigned accumulate = (kb > 0 || kk > 0) ? 1u : 0u;
+                asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                             "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+                             "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate) : "memory");
             }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             l_smem_u32(&bar[b])) : "memory");
+        }
+        issued = kb + 1;
+    }
+    /* the last commit covers every MMA issued before it */
+    if (ok && issued > 0) {
+        const int last = issued - 1;
+        unsigned spins = 0;
+        while (!l_try_wait(&bar[last & 1], (last >> 1) & 1))
+            if (++spins > GSPIN) { ok = false; break; }
+    }
+    ok = !__syncthreads_or(!ok);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (ok) {
+        const int i = i0 + warp * 32 + lane;
+        for (int c0 = 0; c0 < GTN; c0 += 16) {
+            unsigned v[16];
+            const unsigned taddr = tmem + ((unsigned)(warp * 32) << 16) + (unsigned)c0;
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+                         "%14,%15}, [%16];"
+                         : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                           "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+                           "=r"(v[14]), "=r"(v[15])
+                         : "r"(taddr));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (i >= M) continue;
+#pragma unroll
+            for (int q = 0; q < 16; q++) {
+                const int j = j0 + c0 + q;
+                if (j >= N) continue;
+                float val = issued > 0 ? __uint_as_float(v[q]) : 0.f;   /* K = 0: no MMA wrote TMEM */
+                if (bias) val += bias[j];
+                if (mask && !(mask[i * ldm + j] > 0.f)) val = 0.f;
+                if (act == 1) val = val > 0.f ? val : 0.f;
+                if (C) C[i * ldc + j] = val;
+                if (C16) C16[i * ldc16 + j] = __float2bfloat16(val);
+            }
+        }
+    } else if (tid == 0) {
+        atomicOr(&g_learned_err, 1u);
+        if (issued > 0) {                      /* bounded wait for the MMAs still in flight */
+            const int last = issued - 1;
+            unsigned spins = 0;
+            while (!l_try_wait(&bar[last & 1], (last >> 1) & 1) && ++spins < GSPIN) {
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(GTN) : "memory");
 }
 
 extern "C" int gade_gemm_bf16(int32_t M, int32_t N, int32_t K, const void *A, int64_t sa0, int64_t sa1,
@@ -144,10 +220,28 @@ extern "C" int gade_gemm_bf16(int32_t M, int32_t N, int32_t K, const void *A, in
     if (M < 0 || N < 0 || K < 0 || !A || !B || (!C && !C16) || (act != 0 && act != 1))
         return gade_set_error(GADE_ERR_ARG, "gade_gemm_bf16: bad argument");
     if (M == 0 || N == 0) return GADE_OK;
-    dim3 grid((N + GBN - 1) / GBN, (M + GBM - 1) / GBM);
-    k_gemm_bf16<<<grid, 128, 0, (cudaStream_t)stream>>>(M, N, K, (const bf16 *)A, sa0, sa1, (const bf16 *)B, sb0, sb1,
-                                                         bias, mask, ldm, act, C, ldc, (bf16 *)C16, ldc16);
+    static bool smem_set = false;        /* 2 x 24 KB dynamic shared memory is above the 48 KB default */
+    if (!smem_set) {
+        cudaError_t e = cudaFuncSetAttribute(k_gemm_bf16, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * GSTAGE);
+        if (e != cudaSuccess) return lfail(GADE_ERR_CUDA, "gade_gemm_bf16", e);
+        smem_set = true;
+    }
+    dim3 grid((N + GTN - 1) / GTN, (M + GTM - 1) / GTM);
+    k_gemm_bf16<<<grid, 128, 2 * GSTAGE, (cudaStream_t)stream>>>(M, N, K, (const bf16 *)A, sa0, sa1,
+                                                                 (const bf16 *)B, sb0, sb1, bias, mask, ldm, act,
+                                                                 C, ldc, (bf16 *)C16, ldc16);
     LCK("gade_gemm_bf16");
+    return GADE_OK;
+}
+
+extern "C" int gade_learned_status(int32_t *flags)
+{
+    if (!flags) return gade_set_error(GADE_ERR_ARG, "gade_learned_status: NULL argument");
+    unsigned v = 0, z = 0;
+    cudaError_t e = cudaMemcpyFromSymbol(&v, g_learned_err, sizeof(v));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_learned_err, &z, sizeof(z));
+    if (e != cudaSuccess) return lfail(GADE_ERR_CUDA, "gade_learned_status", e);
+    *flags = (int32_t)v;
     return GADE_OK;
 }
 

@@ -22,8 +22,8 @@
 extern "C" {
 #endif
 
-/* C = epi(A B + bias) on the tensor cores (BF16 operands, FP32
- * accumulation).  A(i,k) = A[i*sa0 + k*sa1] (M x K), B(k,j) = B[k*sb0 +
+/* C = epi(A B + bias) on the tensor cores (tcgen05.mma, BF16 operands,
+ * FP32 accumulation in tensor memory).  A(i,k) = A[i*sa0 + k*sa1] (M x K), B(k,j) = B[k*sb0 +
  * j*sb1] (K x N), so either operand may be read transposed.  bias [N] may be
  * NULL.  mask (M x N, row stride ldm) may be NULL; where mask <= 0 the
  * result is 0 (ReLU backward).  act: 0 none, 1 ReLU.  C (FP32, row stride
@@ -31,6 +31,11 @@ extern "C" {
 int gade_gemm_bf16(int32_t M, int32_t N, int32_t K, const void *A, int64_t sa0, int64_t sa1,
                    const void *B, int64_t sb0, int64_t sb1, const float *bias, const float *mask,
                    int64_t ldm, int32_t act, float *C, int64_t ldc, void *C16, int64_t ldc16, void *stream);
+
+/* Status of the learned-model kernels since the last call (synchronous,
+ * clears it): bit 0 = a tensor-core wait of gade_gemm_bf16 ran out (the
+ * tile it was computing was not written). */
+int gade_learned_status(int32_t *flags);
 
 /* mean squared error of out against target (M x N, FP32): gradient
  * 2 (out - target)/(M N) into grad (FP32, may be NULL) and grad16 (BF16);

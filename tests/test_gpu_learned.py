@@ -1,7 +1,7 @@
 """GPU kernels of the learned initial guess against the numpy oracle
 (oracle/mlp.py) and numpy linear algebra:
 
-  * BF16 tensor-core GEMM (every transposition, ragged sizes, bias, ReLU,
+  * BF16 tcgen05 GEMM (every transposition, ragged sizes, bias, ReLU,
     mask): relative error <= 1e-5 against float64 products of the same
     BF16-rounded operands (FP32 accumulation)
   * MLP loss gradients: relative Frobenius error <= 2e-3 per parameter
@@ -9,6 +9,8 @@
   * Adam: <= 1e-5 relative against the float64 update
   * POD projection / expansion: <= 1e-6 relative (complex64 basis)
 """
+import ctypes
+
 import numpy as np
 import pytest
 import torch
@@ -55,6 +57,9 @@ def test_gemm_bf16(native_lib, M_, N_, K_, ta, tb):
         got = C.cpu().numpy().astype(np.float64)
         assert _rel(got, ref) <= 1e-5, (act, use_mask)
         assert np.array_equal(C16.float().cpu().numpy(), M.bf16(got).astype(np.float32))
+    flags = ctypes.c_int32(-1)
+    native.call("gade_learned_status", ctypes.byref(flags))
+    assert flags.value == 0                     # no tensor-core wait ran out
 
 
 def test_mlp_gradients_match_oracle(native_lib):
