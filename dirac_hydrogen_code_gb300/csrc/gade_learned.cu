@@ -18,6 +18,7 @@
  * throughput.
  */
 #include <cuda_bf16.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -53,25 +54,44 @@ typedef __nv_bfloat16 bf16;
  *
  * One CTA computes a 128 x 64 tile of C with tcgen05.mma (kind::f16, BF16
  * A and B, FP32 accumulator in tensor memory, M = 128, N = 64, K = 16 per
- * instruction).  The four warps stage 64-wide K blocks of A and B in
- * shared memory in the no-swizzle K-major layout of 8-row x 16-byte core
- * matrices (element (r, k) at (r/8)*GSBO + (k/8)*GLBO + (r%8)*16 + (k%8)*2
- * bytes), two buffers deep: while the tensor core multiplies block k (four
- * MMAs issued by one thread, completion signalled by tcgen05.commit on the
- * buffer's mbarrier) the warps stage block k+1.  The accumulator is read
- * back with tcgen05.ld (warp w owns TMEM lanes 32w..32w+31 = rows of the
- * tile) for the epilogue.  Every mbarrier wait is bounded: on a timeout the
- * CTA records it in the library's learned-kernel status word, waits
- * (bounded) for its MMAs in flight, frees its tensor memory and returns. */
+ * instruction), 64-wide K blocks staged in shared memory in the no-swizzle
+ * canonical layouts of 8 x 16-byte core matrices: element (r, k) of an
+ * operand tile (r along M or N, k along K) sits at
+ *     (r/8)*SBO + (k/8)*LBO + (r%8)*16 + (k%8)*2          (K-major)
+ *     (r/8)*SBO + (k/8)*LBO + (k%8)*16 + (r%8)*2          (M/N-major)
+ * bytes, LBO and SBO in the shared-memory descriptor of each MMA.
+ *
+ * k_gemm_tma (operands 16-byte aligned with 16-byte row strides): one
+ * thread fills a GST-deep ring of stages with 2-D tensor copies
+ * (cp.async.bulk.tensor, boxes 16 bytes wide so that each copy lands as a
+ * column of core matrices; out-of-range rows and columns arrive as zeros),
+ * one thread issues the MMAs of a stage once its mbarrier has seen all
+ * bytes and frees the stage with tcgen05.commit on the stage's empty
+ * mbarrier, and all four warps read the accumulator back with tcgen05.ld
+ * (warp w owns TMEM lanes 32w..32w+31 = tile rows) for the epilogue.  An
+ * operand contiguous along K is staged K-major; one contiguous along M or N
+ * is staged M/N-major with the descriptor's transpose bit, so no operand is
+ * transposed by the SMs.
+ *
+ * k_gemm_ld (any strides): the four warps stage each K block with plain
+ * loads into two K-major buffers while the tensor core multiplies the
+ * other.
+ *
+ * Every mbarrier wait is bounded: on a timeout the CTA records it in the
+ * learned-kernel status word, waits (bounded) for its copies and MMAs in
+ * flight, frees its tensor memory and returns without writing its tile. */
 #define GTM 128
 #define GTN 64
 #define GTK 64
-#define GLBO 128                         /* bytes between K-adjacent core matrices */
-#define GSBO ((GTK / 8) * 128)           /* bytes between 8-row groups */
-#define GSTAGE ((GTM + GTN) * GTK * 2)   /* bytes of one buffer: A then B */
-#define GSPIN (1u << 24)
+#define GST 4                            /* stages of the tensor-copy ring */
+#define GSTAGE ((GTM + GTN) * GTK * 2)   /* bytes of one stage: A then B */
+#define GSPIN_DEFAULT (1u << 24)
+#define GDRAIN (1u << 24)
 
 static __device__ unsigned g_learned_err;   /* bit 0: a tensor-core wait ran out */
+static unsigned g_gemm_spin = GSPIN_DEFAULT; /* waits before a CTA gives up */
+static int g_gemm_path = 0;                  /* 0 automatic, 1 plain loads */
+static int g_gemm_withhold = 0;              /* 1: the copy thread issues nothing */
 
 __device__ __forceinline__ unsigned l_smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
 __device__ __forceinline__ bool l_try_wait(uint64_t *bar, unsigned parity)
@@ -82,31 +102,206 @@ __device__ __forceinline__ bool l_try_wait(uint64_t *bar, unsigned parity)
                  : "=r"(ok) : "r"(l_smem_u32(bar)), "r"(parity) : "memory");
     return ok != 0;
 }
+/* bounded wait; false when it ran out (or another thread of the CTA gave up) */
+__device__ __forceinline__ bool l_wait(uint64_t *bar, unsigned parity, unsigned limit, volatile int *fail)
+{
+    for (unsigned spins = 0; !l_try_wait(bar, parity);)
+        if (++spins > limit || (fail && *fail)) return false;
+    return true;
+}
 /* shared-memory matrix descriptor: start address, leading (K) and stride
    (8-row group) byte offsets, the tcgen05 descriptor version, no swizzle */
-__device__ __forceinline__ uint64_t l_sdesc(unsigned addr)
+__device__ __forceinline__ uint64_t l_sdesc(unsigned addr, unsigned lbo, unsigned sbo)
 {
-    return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)((GLBO >> 4) & 0x3FFF) << 16) |
-           ((uint64_t)((GSBO >> 4) & 0x3FFF) << 32) | (1ull << 46);
+    return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | (1ull << 46);
+}
+/* instruction descriptor: FP32 accumulator, BF16 A and B, A/B M/N-major when
+   a_mn/b_mn (transpose bits), N and M of the tile */
+__device__ __forceinline__ unsigned l_idesc(bool a_mn, bool b_mn)
+{
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((a_mn ? 1u : 0u) << 15) | ((b_mn ? 1u : 0u) << 16) |
+           ((unsigned)(GTN >> 3) << 17) | ((unsigned)(GTM >> 4) << 24);
+}
+__device__ __forceinline__ void l_mma(unsigned tmem, uint64_t ad, uint64_t bd, unsigned idesc, unsigned acc)
+{
+    asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                 "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+                 "l"(ad), "l"(bd), "r"(idesc), "r"(acc) : "memory");
+}
+__device__ __forceinline__ void l_commit(uint64_t *bar)
+{
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     l_smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void l_tmem_alloc(unsigned *dst)
+{
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(l_smem_u32(dst)),
+                 "r"(GTN) : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void l_tmem_free(unsigned tmem)
+{
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(GTN) : "memory");
 }
 
-__global__ void __launch_bounds__(128) k_gemm_bf16(int M, int N, int K, const bf16 *__restrict__ A, long long sa0,
-                                                   long long sa1, const bf16 *__restrict__ B, long long sb0,
-                                                   long long sb1, const float *__restrict__ bias,
-                                                   const float *__restrict__ mask, long long ldm, int act,
-                                                   float *__restrict__ C, long long ldc, bf16 *__restrict__ C16,
-                                                   long long ldc16)
+/* accumulator rows -> epilogue -> C / C16; warp w reads TMEM lanes 32w.. */
+__device__ __forceinline__ void l_epilogue(unsigned tmem, bool have_acc, int M, int N, int i0, int j0,
+                                           const float *__restrict__ bias, const float *__restrict__ mask,
+                                           long long ldm, int act, float *__restrict__ C, long long ldc,
+                                           bf16 *__restrict__ C16, long long ldc16)
+{
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i = i0 + warp * 32 + lane;
+    for (int c0 = 0; c0 < GTN; c0 += 16) {
+        if (j0 + c0 >= N) break;               /* warp-uniform */
+        unsigned v[16];
+        const unsigned taddr = tmem + ((unsigned)(warp * 32) << 16) + (unsigned)c0;
+        asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+                     "%14,%15}, [%16];"
+                     : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+                       "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+                       "=r"(v[14]), "=r"(v[15])
+                     : "r"(taddr));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (i >= M) continue;
+#pragma unroll
+        for (int q = 0; q < 16; q++) {
+            const int j = j0 + c0 + q;
+            if (j >= N) continue;
+            float val = have_acc ? __uint_as_float(v[q]) : 0.f;   /* K = 0: no MMA wrote TMEM */
+            if (bias) val += bias[j];
+            if (mask && !(mask[i * ldm + j] > 0.f)) val = 0.f;
+            if (act == 1) val = val > 0.f ? val : 0.f;
+            if (C) C[i * ldc + j] = val;
+            if (C16) C16[i * ldc16 + j] = __float2bfloat16(val);
+        }
+    }
+}
+
+__device__ __forceinline__ void l_tma2d(unsigned dst, const CUtensorMap *map, int x, int y, uint64_t *bar)
+{
+    asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, "
+                 "%3}], [%4];" ::"r"(dst),
+                 "l"((uint64_t)map), "r"(x), "r"(y), "r"(l_smem_u32(bar)) : "memory");
+}
+
+/* A_MN: A staged M-major (A contiguous along M), else K-major; B_MN likewise
+   along N.  Tensor maps: K-major operand {K, rows}, box {8, rows of the
+   tile}, one copy per 8-wide K slice (LBO = rows x 16 B, SBO = 128 B);
+   M/N-major operand {rows, K}, box {8, 64}, one copy per 8 rows (LBO =
+   128 B, SBO = 1 KB).  Every x coordinate is a multiple of 8 elements. */
+template <bool A_MN, bool B_MN>
+__global__ void __launch_bounds__(128) k_gemm_tma(const __grid_constant__ CUtensorMap mapA,
+                                                  const __grid_constant__ CUtensorMap mapB, int M, int N, int K,
+                                                  const float *__restrict__ bias, const float *__restrict__ mask,
+                                                  long long ldm, int act, float *__restrict__ C, long long ldc,
+                                                  bf16 *__restrict__ C16, long long ldc16, unsigned spin_limit,
+                                                  int withhold)
+{
+    extern __shared__ __align__(1024) unsigned char gsm[];   /* [GST][A 128x64 | B 64x64] */
+    __shared__ __align__(8) uint64_t full[GST], empty[GST];
+    __shared__ unsigned tmem_base;
+    __shared__ int s_copied, s_issued;          /* K blocks copied / multiplied */
+    __shared__ volatile int s_fail;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int i0 = blockIdx.y * GTM, j0 = blockIdx.x * GTN;
+    constexpr unsigned A_LBO = A_MN ? 128 : GTM * 16, A_SBO = A_MN ? 1024 : 128;
+    constexpr unsigned B_LBO = B_MN ? 128 : GTN * 16, B_SBO = B_MN ? 1024 : 128;
+    if (warp == 0) l_tmem_alloc(&tmem_base);
+    if (tid == 0) {
+        for (int b = 0; b < GST; b++) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(l_smem_u32(&full[b])) : "memory");
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(l_smem_u32(&empty[b])) : "memory");
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        s_copied = 0;
+        s_issued = 0;
+        s_fail = 0;
+    }
+    if (tid == 32) {
+        asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&mapA) : "memory");
+        asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)&mapB) : "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const unsigned tmem = tmem_base;
+    const int nkb = (K + GTK - 1) / GTK;
+    const unsigned gbase = l_smem_u32(gsm);
+
+    if (tid == 0) {                            /* copy thread */
+        for (int kb = 0; kb < nkb && !withhold; kb++) {
+            const int st = kb % GST, k0 = kb * GTK;
+            if (kb >= GST && !l_wait(&empty[st], ((kb / GST) - 1) & 1, spin_limit, &s_fail)) {
+                s_fail = 1;
+                break;
+            }
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(l_smem_u32(&full[st])),
+                         "r"(GSTAGE) : "memory");
+            const unsigned As = gbase + st * GSTAGE, Bs = As + GTM * GTK * 2;
+            if (A_MN)
+                for (int g = 0; g < GTM / 8; g++) l_tma2d(As + g * 1024, &mapA, i0 + 8 * g, k0, &full[st]);
+            else
+                for (int q = 0; q < GTK / 8; q++) l_tma2d(As + q * GTM * 16, &mapA, k0 + 8 * q, i0, &full[st]);
+            if (B_MN)
+                for (int g = 0; g < GTN / 8; g++) l_tma2d(Bs + g * 1024, &mapB, j0 + 8 * g, k0, &full[st]);
+            else
+                for (int q = 0; q < GTK / 8; q++) l_tma2d(Bs + q * GTN * 16, &mapB, k0 + 8 * q, j0, &full[st]);
+            s_copied = kb + 1;
+        }
+    } else if (tid == 32) {                    /* MMA thread */
+        const unsigned idesc = l_idesc(A_MN, B_MN);
+        for (int kb = 0; kb < nkb; kb++) {
+            const int st = kb % GST;
+            if (!l_wait(&full[st], (kb / GST) & 1, spin_limit, &s_fail)) {
+                s_fail = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const unsigned As = gbase + st * GSTAGE, Bs = As + GTM * GTK * 2;
+#pragma unroll
+            for (int kk = 0; kk < GTK / 16; kk++)
+                l_mma(tmem, l_sdesc(As + kk * 2 * A_LBO, A_LBO, A_SBO), l_sdesc(Bs + kk * 2 * B_LBO, B_LBO, B_SBO),
+                      idesc, (kb > 0 || kk > 0) ? 1u : 0u);
+            l_commit(&empty[st]);              /* frees the stage; the last one also marks the end */
+            s_issued = kb + 1;
+        }
+    }
+    __syncthreads();
+    /* every thread: the last commit covers every MMA issued before it */
+    bool ok = !s_fail;
+    if (ok && nkb > 0) ok = l_wait(&empty[(nkb - 1) % GST], ((nkb - 1) / GST) & 1, spin_limit, nullptr);
+    ok = !__syncthreads_or(!ok);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (ok) {
+        l_epilogue(tmem, nkb > 0, M, N, i0, j0, bias, mask, ldm, act, C, ldc, C16, ldc16);
+    } else if (tid == 0) {
+        atomicOr(&g_learned_err, 1u);
+        /* copies in flight: the stages copied and not yet seen complete */
+        for (int kb = s_copied - GST > 0 ? s_copied - GST : 0; kb < s_copied; kb++)
+            l_wait(&full[kb % GST], (kb / GST) & 1, GDRAIN, nullptr);
+        if (s_issued > 0) l_wait(&empty[(s_issued - 1) % GST], ((s_issued - 1) / GST) & 1, GDRAIN, nullptr);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) l_tmem_free(tmem);
+}
+
+__global__ void __launch_bounds__(128) k_gemm_ld(int M, int N, int K, const bf16 *__restrict__ A, long long sa0,
+                                                 long long sa1, const bf16 *__restrict__ B, long long sb0,
+                                                 long long sb1, const float *__restrict__ bias,
+                                                 const float *__restrict__ mask, long long ldm, int act,
+                                                 float *__restrict__ C, long long ldc, bf16 *__restrict__ C16,
+                                                 long long ldc16, unsigned spin_limit)
 {
     extern __shared__ __align__(1024) unsigned char gsm[];   /* [2][A 128x64 | B 64x64] */
     __shared__ __align__(8) uint64_t bar[2];
     __shared__ unsigned tmem_base;
-    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int tid = threadIdx.x, warp = tid >> 5;
     const int i0 = blockIdx.y * GTM, j0 = blockIdx.x * GTN;
-    if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(l_smem_u32(&tmem_base)),
-                     "r"(GTN) : "memory");
-        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
-    }
+    constexpr unsigned LBO = 128, SBO = (GTK / 8) * 128;   /* K-major, 8 core matrices per row group */
+    if (warp == 0) l_tmem_alloc(&tmem_base);
     if (tid == 0) {
         for (int b = 0; b < 2; b++)
             asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(l_smem_u32(&bar[b])) : "memory");
@@ -116,9 +311,7 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(int M, int N, int K, const bf
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const unsigned tmem = tmem_base;
-    /* instruction descriptor: FP32 accumulator, BF16 A and B, both K-major, N, M */
-    const unsigned idesc = (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(GTN >> 3) << 17) |
-                           ((unsigned)(GTM >> 4) << 24);
+    const unsigned idesc = l_idesc(false, false);
     const bf16 zero = __float2bfloat16(0.f);
     const int nkb = (K + GTK - 1) / GTK;
     bool ok = true;
@@ -126,22 +319,18 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(int M, int N, int K, const bf
     for (int kb = 0; kb < nkb; kb++) {
         const int b = kb & 1, k0 = kb * GTK;
         unsigned char *As = gsm + b * GSTAGE, *Bs = As + GTM * GTK * 2;
-        if (kb >= 2) {                         /* the MMAs of block kb-2 are done with this buffer */
-            unsigned spins = 0;
-            while (!l_try_wait(&bar[b], ((kb - 2) >> 1) & 1))
-                if (++spins > GSPIN) { ok = false; break; }
-        }
-        if (__syncthreads_or(!ok)) break;
+        if (kb >= 2) ok = l_wait(&bar[b], ((kb - 2) >> 1) & 1, spin_limit, nullptr);   /* block kb-2 done */
+        if (__syncthreads_or(!ok)) { ok = false; break; }
         for (int e = tid; e < GTM * GTK; e += 128) {
             const int r = e / GTK, k = e % GTK;
             const int gi = i0 + r, gk = k0 + k;
-            *(bf16 *)(As + (r >> 3) * GSBO + (k >> 3) * GLBO + (r & 7) * 16 + (k & 7) * 2) =
+            *(bf16 *)(As + (r >> 3) * SBO + (k >> 3) * LBO + (r & 7) * 16 + (k & 7) * 2) =
                 (gi < M && gk < K) ? A[gi * sa0 + gk * sa1] : zero;
         }
         for (int e = tid; e < GTN * GTK; e += 128) {
             const int c = e / GTK, k = e % GTK;
             const int gj = j0 + c, gk = k0 + k;
-            *(bf16 *)(Bs + (c >> 3) * GSBO + (k >> 3) * GLBO + (c & 7) * 16 + (k & 7) * 2) =
+            *(bf16 *)(Bs + (c >> 3) * SBO + (k >> 3) * LBO + (c & 7) * 16 + (k & 7) * 2) =
                 (gj < N && gk < K) ? B[gk * sb0 + gj * sb1] : zero;
         }
         /* the generic-proxy stores become visible to the tensor core */
@@ -150,66 +339,82 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(int M, int N, int K, const bf
         __syncthreads();
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         if (tid == 0) {
-            for (int kk = 0; kk < GTK / 16; kk++) {
-                const uint64_t ad = l_sdesc(l_smem_u32(As) + kk * 2 * GLBO);
-                const uint64_t bd = l_sdesc(l_smem_u32(Bs) + kk * 2 * GLBO);
-                const unsigned accumulate = (kb > 0 || kk > 0) ? 1u : 0u;
-                asm volatile("{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
-                             "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
-                             "l"(ad), "l"(bd), "r"(idesc), "r"(accumulate) : "memory");
-            }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                             l_smem_u32(&bar[b])) : "memory");
+            for (int kk = 0; kk < GTK / 16; kk++)
+                l_mma(tmem, l_sdesc(l_smem_u32(As) + kk * 2 * LBO, LBO, SBO),
+                      l_sdesc(l_smem_u32(Bs) + kk * 2 * LBO, LBO, SBO), idesc, (kb > 0 || kk > 0) ? 1u : 0u);
+            l_commit(&bar[b]);
         }
         issued = kb + 1;
     }
     /* the last commit covers every MMA issued before it */
-    if (ok && issued > 0) {
-        const int last = issued - 1;
-        unsigned spins = 0;
-        while (!l_try_wait(&bar[last & 1], (last >> 1) & 1))
-            if (++spins > GSPIN) { ok = false; break; }
-    }
+    if (ok && issued > 0) ok = l_wait(&bar[(issued - 1) & 1], ((issued - 1) >> 1) & 1, spin_limit, nullptr);
     ok = !__syncthreads_or(!ok);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     if (ok) {
-        const int i = i0 + warp * 32 + lane;
-        for (int c0 = 0; c0 < GTN; c0 += 16) {
-            unsigned v[16];
-            const unsigned taddr = tmem + ((unsigned)(warp * 32) << 16) + (unsigned)c0;
-            asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
-                         "%14,%15}, [%16];"
-                         : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
-                           "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
-                           "=r"(v[14]), "=r"(v[15])
-                         : "r"(taddr));
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-            if (i >= M) continue;
-#pragma unroll
-            for (int q = 0; q < 16; q++) {
-                const int j = j0 + c0 + q;
-                if (j >= N) continue;
-                float val = issued > 0 ? __uint_as_float(v[q]) : 0.f;   /* K = 0: no MMA wrote TMEM */
-                if (bias) val += bias[j];
-                if (mask && !(mask[i * ldm + j] > 0.f)) val = 0.f;
-                if (act == 1) val = val > 0.f ? val : 0.f;
-                if (C) C[i * ldc + j] = val;
-                if (C16) C16[i * ldc16 + j] = __float2bfloat16(val);
-            }
-        }
+        l_epilogue(tmem, issued > 0, M, N, i0, j0, bias, mask, ldm, act, C, ldc, C16, ldc16);
     } else if (tid == 0) {
         atomicOr(&g_learned_err, 1u);
-        if (issued > 0) {                      /* bounded wait for the MMAs still in flight */
-            const int last = issued - 1;
-            unsigned spins = 0;
-            while (!l_try_wait(&bar[last & 1], (last >> 1) & 1) && ++spins < GSPIN) {
-            }
-        }
+        if (issued > 0) l_wait(&bar[(issued - 1) & 1], ((issued - 1) >> 1) & 1, GDRAIN, nullptr);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
-    if (warp == 0)
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(GTN) : "memory");
+    if (warp == 0) l_tmem_free(tmem);
+}
+
+/* cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+   against the driver library) */
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+        cudaGetLastError();
+    }
+    return fn;
+}
+
+/* 2-D BF16 map of a (rows x inner) operand with row stride ld elements and
+   box {8, box_rows}; false when the layout does not allow tensor copies */
+static bool encode_operand(CUtensorMap *map, const void *base, long long inner, long long rows, long long ld,
+                           int box_rows)
+{
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc || ((uintptr_t)base & 15) || inner <= 0 || rows <= 0 || inner > (1ll << 32) || rows > (1ll << 32))
+        return false;
+    long long stride = ld * 2;
+    if (rows == 1 && stride < inner * 2) stride = (inner * 2 + 15) / 16 * 16;   /* unused for one row */
+    if ((stride & 15) || stride < inner * 2 || stride >= (1ll << 40)) return false;
+    cuuint64_t dims[2] = {(cuuint64_t)inner, (cuuint64_t)rows};
+    cuuint64_t strides[1] = {(cuuint64_t)stride};
+    cuuint32_t box[2] = {8, (cuuint32_t)box_rows};
+    cuuint32_t estr[2] = {1, 1};
+    return enc(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(base), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <bool A_MN, bool B_MN>
+static cudaError_t launch_gemm_tma(dim3 grid, cudaStream_t st, const CUtensorMap &ma, const CUtensorMap &mb, int M,
+                                   int N, int K, const float *bias, const float *mask, long long ldm, int act,
+                                   float *C, long long ldc, bf16 *C16, long long ldc16)
+{
+    static bool smem_set = false;        /* GST x 24 KB dynamic shared memory is above the 48 KB default */
+    if (!smem_set) {
+        cudaError_t e = cudaFuncSetAttribute(k_gemm_tma<A_MN, B_MN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             GST * GSTAGE);
+        if (e != cudaSuccess) return e;
+        smem_set = true;
+    }
+    k_gemm_tma<A_MN, B_MN><<<grid, 128, GST * GSTAGE, st>>>(ma, mb, M, N, K, bias, mask, ldm, act, C, ldc, C16,
+                                                           ldc16, g_gemm_spin, g_gemm_withhold);
+    return cudaGetLastError();
 }
 
 extern "C" int gade_gemm_bf16(int32_t M, int32_t N, int32_t K, const void *A, int64_t sa0, int64_t sa1,
@@ -220,17 +425,62 @@ extern "C" int gade_gemm_bf16(int32_t M, int32_t N, int32_t K, const void *A, in
     if (M < 0 || N < 0 || K < 0 || !A || !B || (!C && !C16) || (act != 0 && act != 1))
         return gade_set_error(GADE_ERR_ARG, "gade_gemm_bf16: bad argument");
     if (M == 0 || N == 0) return GADE_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    dim3 grid((N + GTN - 1) / GTN, (M + GTM - 1) / GTM);
+    if (g_gemm_path == 0 && K > 0) {
+        /* A contiguous along K (sa1 = 1) is staged K-major, along M (sa0 = 1)
+           M-major; B contiguous along K (sb0 = 1) K-major, along N N-major */
+        CUtensorMap ma, mb;
+        const bool a_k = sa1 == 1, b_k = sb0 == 1;
+        const bool a_ok = a_k ? encode_operand(&ma, A, K, M, sa0, GTM)
+                              : (sa0 == 1 && encode_operand(&ma, A, M, K, sa1, GTK));
+        const bool b_ok = b_k ? encode_operand(&mb, B, K, N, sb1, GTN)
+                              : (sb1 == 1 && encode_operand(&mb, B, N, K, sb0, GTK));
+        if (a_ok && b_ok) {
+            cudaError_t e;
+            if (!a_k && !b_k) e = launch_gemm_tma<true, true>(grid, st, ma, mb, M, N, K, bias, mask, ldm, act, C,
+                                                              ldc, (bf16 *)C16, ldc16);
+            else if (!a_k) e = launch_gemm_tma<true, false>(grid, st, ma, mb, M, N, K, bias, mask, ldm, act, C, ldc,
+                                                            (bf16 *)C16, ldc16);
+            else if (!b_k) e = launch_gemm_tma<false, true>(grid, st, ma, mb, M, N, K, bias, mask, ldm, act, C, ldc,
+                                                            (bf16 *)C16, ldc16);
+            else e = launch_gemm_tma<false, false>(grid, st, ma, mb, M, N, K, bias, mask, ldm, act, C, ldc,
+                                                   (bf16 *)C16, ldc16);
+            if (e != cudaSuccess) return lfail(GADE_ERR_CUDA, "gade_gemm_bf16", e);
+            return GADE_OK;
+        }
+    }
     static bool smem_set = false;        /* 2 x 24 KB dynamic shared memory is above the 48 KB default */
     if (!smem_set) {
-        cudaError_t e = cudaFuncSetAttribute(k_gemm_bf16, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * GSTAGE);
+        cudaError_t e = cudaFuncSetAttribute(k_gemm_ld, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * GSTAGE);
         if (e != cudaSuccess) return lfail(GADE_ERR_CUDA, "gade_gemm_bf16", e);
         smem_set = true;
     }
-    dim3 grid((N + GTN - 1) / GTN, (M + GTM - 1) / GTM);
-    k_gemm_bf16<<<grid, 128, 2 * GSTAGE, (cudaStream_t)stream>>>(M, N, K, (const bf16 *)A, sa0, sa1,
-                                                                 (const bf16 *)B, sb0, sb1, bias, mask, ldm, act,
-                                                                 C, ldc, (bf16 *)C16, ldc16);
+    k_gemm_ld<<<grid, 128, 2 * GSTAGE, st>>>(M, N, K, (const bf16 *)A, sa0, sa1, (const bf16 *)B, sb0, sb1, bias,
+                                             mask, ldm, act, C, ldc, (bf16 *)C16, ldc16, g_gemm_spin);
     LCK("gade_gemm_bf16");
+    return GADE_OK;
+}
+
+extern "C" int gade_gemm_bf16_path(int32_t M, int32_t N, int32_t K, const void *A, int64_t sa0, int64_t sa1,
+                                   const void *B, int64_t sb0, int64_t sb1)
+{
+    if (g_gemm_path != 0 || K <= 0 || M <= 0 || N <= 0) return 0;
+    CUtensorMap ma, mb;
+    const bool a_ok = sa1 == 1 ? encode_operand(&ma, A, K, M, sa0, GTM)
+                               : (sa0 == 1 && encode_operand(&ma, A, M, K, sa1, GTK));
+    const bool b_ok = sb0 == 1 ? encode_operand(&mb, B, K, N, sb1, GTN)
+                               : (sb1 == 1 && encode_operand(&mb, B, N, K, sb0, GTK));
+    return a_ok && b_ok ? 1 : 0;
+}
+
+extern "C" int gade_learned_set_gemm_options(int32_t path, uint32_t wait_limit, int32_t withhold_copies)
+{
+    if (path < 0 || path > 1 || withhold_copies < 0 || withhold_copies > 1)
+        return gade_set_error(GADE_ERR_ARG, "gade_learned_set_gemm_options: bad argument");
+    g_gemm_path = path;
+    g_gemm_spin = wait_limit ? wait_limit : GSPIN_DEFAULT;
+    g_gemm_withhold = withhold_copies;
     return GADE_OK;
 }
 

@@ -125,6 +125,9 @@ _LEARNED_SIGS = {
     "gade_gemm_bf16": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, _P, C.c_int64, C.c_int64, _P, C.c_int64,
                                  C.c_int64, _P, _P, C.c_int64, C.c_int32, _P, C.c_int64, _P, C.c_int64, _P]),
     "gade_learned_status": (C.c_int, [C.POINTER(C.c_int32)]),
+    "gade_gemm_bf16_path": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, _P, C.c_int64, C.c_int64, _P, C.c_int64,
+                                      C.c_int64]),
+    "gade_learned_set_gemm_options": (C.c_int, [C.c_int32, C.c_uint32, C.c_int32]),
     "gade_mse_grad": (C.c_int, [C.c_int32, C.c_int32, _P, _P, _P, _P, _P, _P]),
     "gade_colsum": (C.c_int, [C.c_int32, C.c_int32, _P, C.c_int64, _P, _P]),
     "gade_adam": (C.c_int, [C.c_int64, _P, _P, _P, _P, _P, C.c_float, C.c_float, C.c_float, C.c_float,

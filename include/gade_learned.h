@@ -23,14 +23,29 @@ extern "C" {
 #endif
 
 /* C = epi(A B + bias) on the tensor cores (tcgen05.mma, BF16 operands,
- * FP32 accumulation in tensor memory).  A(i,k) = A[i*sa0 + k*sa1] (M x K), B(k,j) = B[k*sb0 +
- * j*sb1] (K x N), so either operand may be read transposed.  bias [N] may be
- * NULL.  mask (M x N, row stride ldm) may be NULL; where mask <= 0 the
- * result is 0 (ReLU backward).  act: 0 none, 1 ReLU.  C (FP32, row stride
- * ldc) and C16 (BF16, row stride ldc16) may each be NULL, not both. */
+ * FP32 accumulation in tensor memory).  A(i,k) = A[i*sa0 + k*sa1] (M x K),
+ * B(k,j) = B[k*sb0 + j*sb1] (K x N), so either operand may be read
+ * transposed.  bias [N] may be NULL.  mask (M x N, row stride ldm) may be
+ * NULL; where mask <= 0 the result is 0 (ReLU backward).  act: 0 none,
+ * 1 ReLU.  C (FP32, row stride ldc) and C16 (BF16, row stride ldc16) may
+ * each be NULL, not both.  Operands that are 16-byte aligned, unit-stride
+ * along one dimension and with a row stride of a multiple of 8 elements are
+ * staged by tensor copies (TMA); others by plain loads.  Both stagings give
+ * the same bits. */
 int gade_gemm_bf16(int32_t M, int32_t N, int32_t K, const void *A, int64_t sa0, int64_t sa1,
                    const void *B, int64_t sb0, int64_t sb1, const float *bias, const float *mask,
                    int64_t ldm, int32_t act, float *C, int64_t ldc, void *C16, int64_t ldc16, void *stream);
+
+/* 1 when gade_gemm_bf16 with these operands stages them by tensor copies,
+ * 0 when by plain loads (host only, no GPU work). */
+int gade_gemm_bf16_path(int32_t M, int32_t N, int32_t K, const void *A, int64_t sa0, int64_t sa1,
+                        const void *B, int64_t sb0, int64_t sb1);
+
+/* Process-wide GEMM options (tests): path 0 automatic, 1 plain loads only;
+ * wait_limit = mbarrier polls before a CTA gives up (0: the default, ~2^24);
+ * withhold_copies = 1 makes the tensor-copy stager issue nothing, so that
+ * the MMA thread's wait runs out and the status word is set. */
+int gade_learned_set_gemm_options(int32_t path, uint32_t wait_limit, int32_t withhold_copies);
 
 /* Status of the learned-model kernels since the last call (synchronous,
  * clears it): bit 0 = a tensor-core wait of gade_gemm_bf16 ran out (the

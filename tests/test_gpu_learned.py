@@ -30,8 +30,35 @@ def _bf(x):
     return torch.from_numpy(np.asarray(x, np.float32)).cuda().to(torch.bfloat16)
 
 
-@pytest.mark.parametrize("M_,N_,K_", [(1, 8, 16), (37, 70, 45), (130, 256, 1036), (512, 256, 256)])
-@pytest.mark.parametrize("ta,tb", [(False, False), (True, False), (False, True)])
+def _gemm_options(path=0, wait_limit=0, withhold=0):
+    native.call("gade_learned_set_gemm_options", path, wait_limit, withhold)
+
+
+def _status():
+    flags = ctypes.c_int32(-1)
+    native.call("gade_learned_status", ctypes.byref(flags))
+    return flags.value
+
+
+def _tma_layout(rows, K, s_row, s_k):
+    """Whether an operand (rows x K, element (r, k) at r*s_row + k*s_k) can
+    be staged by 2-D tensor copies: unit stride along one dimension and a
+    16-byte row stride (free for a single row)."""
+    def ok(inner, outer, ld):
+        stride = 2 * ld
+        if outer == 1 and stride < 2 * inner:
+            return True
+        return stride % 16 == 0 and stride >= 2 * inner
+    if s_k == 1:
+        return ok(K, rows, s_row)
+    return s_row == 1 and ok(rows, K, s_k)
+
+
+# (M, N, K): ragged tiles, K blocks past the copy ring's depth, row strides
+# of a multiple of 8 elements (tensor copies) and not (plain loads)
+@pytest.mark.parametrize("M_,N_,K_", [(1, 8, 16), (37, 70, 45), (130, 256, 1036), (512, 256, 256),
+                                      (200, 136, 520)])
+@pytest.mark.parametrize("ta,tb", [(False, False), (True, False), (False, True), (True, True)])
 def test_gemm_bf16(native_lib, M_, N_, K_, ta, tb):
     rng = np.random.default_rng(M_ + N_ + K_)
     A = M.bf16(rng.standard_normal((M_, K_)))
@@ -42,12 +69,22 @@ def test_gemm_bf16(native_lib, M_, N_, K_, ta, tb):
     Bd = _bf(B.T.copy() if tb else B)
     sa = (1, M_) if ta else (K_, 1)
     sb = (1, K_) if tb else (N_, 1)
+    lib = native.load_library()
+    tma = lib.gade_gemm_bf16_path(M_, N_, K_, Ad.data_ptr(), *sa, Bd.data_ptr(), *sb)
+    assert tma == int(_tma_layout(M_, K_, *sa) and _tma_layout(N_, K_, sb[1], sb[0]))
     C = torch.empty(M_, N_, device="cuda")
     C16 = torch.empty(M_, N_, dtype=torch.bfloat16, device="cuda")
+    Cld = torch.empty(M_, N_, device="cuda")
     bd, md = torch.from_numpy(bias).cuda(), torch.from_numpy(mask).cuda()
     for act, use_mask in [(0, False), (1, False), (0, True)]:
-        native.call("gade_gemm_bf16", M_, N_, K_, Ad.data_ptr(), *sa, Bd.data_ptr(), *sb, bd.data_ptr(),
-                    md.data_ptr() if use_mask else None, N_, act, C.data_ptr(), N_, C16.data_ptr(), N_, 0)
+        args = (M_, N_, K_, Ad.data_ptr(), *sa, Bd.data_ptr(), *sb, bd.data_ptr(),
+                md.data_ptr() if use_mask else None, N_, act)
+        native.call("gade_gemm_bf16", *args, C.data_ptr(), N_, C16.data_ptr(), N_, 0)
+        try:                                    # the same product staged by plain loads
+            _gemm_options(path=1)
+            native.call("gade_gemm_bf16", *args, Cld.data_ptr(), N_, None, 0, 0)
+        finally:
+            _gemm_options()
         torch.cuda.synchronize()
         ref = A @ B + bias
         if use_mask:
@@ -57,9 +94,36 @@ def test_gemm_bf16(native_lib, M_, N_, K_, ta, tb):
         got = C.cpu().numpy().astype(np.float64)
         assert _rel(got, ref) <= 1e-5, (act, use_mask)
         assert np.array_equal(C16.float().cpu().numpy(), M.bf16(got).astype(np.float32))
-    flags = ctypes.c_int32(-1)
-    native.call("gade_learned_status", ctypes.byref(flags))
-    assert flags.value == 0                     # no tensor-core wait ran out
+        assert torch.equal(C, Cld)              # same MMAs in the same order: same bits
+    assert _status() == 0                       # no tensor-core wait ran out
+
+
+def test_gemm_wait_timeout_sets_status(native_lib):
+    """The tensor-copy stager withholds its copies (a flag nothing sets): the
+    MMA thread's bounded wait runs out, the CTAs free their tensor memory
+    and return, the status word says so, and the next GEMM is exact."""
+    rng = np.random.default_rng(5)
+    M_, N_, K_ = 256, 128, 192
+    A = M.bf16(rng.standard_normal((M_, K_)))
+    B = M.bf16(rng.standard_normal((K_, N_)))
+    Ad, Bd = _bf(A), _bf(B)
+    assert native.load_library().gade_gemm_bf16_path(M_, N_, K_, Ad.data_ptr(), K_, 1, Bd.data_ptr(), N_, 1) == 1
+    C = torch.full((M_, N_), -7.0, device="cuda")
+    assert _status() == 0
+    try:
+        _gemm_options(wait_limit=1000, withhold=1)
+        native.call("gade_gemm_bf16", M_, N_, K_, Ad.data_ptr(), K_, 1, Bd.data_ptr(), N_, 1, None, None, 0, 0,
+                    C.data_ptr(), N_, None, 0, 0)
+        torch.cuda.synchronize()
+        assert _status() == 1
+        assert bool(torch.all(C == -7.0))       # no tile written
+    finally:
+        _gemm_options()
+    native.call("gade_gemm_bf16", M_, N_, K_, Ad.data_ptr(), K_, 1, Bd.data_ptr(), N_, 1, None, None, 0, 0,
+                C.data_ptr(), N_, None, 0, 0)
+    torch.cuda.synchronize()
+    assert _status() == 0
+    assert _rel(C.cpu().numpy().astype(np.float64), A @ B) <= 1e-5
 
 
 def test_mlp_gradients_match_oracle(native_lib):
