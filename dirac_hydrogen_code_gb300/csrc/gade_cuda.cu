@@ -1443,31 +1443,59 @@ __host__ __device__ __forceinline__ int pc_stage_elems(int bwp)
     return 4 * PC_TP > PC_GCH * 32 * bwp ? 4 * PC_TP : PC_GCH * 32 * bwp;
 }
 
-/* 4 warps per block row, one per SM sub-partition (each has its own FP64
- * unit).  Triangle stages: warp w takes the stage's pair w.  Chain steps:
- * warp w applies chain columns w BWP/4 .. (w+1) BWP/4 - 1 to every row; the
+/* NW (4 or 8) warps per block row, one or two per SM sub-partition (each
+ * has its own FP64 unit).  Triangle stages: the stage's pair w % 4 goes to
+ * warp w; with 8 warps warps w and w + 4 split its 33 products per lane
+ * (products 0-16 and 17-32), each keeping the parts of the two output rows
+ * apart, and the first adds the second's parts.  Chain steps: warp w
+ * applies chain columns w BWP/NW .. (w+1) BWP/NW - 1 to every row; the
  * partial sums meet in shared memory and are combined once per row, spread
- * over all four warps (two adds per lane). */
-template <typename R, int BWP>
-__global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const typename Cx<R>::T *__restrict__ in0,
-                                                     const typename Cx<R>::T *__restrict__ in1,
-                                                     typename Cx<R>::T *io, typename Cx<R>::T *__restrict__ out,
-                                                     DevScal *sc)
+ * over all warps (two adds per lane, then a shuffle over NW/2 lanes). */
+template <typename R, int NW, int Q0, int Q1>
+__device__ __forceinline__ void pc_triangle_part(const typename Cx<R>::T *__restrict__ T,
+                                                 const typename Cx<R>::T *buf, int lane, int c0, int c1, bool has1,
+                                                 bool up, typename Cx<R>::T &p0, typename Cx<R>::T &p1)
 {
     typedef typename Cx<R>::T C;
+    const int sw = up ? 31 - lane : lane;      /* last product of the first row */
+    C acc = mk<C>(0, 0), sav = acc;
+#pragma unroll
+    for (int q = Q0; q < Q1; q++) {
+        int src;
+        if (!up) src = q <= lane ? 32 * c0 + q : (has1 ? 32 * c1 + q - lane - 1 : 0);
+        else src = q <= 31 - lane ? 32 * c0 + lane + q : (has1 ? 32 * c1 + q - 1 : 0);
+        cfma(acc, T[q * 32 + lane], buf[src]);
+        if (q == sw) { sav = acc; acc = mk<C>(0, 0); }
+    }
+    /* the products of row c0 are those up to sw */
+    if (sw >= Q1) { p0 = acc; p1 = mk<C>(0, 0); }
+    else if (sw >= Q0) { p0 = sav; p1 = acc; }
+    else { p0 = mk<C>(0, 0); p1 = acc; }
+}
+
+template <typename R, int BWP, int NW>
+__global__ void __launch_bounds__(NW * 32) k_precond_tma(PcT Q, int mode, const typename Cx<R>::T *__restrict__ in0,
+                                                         const typename Cx<R>::T *__restrict__ in1,
+                                                         typename Cx<R>::T *io, typename Cx<R>::T *__restrict__ out,
+                                                         DevScal *sc)
+{
+    typedef typename Cx<R>::T C;
+    static_assert(NW == 4 || NW == 8, "4 or 8 warps");
+    constexpr int NT = NW * 32;
     constexpr int GC = 32 * BWP;                 /* complex elements of one chain block */
-    constexpr int CPW = BWP / 4;                 /* chain columns per warp */
+    constexpr int CPW = BWP / NW;                /* chain columns per warp */
+    constexpr int PARTS = NW / 2;                /* lanes that combine one row component */
     const int SB = pc_stage_elems(BWP);
     extern __shared__ __align__(128) unsigned char smem_tma[];
     C *stg = (C *)smem_tma;                /* [2][SB] */
     C *buf = stg + 2 * SB;                 /* [Bp]    */
-    C *pt = buf + Q.Bp;                    /* [4][32] partial sums */
+    C *pt = buf + Q.Bp;                    /* [NW][32] chain partial sums / [4][2][32] triangle parts */
     __shared__ __align__(8) uint64_t bar[2];
     __shared__ int all_ok;
     pdl_enter();
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    /* combining lane: row 8 wid + lane / 4, component (lane / 2) & 1, pair lane & 1 */
-    const int crow = wid * 8 + (lane >> 2), ccomp = (lane >> 1) & 1, ch = lane & 1;
+    /* combining thread: row tid / NW, component (tid / PARTS) & 1, part tid % PARTS */
+    const int crow = tid / NW, ccomp = (tid / PARTS) & 1, cpart = tid % PARTS;
     const int r = blockIdx.y;
     if (r >= Q.nblk) return;
     const int pulse = Q.plist ? Q.plist[blockIdx.x] : 0;
@@ -1527,7 +1555,7 @@ __global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const type
     } else if (mode == PC_S) {
         nega = mk<C>(-sc->alpha.x, -sc->alpha.y);
     }
-    for (int o = tid; o < Bp; o += 128) {
+    for (int o = tid; o < Bp; o += NT) {
         C val = mk<C>(0, 0);
         if (o < B) {
             const size_t gi = off + Q.ord[o];
@@ -1571,25 +1599,37 @@ __global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const type
         const int up = k >= nps;                   /* U sweep */
         const int j = up ? k - nps : k;
         if (j < nsa) {
-            /* triangle pair 4 j + wid: chunks c0 = 2p, c1 = 2p + 1 */
-            const int p = 4 * j + wid;
-            if (p < npair) {
-                const C *T = S + wid * PC_TP;
-                const int c0 = 2 * p, c1 = 2 * p + 1;
-                const bool has1 = c1 < nch;
-                const int sw = up ? 31 - lane : lane;  /* last product of the first row */
-                C acc = mk<C>(0, 0), sav = acc;
-#pragma unroll
-                for (int q = 0; q < 33; q++) {
-                    int src;
-                    if (!up) src = q <= lane ? 32 * c0 + q : (has1 ? 32 * c1 + q - lane - 1 : 0);
-                    else src = q <= 31 - lane ? 32 * c0 + lane + q : (has1 ? 32 * c1 + q - 1 : 0);
-                    cfma(acc, T[q * 32 + lane], buf[src]);
-                    if (q == sw) { sav = acc; acc = mk<C>(0, 0); }
+            /* triangle pair 4 j + wid % 4: chunks c0 = 2p, c1 = 2p + 1 */
+            const int w4 = wid & 3, half = wid >> 2;
+            const int p = 4 * j + w4;
+            const bool act = p < npair;
+            const int c0 = 2 * p, c1 = 2 * p + 1;
+            const bool has1 = c1 < nch;
+            C p0 = mk<C>(0, 0), p1 = p0;
+            if (act) {
+                const C *T = S + w4 * PC_TP;
+                if (NW == 4) pc_triangle_part<R, NW, 0, 33>(T, buf, lane, c0, c1, has1, up, p0, p1);
+                else if (half == 0) pc_triangle_part<R, NW, 0, 17>(T, buf, lane, c0, c1, has1, up, p0, p1);
+                else pc_triangle_part<R, NW, 17, 33>(T, buf, lane, c0, c1, has1, up, p0, p1);
+            }
+            if (NW == 8) {
+                if (half == 1 && act) {
+                    pt[(w4 * 2) * 32 + lane] = p0;
+                    pt[(w4 * 2 + 1) * 32 + lane] = p1;
                 }
+                __syncthreads();                   /* every read of buf of this stage is done */
+                if (half == 0 && act) {
+                    const C q0 = pt[(w4 * 2) * 32 + lane], q1 = pt[(w4 * 2 + 1) * 32 + lane];
+                    p0 = mk<C>(p0.x + q0.x, p0.y + q0.y);
+                    p1 = mk<C>(p1.x + q1.x, p1.y + q1.y);
+                }
+            } else {
                 __syncwarp();
-                buf[32 * c0 + lane] = sav;
-                if (has1) buf[32 * c1 + 31 - lane] = acc;
+            }
+            if (half == 0 && act) {
+                /* row lane of chunk c0, row 31 - lane of chunk c1 */
+                buf[32 * c0 + lane] = p0;
+                if (has1) buf[32 * c1 + 31 - lane] = p1;
             }
             __syncthreads();
         } else {
@@ -1610,12 +1650,13 @@ __global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const type
                 pt[wid * 32 + lane] = t;
                 __syncthreads();
                 {
-                    /* the row's sum (p0 + p1) + (p2 + p3), once: warp w sums rows
-                       8w..8w+7, a lane one pair of one component, a shuffle the pairs */
+                    /* the row's sum over the NW partials, once: a thread adds two
+                       partials of one component, a shuffle over PARTS lanes the rest */
                     const R *pr = (const R *)pt;
-                    R sum = pr[((2 * ch) * 32 + crow) * 2 + ccomp] + pr[((2 * ch + 1) * 32 + crow) * 2 + ccomp];
-                    sum += __shfl_xor_sync(0xffffffffu, sum, 1);
-                    if (ch == 0) ((R *)buf)[(32 * c + crow) * 2 + ccomp] = sum;
+                    R sum = pr[((2 * cpart) * 32 + crow) * 2 + ccomp] + pr[((2 * cpart + 1) * 32 + crow) * 2 + ccomp];
+#pragma unroll
+                    for (int o = 1; o < PARTS; o <<= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+                    if (cpart == 0) ((R *)buf)[(32 * c + crow) * 2 + ccomp] = sum;
                 }
                 __syncthreads();
             }
@@ -1636,7 +1677,7 @@ __global__ void __launch_bounds__(128) k_precond_tma(PcT Q, int mode, const type
         __syncthreads();
         return;
     }
-    for (int o = tid; o < B; o += 128) out[off + Q.ord[o]] = buf[o];
+    for (int o = tid; o < B; o += NT) out[off + Q.ord[o]] = buf[o];
 }
 
 /* ------------------------------------------------------------------ */
@@ -2161,7 +2202,16 @@ struct gade_solver {
     void *d_ang_dd[4], *d_Sdd, *d_Hdd, *d_Mdd;
     cdd *xdd, *ddd, *wdd;
     int pc_withhold;            /* failure injection: preconditioner stage whose copy is withheld (-1: none) */
+    int pc_nw;                  /* warps per block row of the FP64 preconditioner solves (4 or 8) */
 };
+
+/* dynamic shared memory of k_precond_tma: two stage buffers, the block
+   row's right-hand side, NW x 32 partial sums (complex of elem bytes) */
+static size_t pc_smem_bytes(const gade_solver *s, size_t elem)
+{
+    return elem * ((size_t)2 * pc_stage_elems(s->bwp) + s->Bp + 8 * 32);
+}
+
 
 static int solver_engine_step(gade_solver *s, const double *ft, int32_t maxit, double tol, gade_step_stats *stats,
                               double *x_out = nullptr);
@@ -2527,6 +2577,7 @@ static int solver_create(const gade_problem *p, int npulse, const double *dts, c
 
     gade_solver *s = new gade_solver();
     s->pc_withhold = -1;
+    s->pc_nw = 8;
     s->device = device;
     s->prec = precision;
     s->rc = p->real_coupling;
@@ -2661,13 +2712,15 @@ static int solver_create(const gade_problem *p, int npulse, const double *dts, c
         }
     }
     {
-        size_t smem = sizeof(double2) * ((size_t)2 * pc_stage_elems(s->bwp) + s->Bp + 128);
+        size_t smem = pc_smem_bytes(s, sizeof(double2));
         if (smem > 220 * 1024) { gade_setup_release(su); gade_solver_free(s); return fail(GADE_ERR_ARG, "block dimension too large for the preconditioner"); }
-        cudaFuncSetAttribute(k_precond_tma<double, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        cudaFuncSetAttribute(k_precond_tma<double, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        size_t smem32 = sizeof(float2) * ((size_t)2 * pc_stage_elems(s->bwp) + s->Bp + 128);
-        cudaFuncSetAttribute(k_precond_tma<float, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem32);
-        cudaFuncSetAttribute(k_precond_tma<float, 32>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem32);
+        const int sm64 = (int)smem, sm32 = (int)pc_smem_bytes(s, sizeof(float2));
+        cudaFuncSetAttribute(k_precond_tma<double, 16, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm64);
+        cudaFuncSetAttribute(k_precond_tma<double, 32, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm64);
+        cudaFuncSetAttribute(k_precond_tma<double, 16, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm64);
+        cudaFuncSetAttribute(k_precond_tma<double, 32, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm64);
+        cudaFuncSetAttribute(k_precond_tma<float, 16, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm32);
+        cudaFuncSetAttribute(k_precond_tma<float, 32, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, sm32);
     }
     /* per-pulse slices: dt-dependent D, i h dt/2 h0 and LU factors; radial tables */
     {
@@ -3360,11 +3413,16 @@ static int launch_precond(gade_solver *s, int mode, const double2 *in0, const do
                           double2 *out, cudaStream_t st, int pred = PRED_NONE)
 {
     PcT Q = pc_params(s, s->d_FL, s->d_FU, pred);
-    size_t smem = sizeof(double2) * ((size_t)2 * pc_stage_elems(s->bwp) + s->Bp + 128);
-    dim3 grid(s->nslot, s->nblk);
+    const size_t smem = pc_smem_bytes(s, sizeof(double2));
+    dim3 grid(s->nslot, s->nblk), block(32 * s->pc_nw);
     prof_begin(s, st);
-    if (s->bwp == 16) launch_pdl(k_precond_tma<double, 16>, grid, dim3(128), smem, st, Q, mode, in0, in1, io, out, s->d_sc);
-    else launch_pdl(k_precond_tma<double, 32>, grid, dim3(128), smem, st, Q, mode, in0, in1, io, out, s->d_sc);
+    if (s->pc_nw == 8) {
+        if (s->bwp == 16) launch_pdl(k_precond_tma<double, 16, 8>, grid, block, smem, st, Q, mode, in0, in1, io, out, s->d_sc);
+        else launch_pdl(k_precond_tma<double, 32, 8>, grid, block, smem, st, Q, mode, in0, in1, io, out, s->d_sc);
+    } else {
+        if (s->bwp == 16) launch_pdl(k_precond_tma<double, 16, 4>, grid, block, smem, st, Q, mode, in0, in1, io, out, s->d_sc);
+        else launch_pdl(k_precond_tma<double, 32, 4>, grid, block, smem, st, Q, mode, in0, in1, io, out, s->d_sc);
+    }
     prof_end(s, st, 1);
     CKL();
     return GADE_OK;
@@ -3573,11 +3631,14 @@ static int launch_precond32(gade_solver *s, int mode, const float2 *in0, const f
                             float2 *out, DevScal *sc, int pred = PRED_NONE)
 {
     PcT Q = pc_params(s, s->d_FL32, s->d_FU32, pred);
-    size_t smem = sizeof(float2) * ((size_t)2 * pc_stage_elems(s->bwp) + s->Bp + 128);
+    /* 4 warps: the complex64 solves are not bound by the FP64 units, and 8
+       warps measured slower in the mixed step (0.099 against 0.080 ms per
+       step at N = 244,000) */
+    const size_t smem = pc_smem_bytes(s, sizeof(float2));
     dim3 grid(s->nslot, s->nblk);
     prof_begin(s, s->stream);
-    if (s->bwp == 16) k_precond_tma<float, 16><<<grid, 128, smem, s->stream>>>(Q, mode, in0, in1, io, out, sc);
-    else k_precond_tma<float, 32><<<grid, 128, smem, s->stream>>>(Q, mode, in0, in1, io, out, sc);
+    if (s->bwp == 16) k_precond_tma<float, 16, 4><<<grid, 128, smem, s->stream>>>(Q, mode, in0, in1, io, out, sc);
+    else k_precond_tma<float, 32, 4><<<grid, 128, smem, s->stream>>>(Q, mode, in0, in1, io, out, sc);
     prof_end(s, s->stream, 1);
     CKL();
     return GADE_OK;
@@ -4621,6 +4682,15 @@ extern "C" int gade_solver_set_wait_limit(gade_solver *s, uint32_t polls)
     if (!s) return fail(GADE_ERR_ARG, "gade_solver_set_wait_limit: NULL solver");
     s->pc_wait = polls;
     if (s->engine) batch_drop_graphs(s->engine);   /* the graphs hold the old kernel parameters */
+    return GADE_OK;
+}
+
+extern "C" int gade_solver_set_precond_warps(gade_solver *s, int32_t warps)
+{
+    if (!s) return fail(GADE_ERR_ARG, "gade_solver_set_precond_warps: NULL solver");
+    if (warps != 4 && warps != 8) return fail(GADE_ERR_ARG, "gade_solver_set_precond_warps: warps must be 4 or 8");
+    s->pc_nw = warps;
+    if (s->engine) batch_drop_graphs(s->engine);   /* the graphs hold the old launch shape */
     return GADE_OK;
 }
 

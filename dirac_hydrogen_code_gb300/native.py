@@ -113,6 +113,7 @@ _SIGS = {
     "gade_solver_set_wait_limit": (C.c_int, [C.c_void_p, C.c_uint32]),
     "gade_solver_restart": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64]),
     "gade_solver_inject_wait_timeout": (C.c_int, [C.c_void_p, C.c_int32]),
+    "gade_solver_set_precond_warps": (C.c_int, [C.c_void_p, C.c_int32]),
     "gade_solver_set_residual_precision": (C.c_int, [C.c_void_p, C.c_int32]),
     "gade_solver_residual_precision": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
     "gade_batch_set_residual_precision": (C.c_int, [C.c_void_p, C.c_int32]),
@@ -377,6 +378,10 @@ class Solver:
         """Polls of each preconditioner stage wait before the step gives up
         with GADE_ERR_CUDA (0: the default)."""
         _check(load_library().gade_solver_set_wait_limit(self._h, int(polls)))
+
+    def set_precond_warps(self, warps: int):
+        """Warps per block row of the block-LU solves: 8 (default) or 4."""
+        _check(load_library().gade_solver_set_precond_warps(self._h, int(warps)))
 
     def set_residual_precision(self, mode: int):
         """Mixed precision: the refinement residual on the FP64 units (0) or

@@ -268,6 +268,13 @@ int gade_solver_residual_precision(const gade_solver *s, int32_t *mode, int32_t 
  * before the next step.  The device stays usable.  Takes effect at the next
  * step (captured graphs are rebuilt). */
 int gade_solver_set_wait_limit(gade_solver *s, uint32_t polls);
+/* Warps per block row of the FP64 block-LU solves (replacing the cuSPARSE
+ * triangular solves of tools/gpu_sparse.c:235-263): 8 (the default; two
+ * per SM sub-partition, the triangle products of a chunk pair split over
+ * two warps) or 4.  The two differ only in the order of FP64 additions.
+ * The complex64 solves of the mixed-precision inner iterations always use
+ * 4.  Takes effect at the next step. */
+int gade_solver_set_precond_warps(gade_solver *s, int32_t warps);
 /* Failure injection for tests of that path (no reference counterpart): the
  * preconditioner kernel does not issue the copy of stage `stage` (0 is the
  * first; -1 turns the injection off), so the wait for it runs out after the

@@ -62,11 +62,15 @@ def test_operator_matches_oracle(workdirs, native_lib, name, op):
     assert sol.launch_count() > 0
 
 
+@pytest.mark.parametrize("warps", [8, 4])
 @pytest.mark.parametrize("name", ["tiny_dipole", "tiny_nondipole", "dipole_small"])
-def test_preconditioner_matches_oracle(workdirs, native_lib, name):
+def test_preconditioner_matches_oracle(workdirs, native_lib, name, warps):
     d, params, info, T, dt = _setup(workdirs, name)
     p = O.load_problem(d, info["lmax"])
     sol = Solver(Problem(d, info["lmax"]), dt)
+    sol.set_precond_warps(warps)
+    with pytest.raises(GadeError):
+        sol.set_precond_warps(6)
     S, Hst = O.stationary(p, dt)
     rng = np.random.default_rng(3)
     b = rng.standard_normal(p.n) + 1j * rng.standard_normal(p.n)
