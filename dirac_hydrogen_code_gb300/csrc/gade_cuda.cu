@@ -732,6 +732,9 @@ __host__ __device__ __forceinline__ ApplySmem apply_smem(int CS, int W, int RM, 
  * contracted vectors u, w, u', w' of a column are interleaved (one 32- or
  * 64-byte record) and so are the four angular factors of a term.
  */
+#ifndef GADE_TABLE_PF
+#define GADE_TABLE_PF 1    /* bulk L2 prefetch of each order group's table rows (double-float instance) */
+#endif
 #ifndef GADE_DD_MINB
 #define GADE_DD_MINB 2     /* resident CTAs per SM the double-float instance is compiled for */
 #endif
@@ -893,6 +896,30 @@ __global__ void __launch_bounds__(256, std::is_same<R, dd>::value ? GADE_DD_MINB
     for (int ag = pd.y; ag < a_end; ag += G) {
         const int ng = a_end - ag < G ? a_end - ag : G;
         __syncthreads();     /* staging done / previous group's apply done */
+#if GADE_TABLE_PF
+        if constexpr (std::is_same<R, dd>::value) {
+            /* the group's table rows into L2 while the gather below runs: per
+               (order, slot) the chunk's rows are two contiguous runs, the
+               first and second half of the sorted chunk_rows (splines s and
+               their partners s + B/2).  Double-float instance only: it lifted
+               the mixed NKappa=16 step 650 -> 673 steps/s; the complex64
+               instance measured slower at N = 53,040 (tables L2-resident,
+               70 -> 77 us) and the FP64 one unchanged */
+            typedef typename std::conditional<RC, typename R4<R>::T, C4<C>>::type Q4;
+            const int n0 = nrows >> 1;
+            for (int it = tid; it < ng * W * 2; it += nt) {
+                const int g = it / (2 * W), rem = it - g * 2 * W, w = rem >> 1, h = rem & 1;
+                const int len = h ? nrows - n0 : n0;
+                if (len <= 0) continue;
+                const int rs = P.chunk_rows[q * P.RM + (h ? n0 : 0)];
+                const int l = oinf[ag - pd.y + g].x;
+                const Q4 *src = (const Q4 *)P.M + (size_t)pulse * P.mstride +
+                                ((size_t)l * P.nk + kk) * W * B + (size_t)w * B + rs;
+                asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src),
+                             "r"((unsigned)(len * sizeof(Q4))) : "memory");
+            }
+        }
+#endif
         /* gather u, w, u', w' of ng orders at once: (order, column) items */
         for (int item = tid; item < ng * ncols; item += nt) {
             const int g = item / ncols, c = item - g * ncols;
