@@ -796,7 +796,8 @@ def learned_variant(args, torch):
         out["build_s"] = time.perf_counter() - t0
         out["model"] = {k: model.history[k] for k in ("rows", "rank", "sv_ratio", "snapshots", "train_s")}
         out["model"]["loss_first_last"] = [model.history["loss"][0], model.history["loss"][-1]]
-        xr, _, _ = L.run_held_out(prob, held, W, 1e-12, "fp64", None)
+        xr, _, ms_ref = L.run_held_out(prob, held, W, 1e-12, "fp64", None)
+        out["fp64_tol1e-12"] = {"steps_per_s": len(held) * W / (ms_ref / 1e3)}
         eb = _eigenbasis(prob)
         pref = [eb.populations(x) for x in xr]
         out["fp64_tol1e-12_populations_mean"] = {k: float(np.mean([p[k] for p in pref])) for k in pref[0]}
@@ -818,6 +819,9 @@ def learned_variant(args, torch):
         prob.close()
     base = out["fp64_tol1e-10"]["steps_per_s"]
     out["speedup_vs_fp64"] = {k: out[k]["steps_per_s"] / base for k in ("mixed_tol1e-10", "learned_mixed_tol1e-10")}
+    base12 = out["fp64_tol1e-12"]["steps_per_s"]
+    out["speedup_vs_fp64_tol1e-12"] = {k: out[k]["steps_per_s"] / base12
+                                       for k in ("mixed_tol1e-10", "learned_mixed_tol1e-10")}
     return out
 
 
