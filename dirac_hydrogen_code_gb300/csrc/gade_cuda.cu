@@ -317,6 +317,12 @@ enum { PC_PLAIN = 0, PC_P, PC_S };
 
 #define NRED 4   /* values per partial: up to 4 doubles */
 #define APPLY_G64 3   /* Bessel orders per gather phase of the FP64 operator */
+#ifndef APPLY_G32
+#define APPLY_G32 4   /* ... of the complex64 operator */
+#endif
+#ifndef APPLY_GDD
+#define APPLY_GDD 3   /* ... of the double-float residual pass */
+#endif
 
 /* ------------------------------------------------------------------ */
 /* operator parameters                                                 */
@@ -753,9 +759,10 @@ __global__ void __launch_bounds__(256, std::is_same<R, dd>::value ? GADE_DD_MINB
     typedef typename Cx<R>::T C;
     typedef typename std::conditional<RC, typename R4<R>::T, C4<C>>::type A4;   /* a0, a0 k_c, a1, a1 k_c */
     extern __shared__ __align__(32) unsigned char smem_raw[];
-    /* G orders per gather phase: 3 (FP64) or 4 (FP32); with ~150 columns a
-       chunk's G x columns gather items fill the CTA's threads twice */
-    constexpr int G = sizeof(R) == 8 ? APPLY_G64 : 4;
+    /* G orders per gather phase: 3 (FP64, double-float) or 4 (FP32); with
+       ~150 columns a chunk's G x columns gather items fill the CTA's threads
+       twice (2, 4 and 6, 8 measured no faster) */
+    constexpr int G = std::is_same<R, dd>::value ? APPLY_GDD : (sizeof(R) == 8 ? APPLY_G64 : APPLY_G32);
     const int CS = (P.CM + 2) & ~1;           /* column stride: CM + the zero column, even */
     const ApplySmem L = apply_smem(CS, P.W, P.RM, P.AM, G, sizeof(C), sizeof(A4), blockDim.x, P.lmax);
     C *xr = (C *)(smem_raw + L.xr);           /* [CS] */
@@ -2955,12 +2962,12 @@ static RedP make_red(const gade_solver *s, DevScal *sc, int kind, int pred, DevS
 }
 
 /* k_apply launch shape: one thread per output row and per gathered column */
-static void apply_dims(const gade_solver *s, size_t elem, int *nt, size_t *smem)
+static void apply_dims(const gade_solver *s, size_t elem, int *nt, size_t *smem, bool ddinst = false)
 {
     int t = 2 * s->RM > s->CM ? 2 * s->RM : s->CM;   /* two threads per row */
     t = (t + 31) / 32 * 32;
     *nt = t;
-    const int G = elem == sizeof(double2) ? APPLY_G64 : 4;
+    const int G = ddinst ? APPLY_GDD : (elem == sizeof(double2) ? APPLY_G64 : APPLY_G32);
     const unsigned ang4 = s->rc ? (unsigned)(2 * elem) : (unsigned)(4 * elem);   /* four angular factors */
     const int CS = (s->CM + 2) & ~1;                 /* columns + the zero column, even */
     *smem = apply_smem(CS, s->W, s->RM, s->AM, G, (unsigned)elem, ang4, t, s->lmax).total;
@@ -2989,7 +2996,7 @@ static int apply_occupancy(const gade_solver *s, bool sep)
 {
     int nt;
     size_t smem;
-    apply_dims(s, sizeof(typename Cx<R>::T), &nt, &smem);
+    apply_dims(s, sizeof(typename Cx<R>::T), &nt, &smem, std::is_same<R, dd>::value);
     int n = 0;
     cudaError_t e = cudaSuccess;
 #define OC(RC_, SEP_, Z_) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_apply<R, RC_, SEP_, Z_>, nt, smem)
@@ -4279,7 +4286,7 @@ static int launch_apply_mix_dd(gade_solver *s, VecP V, cudaStream_t st)
     dim3 grid(s->nslot, op_partition(s, P, false, AX_MIX));
     int nt;
     size_t smem;
-    apply_dims(s, sizeof(cdd), &nt, &smem);
+    apply_dims(s, sizeof(cdd), &nt, &smem, true);
     V.in0dd = s->xdd; V.in1dd = s->ddd;
     prof_begin(s, st);
     if (s->zskip) k_apply<dd, true, true, true><<<grid, nt, smem, st>>>(P, s->wdd, AX_MIX, V, red);
