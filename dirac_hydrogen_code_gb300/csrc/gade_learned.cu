@@ -867,3 +867,33 @@ extern "C" int gade_eigproj(int32_t npulse, int32_t nblk, int32_t B, const int32
     LCK("gade_eigproj");
     return GADE_OK;
 }
+
+/* ------------------------------------------------------------------ */
+/* the learned guess of a batch, one step per call                      */
+/* ------------------------------------------------------------------ */
+extern "C" int gade_learned_guess_step(const gade_learned_guess_plan *P, int32_t head, const double *ft, void *stream)
+{
+    if (!P || head < 0 || head >= P->K || P->npulse < 1 || P->R < 1 || P->din != P->K * 2 * P->R + 12 ||
+        P->dout != 2 * P->R)
+        return gade_set_error(GADE_ERR_ARG, "gade_learned_guess_step: bad plan");
+    const int np = P->npulse, R = P->R;
+    void *slot = (char *)P->hist + (size_t)head * np * R * 16;      /* complex128 [npulse][R] */
+    int rc = gade_pod_project(P->n, R, P->U, P->x, P->ldx, np, slot, P->scratch, P->scratch_bytes, stream);
+    if (rc || !ft) return rc;
+    if ((rc = gade_learned_features(np, R, P->K, head, P->hist, ft, P->mu_in, P->sd_in, P->x16, nullptr, stream)))
+        return rc;
+    /* the network: din -> dh (ReLU) -> dh (ReLU) -> dout, BF16 operands, FP32 accumulation */
+    if ((rc = gade_gemm_bf16(np, P->dh, P->din, P->x16, P->din, 1, P->W16[0], P->dh, 1, P->bias[0], nullptr, 0, 1,
+                             P->H1, P->dh, P->H1_16, P->dh, stream)))
+        return rc;
+    if ((rc = gade_gemm_bf16(np, P->dh, P->dh, P->H1_16, P->dh, 1, P->W16[1], P->dh, 1, P->bias[1], nullptr, 0, 1,
+                             P->H2, P->dh, P->H2_16, P->dh, stream)))
+        return rc;
+    if ((rc = gade_gemm_bf16(np, P->dout, P->dh, P->H2_16, P->dh, 1, P->W16[2], P->dout, 1, P->bias[2], nullptr, 0,
+                             0, P->out, P->dout, nullptr, 0, stream)))
+        return rc;
+    if ((rc = gade_learned_outputs(np, R, P->K, head, P->out, P->mu_out, P->sd_out, P->hist, P->limit, P->c,
+                                   P->scale, stream)))
+        return rc;
+    return gade_pod_expand(P->n, R, P->U, P->c, P->scale, np, P->corr, P->ldcorr, stream);
+}

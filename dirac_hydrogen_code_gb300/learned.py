@@ -314,20 +314,23 @@ def build_model(problem: Problem, train_pulses, nsteps: int, rank: int = 128, ns
 class LearnedGuess:
     """Drives a mixed-precision batch with the model's guess: after every
     step it projects the new states, runs the network for the next step and
-    writes U c into the batch's guess buffer (the package's kernels on the
-    batch's stream; torch only allocates, on its own stream)."""
+    writes U c into the batch's guess buffer, all in one C-ABI call
+    (gade_learned_guess_step) on the batch's stream; torch only allocates.
+    The pulse factors of the next step come from device memory, so nothing
+    is copied or synchronised between steps."""
 
     def __init__(self, model: LearnedModel, batch: Batch, limit: float = 1.0):
         self.m, self.b = model, batch
         self.np = batch.npulse
         R, n = model.R, model.n
+        mlp = model.mlp
+        assert self.np <= mlp.max_rows
         self.hist = torch.zeros(K_HIST, self.np, R, dtype=torch.complex128, device="cuda")
         self.count = 0
         self.head = K_HIST - 1
         self.scratch_b = native.call("gade_pod_project_scratch", n, R, self.np)
         self.scratch = torch.empty(self.scratch_b, dtype=torch.uint8, device="cuda")
-        din = model.mlp.din
-        self.x16 = torch.empty(self.np, din, dtype=torch.bfloat16, device="cuda")
+        self.x16 = torch.empty(self.np, mlp.din, dtype=torch.bfloat16, device="cuda")
         self.c = torch.empty(self.np, R, dtype=torch.complex64, device="cuda")
         self.scale = torch.empty(self.np, dtype=torch.float32, device="cuda")
         self.ft = torch.empty(self.np, 12, dtype=torch.float64, device="cuda")
@@ -335,19 +338,55 @@ class LearnedGuess:
         self.xptr, self.xld = batch.state_device()
         self.limit = limit
         self.used = 0
+        self.guess_on = None
+        P = native.LearnedGuessPlan()
+        P.n, P.R, P.npulse, P.K = n, R, self.np, K_HIST
+        P.din, P.dh, P.dout = mlp.din, mlp.dh, mlp.dout
+        P.U, P.hist, P.x, P.ldx = model.U.data_ptr(), self.hist.data_ptr(), self.xptr, self.xld
+        P.scratch, P.scratch_bytes = self.scratch.data_ptr(), self.scratch_b
+        P.mu_in, P.sd_in = model.mu_in.data_ptr(), model.sd_in.data_ptr()
+        P.mu_out, P.sd_out = model.mu_out.data_ptr(), model.sd_out.data_ptr()
+        P.x16 = self.x16.data_ptr()
+        for i in range(3):
+            P.W16[i] = mlp.W16[i].data_ptr()
+            P.bias[i] = mlp.b[i].data_ptr()
+        P.H1, P.H2, P.out = mlp.H1.data_ptr(), mlp.H2.data_ptr(), mlp.out.data_ptr()
+        P.H1_16, P.H2_16 = mlp.H1_16.data_ptr(), mlp.H2_16.data_ptr()
+        P.c, P.scale, P.corr, P.ldcorr, P.limit = self.c.data_ptr(), self.scale.data_ptr(), self.corr, self.ld, limit
+        self.plan = P
+        self._lib = native.load_library()
+
+    def _use(self, on: bool):
+        if on != self.guess_on:
+            self.b.use_guess(on)
+            self.guess_on = on
+
+    def advance(self, ft_next_dev: int | None) -> bool:
+        """Project the batch's current states into the history and, once K
+        states are there and ft_next_dev (device address of the next step's
+        [npulse, 12] pulse-factor reals) is given, prepare the guess for the
+        next step.  Returns whether the next step uses it."""
+        self.head = (self.head + 1) % K_HIST
+        self.count += 1
+        infer = self.count >= K_HIST and ft_next_dev is not None
+        native._check(self._lib.gade_learned_guess_step(native.C.byref(self.plan), self.head,
+                                                        ft_next_dev if infer else None, self.b.stream()))
+        self._use(infer)
+        if infer:
+            self.used += 1
+        return infer
 
     def observe(self):
         """Project the batch's current states into the history."""
-        m, st = self.m, self.b.stream()
-        self.head = (self.head + 1) % K_HIST
-        native.call("gade_pod_project", m.n, m.R, m.U.data_ptr(), self.xptr, self.xld, self.np,
-                    self.hist[self.head].data_ptr(), self.scratch.data_ptr(), self.scratch_b, st)
-        self.count += 1
+        self.advance(None)
 
     def prepare(self, ft_next: np.ndarray) -> bool:
-        """Guess for the next step (pulse factors ft_next, [npulse, 12] reals)."""
+        """Guess for the next step from host pulse factors ft_next ([npulse,
+        12] reals), on the newest projection already in the history (after
+        observe): the network half of advance, for callers without device
+        pulse factors."""
         if self.count < K_HIST:
-            self.b.use_guess(False)
+            self._use(False)
             return False
         m, st = self.m, self.b.stream()
         # a blocking copy on torch's stream: no torch work is ever queued on
@@ -361,7 +400,7 @@ class LearnedGuess:
                     self.scale.data_ptr(), st)
         native.call("gade_pod_expand", m.n, m.R, m.U.data_ptr(), self.c.data_ptr(), self.scale.data_ptr(),
                     self.np, self.corr, self.ld, st)
-        self.b.use_guess(True)
+        self._use(True)
         self.used += 1
         return True
 
@@ -374,19 +413,19 @@ def run_held_out(problem: Problem, pulses, nsteps: int, tol: float, precision: s
     grids = [step_times(p["maxtime"], p["ntime"]) for p in pulses]
     b = Batch(problem, [g[0] for g in grids], None, precision=precision, **batch_kw)
     lg = LearnedGuess(model, b) if model is not None else None
+    ft_all = [_pulse_factors(pulses, grids, j) for j in range(nsteps + 1)]
+    ft_dev = torch.from_numpy(np.stack(ft_all)).cuda() if lg is not None else None   # [nsteps+1][npulse][12]
     if lg is not None:
-        lg.observe()                                            # x_0
+        lg.advance(None)                                        # x_0
     st = torch.cuda.ExternalStream(b.stream())
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     stats = []
-    ft_all = [_pulse_factors(pulses, grids, j) for j in range(nsteps + 1)]
     torch.cuda.synchronize()
     e0.record(st)
     for j in range(nsteps):
         stats.append(b.step(_ft_complex(ft_all[j]), maxit=500, tol=tol))
         if lg is not None:
-            lg.observe()
-            lg.prepare(ft_all[j + 1])
+            lg.advance(ft_dev[j + 1].data_ptr())
     e1.record(st)
     e1.synchronize()
     ms = e0.elapsed_time(e1)

@@ -122,10 +122,24 @@ _SIGS = {
 
 # include/gade_learned.h (device pointers as integers)
 _P = C.c_void_p
+
+
+class LearnedGuessPlan(C.Structure):
+    """gade_learned_guess_plan (include/gade_learned.h), field for field."""
+    _fields_ = [("n", C.c_int32), ("R", C.c_int32), ("npulse", C.c_int32), ("K", C.c_int32),
+                ("din", C.c_int32), ("dh", C.c_int32), ("dout", C.c_int32),
+                ("U", _P), ("hist", _P), ("x", _P), ("ldx", C.c_int64), ("scratch", _P),
+                ("scratch_bytes", C.c_int64), ("mu_in", _P), ("sd_in", _P), ("mu_out", _P), ("sd_out", _P),
+                ("x16", _P), ("W16", _P * 3), ("bias", _P * 3), ("H1", _P), ("H2", _P), ("out", _P),
+                ("H1_16", _P), ("H2_16", _P), ("c", _P), ("scale", _P), ("corr", _P), ("ldcorr", C.c_int64),
+                ("limit", C.c_float)]
+
+
 _LEARNED_SIGS = {
     "gade_gemm_bf16": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, _P, C.c_int64, C.c_int64, _P, C.c_int64,
                                  C.c_int64, _P, _P, C.c_int64, C.c_int32, _P, C.c_int64, _P, C.c_int64, _P]),
     "gade_learned_status": (C.c_int, [C.POINTER(C.c_int32)]),
+    "gade_learned_guess_step": (C.c_int, [C.POINTER(LearnedGuessPlan), C.c_int32, _P, _P]),
     "gade_gemm_bf16_path": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, _P, C.c_int64, C.c_int64, _P, C.c_int64,
                                       C.c_int64]),
     "gade_learned_set_gemm_options": (C.c_int, [C.c_int32, C.c_uint32, C.c_int32]),

@@ -97,6 +97,37 @@ int gade_learned_features(int32_t npulse, int32_t R, int32_t K, int32_t head, co
 int gade_learned_outputs(int32_t npulse, int32_t R, int32_t K, int32_t head, const float *out, const float *mu,
                          const float *sd, const void *hist, float limit, void *c, float *scale, void *stream);
 
+/* The learned guess of a batch, one step in one call: every pointer a
+ * device address fixed for the batch's lifetime (set once by the caller). */
+typedef struct {
+    int32_t n, R, npulse, K;        /* state length, POD rank, pulses, history length */
+    int32_t din, dh, dout;          /* network widths: K*2R + 12 -> dh -> dh -> 2R */
+    const void *U;                  /* complex64 POD basis [R][n] */
+    void *hist;                     /* complex128 projection ring [K][npulse][R] */
+    const void *x;                  /* complex128 states, pulse stride ldx */
+    int64_t ldx;
+    void *scratch;                  /* >= gade_pod_project_scratch(n, R, npulse) bytes */
+    int64_t scratch_bytes;
+    const float *mu_in, *sd_in, *mu_out, *sd_out;   /* input / output normalisation */
+    void *x16;                      /* BF16 network inputs [npulse][din] */
+    const void *W16[3];             /* BF16 weights [din][dh], [dh][dh], [dh][dout] */
+    const float *bias[3];
+    float *H1, *H2, *out;           /* FP32 activations [npulse][dh], [npulse][dh], outputs [npulse][dout] */
+    void *H1_16, *H2_16;            /* their BF16 copies */
+    void *c;                        /* complex64 coefficients [npulse][R] */
+    float *scale;                   /* [npulse] */
+    void *corr;                     /* complex128 guess correction, pulse stride ldcorr */
+    int64_t ldcorr;
+    float limit;                    /* gade_learned_outputs' plausibility limit */
+} gade_learned_guess_plan;
+
+/* Project the current states into hist[head] (gade_pod_project); when ft
+ * (device, [npulse][12] reals: the next step's pulse factors) is not NULL,
+ * also run the network on the K newest projections (gade_learned_features,
+ * three gade_gemm_bf16, gade_learned_outputs) and write U c into corr
+ * (gade_pod_expand).  Every kernel on stream, nothing synchronises. */
+int gade_learned_guess_step(const gade_learned_guess_plan *plan, int32_t head, const double *ft, void *stream);
+
 /* Eigenstate projection of states (the populations of src/process_output.cpp
  * with src/hamiltonian.h:1246-1330): for every pulse p < npulse and block
  * row r, coef[p][r][j] = sum_i conj(x_p[r*B + i]) W[k_r][i][j] with

@@ -29,6 +29,25 @@ def test_library_exports_every_declared_symbol(native_lib):
     assert set(_LEARNED_SIGS) == set(learned), set(learned) ^ set(_LEARNED_SIGS)
 
 
+def test_learned_plan_layout_matches_header(tmp_path):
+    """native.LearnedGuessPlan has gade_learned_guess_plan's size and field
+    offsets (a C program compiled against include/gade_learned.h)."""
+    import ctypes
+    import subprocess
+    from dirac_hydrogen_code_gb300.native import LearnedGuessPlan
+    names = [f[0] for f in LearnedGuessPlan._fields_]
+    prog = ['#include <stdio.h>', '#include <stddef.h>', '#include "gade_learned.h"', 'int main(void) {',
+            '  printf("%zu\\n", sizeof(gade_learned_guess_plan));']
+    prog += [f'  printf("%zu\\n", offsetof(gade_learned_guess_plan, {n}));' for n in names]
+    prog += ['  return 0;', '}']
+    (tmp_path / "plan.c").write_text("\n".join(prog) + "\n")
+    exe = str(tmp_path / "plan")
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(tmp_path / "plan.c"), "-o", exe], check=True)
+    got = [int(v) for v in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
+    want = [ctypes.sizeof(LearnedGuessPlan)] + [getattr(LearnedGuessPlan, n).offset for n in names]
+    assert got == want
+
+
 def test_problem_load_on_host(workdirs, native_lib):
     from dirac_hydrogen_code_gb300 import formats
     from dirac_hydrogen_code_gb300.native import Problem

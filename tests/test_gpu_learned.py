@@ -193,3 +193,56 @@ def test_pod_project_and_expand(native_lib):
     yref = (scale[:, None] * c.astype(np.complex128)) @ U.astype(np.complex128)
     assert _rel(y.cpu().numpy(), yref) <= 1e-6
     assert np.all(y[1].cpu().numpy() == 0)
+
+
+def test_fused_guess_step_matches_separate_calls(workdirs, native_lib):
+    """LearnedGuess.advance (one gade_learned_guess_step per step, pulse
+    factors from device memory) and the separate projection / features /
+    network / outputs / expansion calls (observe + prepare, pulse factors
+    from the host) give bit-identical guesses over a few mixed steps of two
+    batches on the same pulses."""
+    from dirac_hydrogen_code_gb300 import learned as L
+    from dirac_hydrogen_code_gb300.cn import step_times
+    from dirac_hydrogen_code_gb300.native import Batch, Problem
+    d, params, info = workdirs["tiny_nondipole"]
+    prob = Problem(d, info["lmax"])
+    pulses = L.intensity_pulses(2, 5, params["Omega"], params["Cycles"], params["Ntime"])
+    grids = [step_times(p["maxtime"], p["ntime"]) for p in pulses]
+    rng = np.random.default_rng(9)
+    R = 6
+    Q, _ = np.linalg.qr(rng.standard_normal((prob.n, R)) + 1j * rng.standard_normal((prob.n, R)))
+    din = L.K_HIST * 2 * R + 12
+    mlp = MLP(din, 32, 2 * R, 8, seed=3)
+    ones, zeros = torch.ones, torch.zeros
+    model = L.LearnedModel(Q.T.conj(), mlp, zeros(din), ones(din), zeros(2 * R), 1e-3 * ones(2 * R), {})
+    nsteps = 8
+    ft_all = [L._pulse_factors(pulses, grids, j) for j in range(nsteps + 1)]
+    ft_dev = torch.from_numpy(np.stack(ft_all)).cuda()
+    runs = []
+    for fused in (True, False):
+        # fixed operator and chunking: the timed choices may differ between batches
+        b = Batch(prob, [g[0] for g in grids], None, precision="mixed", chunk_splines=16)
+        b.set_operator(0)
+        lg = L.LearnedGuess(model, b, limit=1e30)
+        corr_ptr, ld = b.guess_buffer()
+        corr = L.device_view(corr_ptr, (2, ld))
+        lg.advance(None)
+        seen = []
+        for j in range(nsteps):
+            b.step(L._ft_complex(ft_all[j]), maxit=500, tol=1e-10)
+            if fused:
+                used = lg.advance(ft_dev[j + 1].data_ptr())
+            else:
+                lg.observe()
+                used = lg.prepare(ft_all[j + 1])
+            torch.cuda.synchronize()
+            seen.append((used, corr[:, :prob.n].clone().cpu().numpy()))
+        runs.append((seen, np.stack([b.get_x(k) for k in range(2)])))
+        b.close()
+    (sa, xa), (sb, xb) = runs
+    assert [u for u, _ in sa] == [u for u, _ in sb]
+    assert sum(u for u, _ in sa) == sum(j + 2 >= L.K_HIST for j in range(nsteps))
+    for (_, ca), (_, cb) in zip(sa, sb):
+        assert np.array_equal(ca, cb)
+    assert np.any(sa[-1][1] != 0)
+    assert np.array_equal(xa, xb)
