@@ -606,26 +606,49 @@ extern "C" int gade_to_bf16(int64_t n, const float *x, void *y, void *stream)
  * chunk); every block stages its x slice in shared memory and 8 warps take
  * the basis rows; partials [chunk][p][r].  Stage 2 sums chunks in order. */
 #define PJ_L 1024
+/* FP64 -> FP32 by bit operations, without the conversion instruction (which
+   runs at the FP64 rate on this GPU): sign, rebiased exponent and the top 23
+   mantissa bits (truncation, relative error < 2^-23); magnitudes below the
+   FP32 normal range give 0, above it infinity, NaN stays NaN. */
+__device__ __forceinline__ float l_f32_bits(double v)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    const unsigned sign = (unsigned)(b >> 63) << 31;
+    const int e11 = (int)((b >> 52) & 0x7FF);
+    const unsigned mant = (unsigned)((b >> 29) & 0x7FFFFF);
+    if (e11 == 0x7FF) return __uint_as_float(sign | 0x7F800000u | (b & 0xFFFFFFFFFFFFFull ? 0x400000u : 0u));
+    const int e8 = e11 - 1023 + 127;
+    if (e8 <= 0) return __uint_as_float(sign);
+    if (e8 >= 255) return __uint_as_float(sign | 0x7F800000u);
+    return __uint_as_float(sign | ((unsigned)e8 << 23) | mant);
+}
+
+/* partial projections of one 1024-element chunk of one pulse's state: the
+   network's BF16 inputs need no more than FP32 products and per-chunk FP32
+   sums (relative error ~1e-7); chunks are added in FP64 in a fixed order */
 __global__ void __launch_bounds__(256) k_pod_partial(int n, int R, const float2 *__restrict__ U,
                                                      const double2 *__restrict__ x, long long ldx,
                                                      double2 *__restrict__ part, int npulse)
 {
-    __shared__ double2 xs[PJ_L];
+    __shared__ float2 xs[PJ_L];
     const int p = blockIdx.x, ch = blockIdx.y;
     const int i0 = ch * PJ_L;
     const int len = n - i0 < PJ_L ? n - i0 : PJ_L;
     const double2 *xp = x + (size_t)p * ldx + i0;
-    for (int e = threadIdx.x; e < len; e += 256) xs[e] = xp[e];
+    for (int e = threadIdx.x; e < len; e += 256) {
+        const double2 v = xp[e];
+        xs[e] = make_float2(l_f32_bits(v.x), l_f32_bits(v.y));
+    }
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     for (int r = warp; r < R; r += 8) {
         const float2 *u = U + (size_t)r * n + i0;
-        double sr = 0, si = 0;
+        float sr = 0.f, si = 0.f;
         for (int e = lane; e < len; e += 32) {
             const float2 uv = u[e];
-            const double2 xv = xs[e];
-            sr += (double)uv.x * xv.x + (double)uv.y * xv.y;
-            si += (double)uv.x * xv.y - (double)uv.y * xv.x;
+            const float2 xv = xs[e];
+            sr = fmaf(uv.x, xv.x, fmaf(uv.y, xv.y, sr));      /* conj(u) x */
+            si = fmaf(uv.x, xv.y, fmaf(-uv.y, xv.x, si));
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {

@@ -70,9 +70,11 @@ int gade_adam(int64_t n, float *w, void *w16, const float *g, float *m, float *v
 int gade_to_bf16(int64_t n, const float *x, void *y, void *stream);
 
 /* coef[p][r] = sum_i conj(U[r][i]) x_p[i] for p < npulse: U complex64
- * [R][n], x complex128 with pulse stride ldx, coef complex128 [npulse][R],
- * FP64 accumulation in a fixed order.  scratch: device bytes, at least
- * gade_pod_project_scratch(n, R, npulse). */
+ * [R][n], x complex128 with pulse stride ldx, coef complex128 [npulse][R].
+ * FP32 products of U and x's FP32 part, summed in FP32 over chunks of 1024
+ * elements and the chunks in FP64, in a fixed order (relative error
+ * ~1e-7: the network's BF16 inputs need no more).  scratch: device bytes,
+ * at least gade_pod_project_scratch(n, R, npulse). */
 int gade_pod_project(int64_t n, int32_t R, const void *U, const void *x, int64_t ldx, int32_t npulse,
                      void *coef, void *scratch, int64_t scratch_bytes, void *stream);
 int64_t gade_pod_project_scratch(int64_t n, int32_t R, int32_t npulse);
