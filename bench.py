@@ -774,9 +774,9 @@ def learned_variant(args, torch):
     on 8 held-out pulses; pulses differ in Intensity only (log-uniform in
     [1, 100], seeded), so they share g, dt and the LU factors.  Bounded
     sample: the first `learned_steps` steps of every pulse.  Compared at the
-    same FP64 residual 1e-10: plain FP64, mixed precision with the
-    extrapolated guess, mixed precision with the learned guess; errors
-    against an FP64 run at tol 1e-12."""
+    same residual 1e-10: plain FP64, mixed precision with the extrapolated
+    guess, mixed precision with the learned guess; and the two mixed runs at
+    1e-12; errors against an FP64 run at tol 1e-12."""
     import numpy as np
     from dirac_hydrogen_code_gb300 import learned as L
     from dirac_hydrogen_code_gb300.gen import CONFIGS, generate
@@ -801,9 +801,11 @@ def learned_variant(args, torch):
         eb = _eigenbasis(prob)
         pref = [eb.populations(x) for x in xr]
         out["fp64_tol1e-12_populations_mean"] = {k: float(np.mean([p[k] for p in pref])) for k in pref[0]}
-        for tag, prec, mdl in (("fp64_tol1e-10", "fp64", None), ("mixed_tol1e-10", "mixed", None),
-                               ("learned_mixed_tol1e-10", "mixed", model)):
-            xs, st, ms = L.run_held_out(prob, held, W, 1e-10, prec, mdl)
+        for tag, prec, mdl, tol in (("fp64_tol1e-10", "fp64", None, 1e-10), ("mixed_tol1e-10", "mixed", None, 1e-10),
+                                    ("learned_mixed_tol1e-10", "mixed", model, 1e-10),
+                                    ("mixed_tol1e-12", "mixed", None, 1e-12),
+                                    ("learned_mixed_tol1e-12", "mixed", model, 1e-12)):
+            xs, st, ms = L.run_held_out(prob, held, W, tol, prec, mdl)
             err = np.linalg.norm(xs - xr, axis=1) / np.linalg.norm(xr, axis=1)
             rec = {"steps_per_s": len(held) * W / (ms / 1e3),
                    "iters_per_step": float(np.mean([[r["iters"] for r in row] for row in st])),
@@ -815,13 +817,17 @@ def learned_variant(args, torch):
                 ini = np.array([[r["init_residual"] for r in row] for row in st])[L.K_HIST:]
                 rec["init_residual_mean"] = float(ini.mean())
                 rec["fp64_residual_passes_per_step"] = float(np.mean([[r["refinements"] for r in row] for row in st]))
+                rec["inner_iters_per_step"] = float(np.mean([[r["inner_iters"] for r in row] for row in st]))
             out[tag] = rec
         prob.close()
     base = out["fp64_tol1e-10"]["steps_per_s"]
     out["speedup_vs_fp64"] = {k: out[k]["steps_per_s"] / base for k in ("mixed_tol1e-10", "learned_mixed_tol1e-10")}
     base12 = out["fp64_tol1e-12"]["steps_per_s"]
     out["speedup_vs_fp64_tol1e-12"] = {k: out[k]["steps_per_s"] / base12
-                                       for k in ("mixed_tol1e-10", "learned_mixed_tol1e-10")}
+                                       for k in ("mixed_tol1e-10", "learned_mixed_tol1e-10", "mixed_tol1e-12",
+                                                 "learned_mixed_tol1e-12")}
+    out["learned_over_extrapolated"] = {t: out[f"learned_mixed_{t}"]["steps_per_s"] / out[f"mixed_{t}"]["steps_per_s"]
+                                        for t in ("tol1e-10", "tol1e-12")}
     return out
 
 
