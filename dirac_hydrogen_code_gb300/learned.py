@@ -406,13 +406,13 @@ class LearnedGuess:
 
 
 def run_held_out(problem: Problem, pulses, nsteps: int, tol: float, precision: str, model: LearnedModel | None,
-                 **batch_kw):
+                 limit: float = 1.0, **batch_kw):
     """Held-out pulses for nsteps steps: plain (model None) or with the
     learned guess.  Returns (final states [npulse, n] complex128 numpy,
     per-step stats, device ms of the whole run)."""
     grids = [step_times(p["maxtime"], p["ntime"]) for p in pulses]
     b = Batch(problem, [g[0] for g in grids], None, precision=precision, **batch_kw)
-    lg = LearnedGuess(model, b) if model is not None else None
+    lg = LearnedGuess(model, b, limit=limit) if model is not None else None
     ft_all = [_pulse_factors(pulses, grids, j) for j in range(nsteps + 1)]
     ft_dev = torch.from_numpy(np.stack(ft_all)).cuda() if lg is not None else None   # [nsteps+1][npulse][12]
     if lg is not None:
@@ -445,7 +445,7 @@ def intensity_pulses(n: int, seed: int, omega: float, cycles: int, ntime: int) -
 
 def experiment(params: dict, nsteps: int, ntrain: int = 32, nheld: int = 8, rank: int = 128, nsnap: int = 200,
                pod_pulses: int = 8, epochs: int = 30, seed: int = 1, tol: float = 1e-10, workdir: str | None = None,
-               log=None) -> dict:
+               log=None, limit: float = 1.0) -> dict:
     """The learned-guess protocol: POD + network from `ntrain` seeded training
     pulses (plain FP64 trajectories), then `nheld` seeded held-out pulses run
     four ways for `nsteps` steps: FP64 at tol 1e-12 (reference), plain FP64 at
@@ -467,6 +467,7 @@ def experiment(params: dict, nsteps: int, ntrain: int = 32, nheld: int = 8, rank
     mk = lambda n, s: intensity_pulses(n, s, params["Omega"], params["Cycles"], params["Ntime"])  # noqa: E731
     train, held = mk(ntrain, 100 + seed), mk(nheld, 200 + seed)
     out = {"params": params, "steps_per_pulse": nsteps, "train_pulses": ntrain, "held_out_pulses": nheld,
+           "limit": limit,
            "seeds": {"train": 100 + seed, "held_out": 200 + seed, "pod_and_network": seed}, "tol": tol}
     t0 = time.perf_counter()
     model = build_model(prob, train, nsteps, rank=rank, nsnap=nsnap, pod_pulses=pod_pulses, seed=seed,
@@ -485,7 +486,7 @@ def experiment(params: dict, nsteps: int, ntrain: int = 32, nheld: int = 8, rank
         if prec == "fp64" and tol == 1e-12:
             xs, st, ms = xr, None, ms_ref                       # the reference run itself
         else:
-            xs, st, ms = run_held_out(prob, held, nsteps, tol, prec, mdl)
+            xs, st, ms = run_held_out(prob, held, nsteps, tol, prec, mdl, limit=limit)
         err = np.linalg.norm(xs - xr, axis=1) / np.linalg.norm(xr, axis=1)
         pops = [eb.populations(x) for x in xs]
         rec = {"steps_per_s": nheld * nsteps / (ms / 1e3),
@@ -564,13 +565,15 @@ def main(argv=None) -> int:
     ap.add_argument("--rank", type=int, default=128)
     ap.add_argument("--epochs", type=int, default=30)
     ap.add_argument("--tol", type=float, default=1e-10, help="residual tolerance of the compared runs")
+    ap.add_argument("--limit", type=float, default=1.0,
+                    help="a prediction is used while |c| <= limit * |projection of the last state change|")
     ap.add_argument("--out", default=None, help="write the result JSON here")
     args = ap.parse_args(argv)
     params = CONFIGS[args.workload]
     T = params["Cycles"] * 2 * math.pi / params["Omega"]
     nsteps = args.steps or len(step_times(T, params["Ntime"])[1])
     res = experiment(params, nsteps, args.train, args.held, rank=args.rank, epochs=args.epochs, tol=args.tol,
-                     log=lambda *a: print(*a, file=sys.stderr, flush=True))
+                     log=lambda *a: print(*a, file=sys.stderr, flush=True), limit=args.limit)
     res["workload"] = args.workload
     txt = json.dumps(res)
     if args.out:
