@@ -659,6 +659,38 @@ __global__ void __launch_bounds__(256) k_pod_partial(int n, int R, const float2 
     }
 }
 
+/* the same partial projections with FP64 products and sums (training
+   targets are second differences of projections, which cancel) */
+__global__ void __launch_bounds__(256) k_pod_partial64(int n, int R, const float2 *__restrict__ U,
+                                                       const double2 *__restrict__ x, long long ldx,
+                                                       double2 *__restrict__ part, int npulse)
+{
+    __shared__ double2 xs[PJ_L];
+    const int p = blockIdx.x, ch = blockIdx.y;
+    const int i0 = ch * PJ_L;
+    const int len = n - i0 < PJ_L ? n - i0 : PJ_L;
+    const double2 *xp = x + (size_t)p * ldx + i0;
+    for (int e = threadIdx.x; e < len; e += 256) xs[e] = xp[e];
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int r = warp; r < R; r += 8) {
+        const float2 *u = U + (size_t)r * n + i0;
+        double sr = 0, si = 0;
+        for (int e = lane; e < len; e += 32) {
+            const float2 uv = u[e];
+            const double2 xv = xs[e];
+            sr += (double)uv.x * xv.x + (double)uv.y * xv.y;
+            si += (double)uv.x * xv.y - (double)uv.y * xv.x;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            sr += __shfl_xor_sync(0xffffffffu, sr, o);
+            si += __shfl_xor_sync(0xffffffffu, si, o);
+        }
+        if (lane == 0) part[((size_t)ch * npulse + p) * R + r] = make_double2(sr, si);
+    }
+}
+
 __global__ void k_pod_sum(int nch, int npulse, int R, const double2 *__restrict__ part, double2 *__restrict__ coef)
 {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -671,8 +703,8 @@ __global__ void k_pod_sum(int nch, int npulse, int R, const double2 *__restrict_
     coef[t] = make_double2(sr, si);
 }
 
-extern "C" int gade_pod_project(int64_t n, int32_t R, const void *U, const void *x, int64_t ldx, int32_t npulse,
-                                void *coef, void *scratch, int64_t scratch_bytes, void *stream)
+static int pod_project(bool fp64, int64_t n, int32_t R, const void *U, const void *x, int64_t ldx, int32_t npulse,
+                       void *coef, void *scratch, int64_t scratch_bytes, void *stream)
 {
     if (n <= 0 || n > (1ll << 31) - 1 || R <= 0 || npulse <= 0 || !U || !x || !coef || !scratch)
         return gade_set_error(GADE_ERR_ARG, "gade_pod_project: bad argument");
@@ -680,12 +712,28 @@ extern "C" int gade_pod_project(int64_t n, int32_t R, const void *U, const void 
     const int64_t need = (int64_t)nch * npulse * R * (int64_t)sizeof(double2);
     if (scratch_bytes < need) return gade_set_error(GADE_ERR_ARG, "gade_pod_project: scratch too small");
     cudaStream_t st = (cudaStream_t)stream;
-    k_pod_partial<<<dim3(npulse, nch), 256, 0, st>>>((int)n, R, (const float2 *)U, (const double2 *)x, ldx,
-                                                     (double2 *)scratch, npulse);
+    if (fp64)
+        k_pod_partial64<<<dim3(npulse, nch), 256, 0, st>>>((int)n, R, (const float2 *)U, (const double2 *)x, ldx,
+                                                           (double2 *)scratch, npulse);
+    else
+        k_pod_partial<<<dim3(npulse, nch), 256, 0, st>>>((int)n, R, (const float2 *)U, (const double2 *)x, ldx,
+                                                         (double2 *)scratch, npulse);
     LCK("gade_pod_project");
     k_pod_sum<<<(npulse * R + 255) / 256, 256, 0, st>>>(nch, npulse, R, (const double2 *)scratch, (double2 *)coef);
     LCK("gade_pod_project");
     return GADE_OK;
+}
+
+extern "C" int gade_pod_project(int64_t n, int32_t R, const void *U, const void *x, int64_t ldx, int32_t npulse,
+                                void *coef, void *scratch, int64_t scratch_bytes, void *stream)
+{
+    return pod_project(false, n, R, U, x, ldx, npulse, coef, scratch, scratch_bytes, stream);
+}
+
+extern "C" int gade_pod_project_fp64(int64_t n, int32_t R, const void *U, const void *x, int64_t ldx,
+                                     int32_t npulse, void *coef, void *scratch, int64_t scratch_bytes, void *stream)
+{
+    return pod_project(true, n, R, U, x, ldx, npulse, coef, scratch, scratch_bytes, stream);
 }
 
 extern "C" int64_t gade_pod_project_scratch(int64_t n, int32_t R, int32_t npulse)

@@ -250,13 +250,13 @@ def build_model(problem: Problem, train_pulses, nsteps: int, rank: int = 128, ns
     scratch = torch.empty(scratch_b, dtype=torch.uint8, device="cuda")
     x0 = torch.from_numpy(np.tile(psi, (npul, 1))).cuda()
     stream0 = torch.cuda.current_stream().cuda_stream
-    native.call("gade_pod_project", n, R, Ud.data_ptr(), x0.data_ptr(), n, npul, coef[0].data_ptr(),
+    native.call("gade_pod_project_fp64", n, R, Ud.data_ptr(), x0.data_ptr(), n, npul, coef[0].data_ptr(),
                 scratch.data_ptr(), scratch_b, stream0)
     torch.cuda.synchronize()
 
     def project(j, b, xv):
         st = b.stream()
-        native.call("gade_pod_project", n, R, Ud.data_ptr(), xv.data_ptr(), xv.shape[1], npul,
+        native.call("gade_pod_project_fp64", n, R, Ud.data_ptr(), xv.data_ptr(), xv.shape[1], npul,
                     coef[j + 1].data_ptr(), scratch.data_ptr(), scratch_b, st)
 
     b, grids, _ = run_trajectories(problem, train_pulses, nsteps, tol, on_step=project)

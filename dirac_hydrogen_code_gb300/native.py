@@ -150,6 +150,7 @@ _LEARNED_SIGS = {
     "gade_to_bf16": (C.c_int, [C.c_int64, _P, _P, _P]),
     "gade_pod_project": (C.c_int, [C.c_int64, C.c_int32, _P, _P, C.c_int64, C.c_int32, _P, _P, C.c_int64, _P]),
     "gade_pod_project_scratch": (C.c_int64, [C.c_int64, C.c_int32, C.c_int32]),
+    "gade_pod_project_fp64": (C.c_int, [C.c_int64, C.c_int32, _P, _P, C.c_int64, C.c_int32, _P, _P, C.c_int64, _P]),
     "gade_pod_expand": (C.c_int, [C.c_int64, C.c_int32, _P, _P, _P, C.c_int32, _P, C.c_int64, _P]),
     "gade_learned_features": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, _P, _P, _P, _P, _P, _P, _P]),
     "gade_learned_outputs": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, C.c_int32, _P, _P, _P, _P, C.c_float,

@@ -78,6 +78,10 @@ int gade_to_bf16(int64_t n, const float *x, void *y, void *stream);
 int gade_pod_project(int64_t n, int32_t R, const void *U, const void *x, int64_t ldx, int32_t npulse,
                      void *coef, void *scratch, int64_t scratch_bytes, void *stream);
 int64_t gade_pod_project_scratch(int64_t n, int32_t R, int32_t npulse);
+/* The same with FP64 products and sums in a fixed order (relative error
+ * ~1e-15): for training targets, second differences of projections. */
+int gade_pod_project_fp64(int64_t n, int32_t R, const void *U, const void *x, int64_t ldx, int32_t npulse,
+                          void *coef, void *scratch, int64_t scratch_bytes, void *stream);
 
 /* y_p = scale[p] * U c_p (complex64 U [R][n] and c [npulse][R], complex128
  * y with pulse stride ldy); scale may be NULL (1). */

@@ -8,7 +8,7 @@
     against the oracle with the same BF16 rounding points
   * Adam: <= 1e-5 relative against the float64 update
   * POD projection / expansion: <= 1e-6 relative (complex64 basis, FP32
-    products)
+    products), the FP64 projection <= 1e-12
 """
 import ctypes
 
@@ -185,6 +185,11 @@ def test_pod_project_and_expand(native_lib):
     torch.cuda.synchronize()
     ref = X @ U.astype(np.complex128).conj().T
     assert _rel(coef.cpu().numpy(), ref) <= 1e-6                # FP32 products and chunk sums
+    coef64 = torch.empty_like(coef)
+    native.call("gade_pod_project_fp64", n, R, Ud.data_ptr(), Xd.data_ptr(), n, P, coef64.data_ptr(),
+                scratch.data_ptr(), sb, 0)
+    torch.cuda.synchronize()
+    assert _rel(coef64.cpu().numpy(), ref) <= 1e-12             # FP64 (training targets)
     # a state change of 1e-4 projected as the difference of two projections
     # (the plausibility bound of gade_learned_outputs) keeps ~1e-3
     X2 = X + 1e-4 * (rng.standard_normal((P, n)) + 1j * rng.standard_normal((P, n)))
