@@ -405,12 +405,14 @@ static cudaError_t launch_gemm_tma(dim3 grid, cudaStream_t st, const CUtensorMap
                                    int N, int K, const float *bias, const float *mask, long long ldm, int act,
                                    float *C, long long ldc, bf16 *C16, long long ldc16)
 {
-    static bool smem_set = false;        /* GST x 24 KB dynamic shared memory is above the 48 KB default */
-    if (!smem_set) {
-        cudaError_t e = cudaFuncSetAttribute(k_gemm_tma<A_MN, B_MN>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             GST * GSTAGE);
+    static unsigned long long smem_set = 0;   /* per device: GST x 24 KB is above the 48 KB default */
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev >= 64 || !(smem_set >> dev & 1ull)) {
+        e = cudaFuncSetAttribute(k_gemm_tma<A_MN, B_MN>, cudaFuncAttributeMaxDynamicSharedMemorySize, GST * GSTAGE);
         if (e != cudaSuccess) return e;
-        smem_set = true;
+        if (dev < 64) smem_set |= 1ull << dev;
     }
     k_gemm_tma<A_MN, B_MN><<<grid, 128, GST * GSTAGE, st>>>(ma, mb, M, N, K, bias, mask, ldm, act, C, ldc, C16,
                                                            ldc16, g_gemm_spin, g_gemm_withhold);
@@ -450,11 +452,14 @@ extern "C" int gade_gemm_bf16(int32_t M, int32_t N, int32_t K, const void *A, in
             return GADE_OK;
         }
     }
-    static bool smem_set = false;        /* 2 x 24 KB dynamic shared memory is above the 48 KB default */
-    if (!smem_set) {
-        cudaError_t e = cudaFuncSetAttribute(k_gemm_ld, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * GSTAGE);
+    static unsigned long long smem_set = 0;   /* per device: 2 x 24 KB is above the 48 KB default */
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return lfail(GADE_ERR_CUDA, "gade_gemm_bf16", e);
+    if (dev >= 64 || !(smem_set >> dev & 1ull)) {
+        e = cudaFuncSetAttribute(k_gemm_ld, cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * GSTAGE);
         if (e != cudaSuccess) return lfail(GADE_ERR_CUDA, "gade_gemm_bf16", e);
-        smem_set = true;
+        if (dev < 64) smem_set |= 1ull << dev;
     }
     k_gemm_ld<<<grid, 128, 2 * GSTAGE, st>>>(M, N, K, (const bf16 *)A, sa0, sa1, (const bf16 *)B, sb0, sb1, bias,
                                              mask, ldm, act, C, ldc, (bf16 *)C16, ldc16, g_gemm_spin);
