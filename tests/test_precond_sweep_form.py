@@ -6,8 +6,10 @@ per lane so that lane i runs 33 products: row i of chunk 2p, then row 31-i
 of chunk 2p+1) and a chain through the neighbour blocks
 G_c = -Linv_c Lband_c (U: GU_c = -Uinv_c Uband_c).  This test restates the
 packing of pack_factors and the index arithmetic of the kernel in numpy, for
-band paddings 16 and 32 and for chunk counts with an unpaired last chunk and
-padded rows, and compares the result with a direct LU solve.  (The kernel
+band paddings 16 and 32, for chunk counts with an unpaired last chunk and
+padded rows, and for 4 and 8 warps per block row (with 8, two warps split a
+lane's 33 products at 17 and the chain's columns spread over 8 partial
+sums), and compares the result with a direct LU solve.  (The kernel
 itself is compared with the oracle's block LU on the GPU in
 tests/test_gpu_parity.py.)
 """
@@ -60,7 +62,32 @@ def _pack(L, U, B, bw, bwp):
     return nch, Bp, npair, TL, TU, GL, GU
 
 
-def _sweeps(b, nch, npair, TL, TU, GL, GU, bwp):
+def _triangle_part(T, buf, p, lane, c0, c1, has1, up, q0, q1):
+    """pc_triangle_part: products q0..q1-1 of one lane, split into the part
+    of row c0 (products up to sw) and the part of row c1."""
+    sw = 31 - lane if up else lane
+    acc = sav = 0
+    for q in range(q0, q1):
+        if not up:
+            src = 32 * c0 + q if q <= lane else (32 * c1 + q - lane - 1 if has1 else 0)
+        else:
+            src = 32 * c0 + lane + q if q <= 31 - lane else (32 * c1 + q - 1 if has1 else 0)
+        acc += T[p, q, lane] * buf[src]
+        if q == sw:
+            sav, acc = acc, 0
+    if sw >= q1:
+        return acc, 0
+    if sw >= q0:
+        return sav, acc
+    return 0, acc
+
+
+def _sweeps(b, nch, npair, TL, TU, GL, GU, bwp, nw=4):
+    """k_precond_tma with nw warps per block row: with 8, warps w and w + 4
+    split a pair's 33 products per lane (0-16, 17-32) and the chain's
+    columns are spread over 8 warps."""
+    halves = [(0, 33)] if nw == 4 else [(0, 17), (17, 33)]
+    cpw = bwp // nw
     buf = b.copy()
     for up in (0, 1):
         T, G = (TU, GU) if up else (TL, GL)
@@ -70,17 +97,10 @@ def _sweeps(b, nch, npair, TL, TU, GL, GU, bwp):
             out0 = np.zeros(32, complex)
             out1 = np.zeros(32, complex)
             for lane in range(32):
-                sw = 31 - lane if up else lane
-                acc = sav = 0
-                for q in range(33):
-                    if not up:
-                        src = 32 * c0 + q if q <= lane else (32 * c1 + q - lane - 1 if has1 else 0)
-                    else:
-                        src = 32 * c0 + lane + q if q <= 31 - lane else (32 * c1 + q - 1 if has1 else 0)
-                    acc += T[p, q, lane] * buf[src]
-                    if q == sw:
-                        sav, acc = acc, 0
-                out0[lane], out1[lane] = sav, acc
+                for q0, q1 in halves:
+                    a0, a1 = _triangle_part(T, buf, p, lane, c0, c1, has1, up, q0, q1)
+                    out0[lane] += a0
+                    out1[lane] += a1
             buf[32 * c0:32 * c0 + 32] = out0
             if has1:
                 buf[32 * c1:32 * c1 + 32] = out1[::-1]
@@ -88,12 +108,19 @@ def _sweeps(b, nch, npair, TL, TU, GL, GU, bwp):
             if (up and c == nch - 1) or (not up and c == 0):
                 continue
             base = 32 * (c + 1) if up else 32 * c - bwp
-            buf[32 * c:32 * c + 32] += G[c].T @ buf[base:base + bwp]
+            parts = []
+            for w in range(nw):
+                t = buf[32 * c:32 * c + 32].copy() if w == 0 else np.zeros(32, complex)
+                for col in range(w * cpw, (w + 1) * cpw):
+                    t += G[c, col] * buf[base + col]
+                parts.append(t)
+            buf[32 * c:32 * c + 32] = sum(parts)
     return buf
 
 
+@pytest.mark.parametrize("nw", [4, 8])
 @pytest.mark.parametrize("B,bw,bwp", [(130, 15, 16), (96, 20, 32), (33, 3, 16), (200, 31, 32)])
-def test_sweep_form_solves_lu(B, bw, bwp):
+def test_sweep_form_solves_lu(B, bw, bwp, nw):
     rng = np.random.default_rng(B + bw)
     A = np.zeros((B, B), complex)
     for r in range(B):
@@ -111,7 +138,7 @@ def test_sweep_form_solves_lu(B, bw, bwp):
     nch, Bp, npair, TL, TU, GL, GU = _pack(L, U, B, bw, bwp)
     b = np.zeros(Bp, complex)
     b[:B] = rng.standard_normal(B) + 1j * rng.standard_normal(B)
-    x = _sweeps(b, nch, npair, TL, TU, GL, GU, bwp)
+    x = _sweeps(b, nch, npair, TL, TU, GL, GU, bwp, nw)
     ref = np.linalg.solve(U, np.linalg.solve(L, b[:B]))
     assert np.abs(x[:B] - ref).max() < 1e-13 * np.abs(ref).max()
     assert not np.any(x[B:])
